@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Throughput of the 2048^2 split-step channel Monte Carlo on GB300.
+
+Workload (config 2 of the reference's advanced channel): RectGrid 2048 x 2048,
+delta 1.5 mm; Gaussian beam 808 nm, w0 0.12 m, collimated; 50 km path with 5
+sparse-spectrum screens (MVK Cn2 5e-16, l0 6 mm, L0 1 km, 1024 log-polar
+annuli from 1/15 km^-1 to 2/l0); CirclePupil 0.2 m.  One step = one batch of
+256 seeded realisations through the engine (screens, propagation, pupil and
+moments).  Synthetic inputs: spectra drawn on the host from numpy's
+default_rng([seed, realisation]) exactly as the reference forms them.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "2048² channel samples/s, batched vs plain on GPU; surrogate PDT/s at KS≤0.02"
+UNIT = "samples/s"
+
+WORKLOAD = dict(N=2048, delta=1.5e-3, wvl=808e-9, w0=0.12, F0=float("inf"), length=50e3, count=5,
+                Cn2=5e-16, l0=6e-3, L0=1e3, points=1024, f_min=1 / 1e3 / 15, f_max=2 / 6e-3,
+                pupil_radius=0.2)
+WORKLOAD_NAME = ("config-2 advanced channel: 2048^2 grid, delta 1.5 mm, 808 nm, w0 0.12 m, 50 km, "
+                 "5 SS screens x 1024 annuli, MVK Cn2 5e-16, pupil 0.2 m")
+
+
+def positions(length, count):
+    return (np.arange(count) + 0.5) * (length / count)
+
+
+def base_and_psd():
+    from pyatmosphere_gb300.engine.spectra import annulus_psd
+    from pyatmosphere_gb300.theory.models import MVKModel
+    w = WORKLOAD
+    base = np.exp(np.linspace(np.log(w["f_min"]), np.log(w["f_max"]), w["points"], dtype=np.float32))
+    model = MVKModel(Cn2=w["Cn2"], l0=w["l0"], L0=w["L0"])
+    psd = annulus_psd(base, model.psd_phi_f, 2 * np.pi / w["wvl"], w["length"] / w["count"])
+    return base, psd
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's restatement of the reference numpy path
+# (reference precision), timed on this host's cores
+# ---------------------------------------------------------------------------
+def cpu_realisations(n_real: int, seed: int = 4242):
+    from oracle import atm_oracle as o
+    w = WORKLOAD
+    spec = o.ChannelSpec(N=w["N"], delta=w["delta"], wvl=w["wvl"], w0=w["w0"], F0=w["F0"], length=w["length"],
+                         count=w["count"], Cn2=w["Cn2"], l0=w["l0"], L0=w["L0"], points=w["points"],
+                         f_min=w["f_min"], f_max=w["f_max"], pupil_radius=w["pupil_radius"])
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    rho, theta, value = o.draw_spectra(seed, range(n_real), spec.count, base, psd)
+    t = time.perf_counter()
+    o.simulate(spec, rho, theta, value, prec="ref")
+    return n_real / (time.perf_counter() - t)
+
+
+def cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    for _ in range(args.warmup):
+        cpu_realisations(1, seed=1)
+    t = time.perf_counter()
+    for k in range(args.steps):
+        cpu_realisations(1, seed=100 + k)
+    el = time.perf_counter() - t
+    val = args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32 (numpy, reference precision)",
+        "data": "synthetic (seeded spectra, reference's own formulas)",
+        "config": {"workload": WORKLOAD_NAME, "realisations_per_step": 1},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores(), "kind": "port",
+                         "sample": f"{args.steps} single-realisation steps of the 2048^2 channel, numpy/OpenBLAS "
+                                   "restatement of the reference path in its own precision"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GB300 engine
+# ---------------------------------------------------------------------------
+def run_gb300(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    from pyatmosphere_gb300.engine import EnginePlan
+    from pyatmosphere_gb300.engine.plan import fma_peak_tflops
+    from pyatmosphere_gb300.engine.spectra import draw_spectra
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    w = WORKLOAD
+    B = args.batch
+    base, psd = base_and_psd()
+    pos = positions(w["length"], w["count"])
+    plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
+                      pupils=[(w["pupil_radius"],)], batch=B, device=dev)
+    n_steps = args.warmup + args.steps
+    # distinct seeded inputs per step (weak scaling: each rank its own realisations)
+    host = []
+    for s in range(n_steps):
+        first = (rank * n_steps + s) * B
+        host.append(draw_spectra(args.seed, range(first, first + B), w["count"], base, psd))
+    pinned = [[torch.from_numpy(a).pin_memory() for a in h] for h in host]
+    devin = [[t.to(dev) for t in p] for p in pinned]
+    out = torch.empty((n_steps, B, plan.n_out), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for s in range(args.warmup):
+        plan.run(*devin[s], out=out[s])
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region, kernels bracketed by CUDA events ----
+    launches = plan.info["launches_per_run"] * args.steps
+    plan.profile_begin(launches + 8)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for s in range(args.warmup, n_steps):
+            plan.run(*devin[s], out=out[s])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    prof = plan.profile_end()
+    ms = e0.elapsed_time(e1)
+    t_max = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    ms = float(t_max.item())
+    value = B * args.steps * world / (ms * 1e-3)
+
+    # ---- end to end through the C ABI: pinned host spectra in, measures out ----
+    meas_host = torch.empty((B, plan.n_out), dtype=torch.float64).pin_memory()
+    scratch = [torch.empty_like(t) for t in devin[0]]
+    h2d = sum(t.numel() * t.element_size() for t in pinned[0])
+    d2h = meas_host.numel() * meas_host.element_size()
+    barrier()
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for s in range(args.warmup, n_steps):
+        for d_, h_ in zip(scratch, pinned[s]):
+            d_.copy_(h_, non_blocking=True)
+        m = plan.run(*scratch, out=out[s])
+        meas_host.copy_(m, non_blocking=True)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = e2.elapsed_time(e3)
+    te = torch.tensor([ms_e2e], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = B * args.steps * world / (float(te.item()) * 1e-3)
+
+    # ---- plain form: one realisation per launch sequence, no batching ----
+    plain = None
+    if args.plain > 0 and rank == 0:
+        p1 = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
+                        pupils=[(w["pupil_radius"],)], batch=1, device=dev)
+        one = [t[:1].contiguous() for t in devin[0]]
+        for _ in range(2):
+            p1.run(*one)
+        torch.cuda.synchronize()
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e4.record(stream)
+        for i in range(args.plain):
+            p1.run(*[t[i:i + 1].contiguous() for t in devin[args.warmup]])
+        e5.record(stream)
+        torch.cuda.synchronize()
+        plain = args.plain / (e4.elapsed_time(e5) * 1e-3)
+        p1.close()
+
+    # ---- roofline of the dominant kernel, measured in the timed region ----
+    N, n = w["N"], w["count"]
+    K = plan.info["gemm_k"]
+    work = {  # algorithmic work per launch of a B-realisation batch
+        "screen_gemm": ("fp32", 2.0 * N * N * K * B, "TFLOP/s"),
+        "col_pass": ("hbm", 16.0 * N * N * B, "GB/s"),
+        # n+1 row launches move 8 (write) + 4 (phi) + (n-1)(16 + 4) + 8 (read) bytes per pixel
+        "row_pass": ("hbm", (12.0 + 20.0 * (n - 1) + 8.0) / (n + 1) * N * N * B, "GB/s"),
+        "screen_table": ("hbm", 2.0 * (plan.info["gemm_k"]) * N * 4.0 * B, "GB/s"),
+    }
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            mp = json.load(f)
+        peaks["hbm"] = (float(mp["hbm_gbs"]), "measured")
+    except (OSError, KeyError, ValueError):
+        peaks["hbm"] = (6800.0, "fallback")
+    peaks["fp32"] = (fma_peak_tflops(dev), "measured (FMA probe)")
+    kernels = {}
+    for kname, st in prof.items():
+        if st["launches"] == 0:
+            continue
+        avg_ms = st["ms"] / st["launches"]
+        entry = {"launches": st["launches"], "total_ms": st["ms"], "avg_ms": avg_ms,
+                 "share": st["ms"] / max(1e-9, sum(v["ms"] for v in prof.values()))}
+        if kname in work:
+            bound, amount, unit = work[kname]
+            achieved = amount / (avg_ms * 1e-3) / (1e12 if unit == "TFLOP/s" else 1e9)
+            pk, src = peaks[bound]
+            entry.update({"bound": bound, "achieved": achieved, "peak": pk, "unit": unit,
+                          "frac": achieved / pk, "peak_source": src})
+        kernels[kname] = entry
+    dom = max(kernels, key=lambda k: kernels[k]["total_ms"])
+    hbm_dom = max((k for k in kernels if kernels[k].get("bound") == "hbm"), key=lambda k: kernels[k]["total_ms"])
+
+    def roof(k):
+        e = kernels[k]
+        return {"kernel": k, "bound": e["bound"], "achieved": e["achieved"], "peak": e["peak"], "unit": e["unit"],
+                "frac": e["frac"], "traffic": None, "peak_source": e["peak_source"]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        n_cpu = args.cpu_realisations
+        v = cpu_realisations(n_cpu)
+        cpu = {"value": v, "unit": UNIT, "cores": cores(), "kind": "port",
+               "sample": f"{n_cpu} realisations of the same 2048^2 channel through the numpy restatement of "
+                         "the reference path in its own precision (OpenBLAS threads = cores; numpy FFT single-threaded)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 (complex64 field, FP64 phase arguments and accumulators)",
+            "data": "synthetic (seeded spectra, reference formulas)",
+            "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B,
+                       "l2": "inputs larger than L2 (field batch 8.6 GB per step)", "gemm_k": K,
+                       "low_annuli": plan.info["low_annuli"], "cheb_terms": plan.info["cheb_terms"]},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "plain": {"value": plain, "unit": UNIT, "realisations": args.plain,
+                      "batched_over_plain": (value / world / plain) if plain else None},
+            "gpu_launches": sum(v["launches"] for v in prof.values()),
+            "roofline": roof(dom),
+            "roofline_hbm": roof(hbm_dom),
+            "kernels": kernels,
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    plan.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--plain", type=int, default=16, help="realisations timed in the plain form (0: skip)")
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-realisations", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    try:
+        return run_gb300(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

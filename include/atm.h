@@ -1,0 +1,184 @@
+/*
+ * atm.h -- C ABI of the GB300 split-step beam-propagation engine (libatm.so).
+ *
+ * The engine replaces pyAtmosphere's numpy/cupy Monte-Carlo path:
+ *   sparse-spectrum phase screens  -> atm_screen / inside atm_run
+ *   angular-spectrum vacuum steps  -> atm_vacuum / inside atm_run
+ *   pupil + intensity moments      -> inside atm_run (measures_out)
+ * Python binds it with ctypes (pyatmosphere_gb300/engine/_lib.py); any other
+ * host language binds the same plain-C signatures.
+ *
+ * Conventions
+ *   - Every array argument of atm_run / atm_screen / atm_vacuum is a DEVICE
+ *     pointer on the device that was current at atm_plan_create.  Descriptor
+ *     arrays (positions, radii, f_base) are HOST pointers, read during
+ *     atm_plan_create only.
+ *   - complex64 arrays are interleaved (re, im) float pairs, passed as void*.
+ *   - Layouts are row-major; a field is [batch][N][N] with row index = y
+ *     (top = -N/2 * delta), column = x, as RectGrid.get_y / get_x.
+ *   - Spectra are [batch][n_screens][P]: rho, theta (float32), value
+ *     (complex64), exactly PolarDiscreteFunction(rho, theta, value) of each
+ *     SSPhaseScreen (phase_screens.py:98-103).
+ *   - Calls are stream-ordered on `stream` (a cudaStream_t, NULL = legacy
+ *     default stream) and return before the GPU work ends.  A plan serves one
+ *     stream at a time; distinct plans are independent.
+ *   - Every call returns ATM_OK (0) or a negative status; atm_last_error()
+ *     gives the message (per host thread).  Nothing is printed, nothing exits.
+ */
+#ifndef ATM_H
+#define ATM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ATM_ABI_VERSION 1
+
+#define ATM_OK 0
+#define ATM_ERR_INVALID (-1)     /* bad argument */
+#define ATM_ERR_UNSUPPORTED (-2) /* e.g. N not a power of two in [128, 4096] */
+#define ATM_ERR_CUDA (-3)        /* CUDA runtime error (message has details) */
+#define ATM_ERR_NOMEM (-4)       /* device allocation failed */
+
+#define ATM_SOURCE_GAUSSIAN 0    /* GaussianSource (sources.py:21-23) */
+#define ATM_SOURCE_PLANE 1       /* PlaneSource (sources.py:16-18) */
+
+#define ATM_MAX_PUPILS 8
+
+/* per-realisation doubles in measures_out (slot index) */
+#define ATM_OUT_ETA_TOTAL 0      /* measures.eta(pupil=False)      measures.py:7-8   */
+#define ATM_OUT_MEAN_X 1         /* measures.mean_x                measures.py:11-13 */
+#define ATM_OUT_MEAN_Y 2         /* measures.mean_y  (-y weighted) measures.py:16-18 */
+#define ATM_OUT_MEAN_X2 3        /* measures.mean_x2               measures.py:26-28 */
+#define ATM_OUT_MEAN_XY 4        /* measures.mean_xy (-x y)        measures.py:31-33 */
+#define ATM_OUT_MEAN_Y2 5        /* measures.mean_y2               measures.py:36-38 */
+#define ATM_OUT_MEAN_X2_R 6      /* BeamResult.mean_x2_r           simulations/beam.py:26-33 */
+#define ATM_OUT_I_CENTER 7       /* |u|^2 at the origin pixel      simulations/si.py:11-12 */
+#define ATM_OUT_PUPIL0 8         /* eta through pupil p (slot 8+p), then tracked pupils */
+
+typedef struct AtmPlan AtmPlan;
+
+typedef struct AtmChannelDesc {
+  int32_t abi_version;        /* ATM_ABI_VERSION */
+  int32_t resolution;         /* RectGrid.resolution N: power of two in [128, 4096] */
+  double delta;               /* RectGrid.delta [m] */
+  int32_t source_kind;        /* ATM_SOURCE_* */
+  double wvl, w0, F0;         /* GaussianSource(wvl, w0, F0); F0 = +/-inf: collimated */
+  int32_t n_screens;          /* screens on the path (0: VacuumPath) */
+  const double* positions;    /* [n_screens] PhaseScreensPath.positions [m] */
+  double length;              /* path length [m] */
+  double losses_db;           /* AbstractPath.losses_db */
+  int32_t path_output_loss;   /* 1: Channel.run (loss applied once more on exit,
+                                 pathes.py:23-24); 0: Channel.generator */
+  int32_t points;             /* RandLogPolarGrid.points P */
+  const float* f_base;        /* [P] RandLogPolarGrid.base (annulus outer radii) */
+  double shift_x, shift_y;    /* SSPhaseScreen.generate_phase_screen shift [m] */
+  int32_t n_pupils;           /* fixed CirclePupils, <= ATM_MAX_PUPILS */
+  const double* pupil_radius; /* [n_pupils] */
+  const double* pupil_shift_x;/* [n_pupils] CirclePupil.get_pupil shift (may be NULL) */
+  const double* pupil_shift_y;/* [n_pupils] (may be NULL) */
+  int32_t n_tracked;          /* pupils centred on each realisation's centroid */
+  const double* tracked_radius;/* [n_tracked] (TrackedPDTResult, simulations/pdt.py:51-66) */
+  int32_t batch;              /* maximum realisations per atm_run */
+  double cheb_cut;            /* low-frequency block: annuli below cheb_cut/(N delta); 0 = 4 */
+  int32_t col_tile;           /* column-pass tile (columns per CTA); 0 = default */
+  int32_t flags;              /* reserved, 0 */
+} AtmChannelDesc;
+
+typedef struct AtmPlanInfo {
+  int32_t n_out;              /* doubles per realisation in measures_out */
+  int32_t low_annuli;         /* annuli folded into the Chebyshev block */
+  int32_t cheb_terms;         /* Chebyshev terms per axis */
+  int32_t gemm_k;             /* inner dimension of the screen GEMM */
+  int64_t workspace_bytes;    /* device memory held by the plan */
+  int32_t launches_per_run;   /* kernel launches of one atm_run (without tracked/field extras) */
+  int32_t row_parts;          /* row-pass CTAs per realisation */
+} AtmPlanInfo;
+
+/* ABI version of the loaded library (ATM_ABI_VERSION). */
+int atm_abi_version(void);
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char* atm_last_error(void);
+
+/* Builds a plan for one channel geometry and batch size: validates the
+ * descriptor, picks the low-frequency split and GEMM shape, uploads the
+ * source / transfer-function tables and allocates the workspace.
+ * Replaces the object graph built by Channel(...) (channels.py:17-29) with
+ * IdenticalPhaseScreensPath / PhaseScreensPath (pathes.py:43-95),
+ * GaussianSource (sources.py:21-23), RectGrid (grids.py:7-85),
+ * RandLogPolarGrid (grids.py:88-119) and CirclePupil (pupils.py:4-13). */
+int atm_plan_create(const AtmChannelDesc* desc, AtmPlan** plan);
+
+/* Frees the plan and its workspace (waits for the device). */
+int atm_plan_destroy(AtmPlan* plan);
+
+/* Sizes chosen by atm_plan_create. */
+int atm_plan_info(const AtmPlan* plan, AtmPlanInfo* info);
+
+/* Runs `batch` realisations of the channel with the injected spectra.
+ * Replaces Channel.run(pupil=False) (channels.py:31-35) driving
+ * PhaseScreensPath.generator (pathes.py:61-75) with SSPhaseScreen screens,
+ * followed by measures.* (measures.py:1-38), BeamResult.mean_x2_r
+ * (simulations/beam.py:26-33) and PDTResult / TrackedPDTResult eta
+ * (simulations/pdt.py:15-26, 51-66).
+ *   measures_out   [batch][n_out] doubles (required)
+ *   field_out      [batch][N][N] complex64 final field (nullable)
+ *   mean_intensity [N][N] float32; the intensity of every realisation is
+ *                  ADDED to it (nullable; the caller zeroes and divides). */
+int atm_run(AtmPlan* plan, const float* rho, const float* theta, const void* value, int32_t batch,
+            double* measures_out, void* field_out, float* mean_intensity, void* stream);
+
+/* Synthesises screen `screen` of every realisation in the batch.
+ * Replaces SSPhaseScreen.generate (phase_screens.py:25-28, 108-136).
+ *   phi_out    [batch][N][N] float32 screen (nullable)
+ *   phasor_out [batch][N][N] complex64 exp(-i phi) as applied on the path
+ *              (pathes.py:72-73; nullable) */
+int atm_screen(AtmPlan* plan, const float* rho, const float* theta, const void* value, int32_t batch,
+               int32_t screen, float* phi_out, void* phasor_out, void* stream);
+
+/* One angular-spectrum vacuum step of length dz, in place on a spatial
+ * field [batch][N][N] complex64.  Replaces VacuumPath.output /
+ * vacuum_propagation (pathes.py:27-40, theory/vacuum.py:5-7,
+ * utils.py:42-50); dz <= 0 leaves the field unchanged. */
+int atm_vacuum(AtmPlan* plan, void* field, int32_t batch, double dz, void* stream);
+
+/* Measures of given spatial fields [batch][N][N] complex64 into
+ * measures_out [batch][n_out] (same slots as atm_run).  Replaces calling
+ * measures.eta / mean_x / mean_y / mean_x2 / mean_xy / mean_y2
+ * (measures.py:1-38) on an output field, CirclePupil.output + eta
+ * (pupils.py:12-13) and BeamResult.mean_x2_r (simulations/beam.py:26-33). */
+int atm_measures(AtmPlan* plan, const void* field, int32_t batch, double* measures_out, void* stream);
+
+/* Launch categories reported by atm_profile_end. */
+#define ATM_KIND_SCREEN_PREP 0
+#define ATM_KIND_SCREEN_TABLE 1
+#define ATM_KIND_SCREEN_GEMM 2
+#define ATM_KIND_ROW_PASS 3
+#define ATM_KIND_COL_PASS 4
+#define ATM_KIND_FINALIZE 5
+#define ATM_KIND_TRACKED 6
+#define ATM_KIND_COUNT 7
+
+/* Starts recording a CUDA event pair around each kernel launch of this plan
+ * (at most max_launches launches), on the stream the kernel runs on.  No
+ * reference counterpart: this is the engine's own per-kernel timer. */
+int atm_profile_begin(AtmPlan* plan, int32_t max_launches);
+
+/* Waits for the recorded launches and returns, per ATM_KIND_*, the summed
+ * device milliseconds and the number of launches; stops recording. */
+int atm_profile_end(AtmPlan* plan, double* ms_by_kind, int32_t* launches_by_kind, int32_t n_kinds);
+
+/* FP32 FMA throughput probe: runs `blocks` x 256 threads of independent FMA
+ * chains (`iters` iterations of 8 chains) on `stream` and returns the device
+ * time in *ms; FLOPs = blocks * 256 * iters * 16.  No reference counterpart:
+ * the roofline denominator for the FP32 screen GEMM. */
+int atm_fma_probe(int32_t blocks, int32_t iters, double* ms, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATM_H */

@@ -1,0 +1,755 @@
+// Plan construction and the extern "C" entry points of libatm.so
+// (declared in include/atm.h).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/atm.h"
+#include "atm_common.cuh"
+#include "atm_internal.h"
+
+using cd = std::complex<double>;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define ATM_CUDA(call)                                                                       \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail(ATM_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                                 \
+  } while (0)
+
+constexpr double kPi = 3.14159265358979323846;
+
+// iterative radix-2 FFT, FP64, twiddles from std::polar (no recurrence)
+void fft_host(std::vector<cd>& a, int sign) {
+  const int n = (int)a.size();
+  for (int i = 1, j = 0; i < n; ++i) {
+    int bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(a[i], a[j]);
+  }
+  for (int len = 2; len <= n; len <<= 1) {
+    const double ang = sign * 2.0 * kPi / len;
+    for (int k = 0; k < len / 2; ++k) {
+      const cd w = std::polar(1.0, ang * k);
+      for (int i = 0; i < n; i += len) {
+        const cd u = a[i + k], v = a[i + k + len / 2] * w;
+        a[i + k] = u + v;
+        a[i + k + len / 2] = u - v;
+      }
+    }
+  }
+}
+
+// exp(-i pi dz lambda f^2) on the unshifted frequency axis f_k = k df
+// (k - N for k >= N/2), df = 1/(N delta), as theory/vacuum.py:7 evaluates it
+// (argument ((pi dz) (2 pi / k)) f^2 in FP64)
+std::vector<cd> transfer_1d(int N, double delta, double kw, double dz) {
+  std::vector<cd> h(N);
+  const double df = 1.0 / (N * delta);
+  const double c1 = (kPi * dz) * (2.0 * kPi / kw);
+  for (int k = 0; k < N; ++k) {
+    const double f = (double)(k < N / 2 ? k : k - N) * df;
+    const double arg = c1 * (f * f);
+    h[k] = cd(std::cos(arg), -std::sin(arg));
+  }
+  return h;
+}
+
+cd global_phase(double kw, double dz) {
+  const double ph = kw * dz;
+  return cd(std::cos(ph), std::sin(ph));
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+int dev_alloc(DevBuf& b, size_t bytes, std::vector<DevBuf*>& all) {
+  b.bytes = bytes;
+  all.push_back(&b);
+  if (bytes == 0) return ATM_OK;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ATM_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return ATM_OK;
+}
+
+template <class T>
+int upload(DevBuf& b, const std::vector<T>& v) {
+  ATM_CUDA(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return ATM_OK;
+}
+
+std::vector<float2> to_c64(const std::vector<cd>& v) {
+  std::vector<float2> o(v.size());
+  for (size_t i = 0; i < v.size(); ++i) o[i] = make_float2((float)v[i].real(), (float)v[i].imag());
+  return o;
+}
+
+}  // namespace
+
+struct AtmPlan {
+  int device = 0;
+  int N = 0, n = 0, P = 0, B = 0, n_pupils = 0, n_tracked = 0;
+  double delta = 0, wvl = 0, w0 = 0, F0 = 0, length = 0, losses_db = 0, kw = 0, sx = 0, sy = 0;
+  int path_output_loss = 0, source_kind = 0, col_tile = 0;
+  int P_L = 0, D = 2, P_H = 0, KH = 0, KC = 0;
+  int rows = 1, n_parts = 0, n_meas = 0, n_out = 0;
+  std::vector<double> positions, dz;      // dz[0..n]
+  std::vector<float> loss;                // per screen amplitude factor
+  float final_loss = 1.f;
+  std::vector<double> tracked_radius;
+
+  // profiling: event pairs around launches (atm_profile_begin / end)
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> ev_kind;
+  int ev_used = 0, ev_cap = 0;
+  bool profiling = false;
+
+  DevBuf field, phi, At, Bt, Ach, ht, Py, Px, Gy, Hx, tw, ay, ax, hy, hx, vac_h, partials, center, pupil_rows,
+      intensity, tracked_r;
+  std::vector<DevBuf*> bufs;
+  int64_t bytes() const {
+    int64_t s = 0;
+    for (auto* b : bufs) s += (int64_t)b->bytes;
+    return s;
+  }
+  ~AtmPlan() {
+    for (auto* b : bufs)
+      if (b->p) cudaFree(b->p);
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+};
+
+namespace {
+
+int plan_tables(AtmPlan* pl, const AtmChannelDesc* d) {
+  const int N = pl->N;
+  // twiddles exp(-2 pi i n / N)
+  std::vector<cd> tw(N);
+  for (int i = 0; i < N; ++i) tw[i] = std::polar(1.0, -2.0 * kPi * i / N);
+  if (int rc = upload(pl->tw, to_c64(tw))) return rc;
+
+  // source rows g(x_j), x_j = (j - N/2) delta; u0(y, x) = g(y) g(x)
+  std::vector<cd> g(N);
+  for (int j = 0; j < N; ++j) {
+    if (pl->source_kind == ATM_SOURCE_PLANE) {
+      g[j] = 1.0;
+    } else {
+      const double x = (double)(j - N / 2) * pl->delta;
+      const cd c(1.0 / (pl->w0 * pl->w0), std::isinf(pl->F0) ? 0.0 : 2.0 * kPi / pl->wvl / 2.0 / pl->F0);
+      g[j] = std::pow(2.0 / kPi, 0.25) / std::sqrt(pl->w0) * std::exp(-c * (x * x));
+    }
+  }
+  // first vacuum segment is separable: a = IFFT(h FFT(g))
+  std::vector<cd> a = g, b;
+  const double dz0 = pl->dz[0];
+  cd gph = 1.0;
+  if (dz0 > 0) {
+    fft_host(a, -1);
+    std::vector<cd> h = transfer_1d(N, pl->delta, pl->kw, dz0);
+    for (int k = 0; k < N; ++k) a[k] *= h[k] / (double)N;
+    fft_host(a, +1);
+    gph = global_phase(pl->kw, dz0);
+  }
+  b = a;
+  for (auto& v : a) v *= gph;
+  if (int rc = upload(pl->ay, to_c64(a))) return rc;
+  if (int rc = upload(pl->ax, to_c64(b))) return rc;
+
+  // transfer functions of the steps after each screen: [n][N] (y incl. phase and 1/N^2)
+  std::vector<float2> hyv((size_t)std::max(pl->n, 1) * N, make_float2(0.f, 0.f)), hxv = hyv;
+  for (int i = 1; i <= pl->n; ++i) {
+    const double dzi = pl->dz[i];
+    if (!(dzi > 0)) continue;
+    std::vector<cd> h = transfer_1d(N, pl->delta, pl->kw, dzi);
+    const cd ph = global_phase(pl->kw, dzi) / ((double)N * (double)N);
+    for (int k = 0; k < N; ++k) {
+      const cd y = ph * h[k];
+      hyv[(size_t)(i - 1) * N + k] = make_float2((float)y.real(), (float)y.imag());
+      hxv[(size_t)(i - 1) * N + k] = make_float2((float)h[k].real(), (float)h[k].imag());
+    }
+  }
+  if (int rc = upload(pl->hy, hyv)) return rc;
+  if (int rc = upload(pl->hx, hxv)) return rc;
+
+  // Chebyshev rows of A^T: T_e(t_y), e = 1..D-1, padded to KC rows
+  if (pl->KC > 0) {
+    std::vector<float> ach((size_t)pl->KC * N, 0.f);
+    const double half = 0.5 * (N - 1);
+    for (int e = 1; e < pl->D; ++e)
+      for (int j = 0; j < N; ++j) {
+        const double t = std::min(1.0, std::max(-1.0, ((double)j - half) / half));
+        ach[(size_t)(e - 1) * N + j] = (float)std::cos(e * std::acos(t));
+      }
+    if (int rc = upload(pl->Ach, ach)) return rc;
+  }
+
+  // pupil masks as inclusive column intervals per row, FP64 predicate
+  // (x - sx)^2 + (y + sy)^2 <= R^2 (pupils.py:8-10)
+  if (pl->n_pupils > 0) {
+    std::vector<int2> rows((size_t)pl->n_pupils * N);
+    for (int p = 0; p < pl->n_pupils; ++p) {
+      const double R = d->pupil_radius[p];
+      const double psx = d->pupil_shift_x ? d->pupil_shift_x[p] : 0.0;
+      const double psy = d->pupil_shift_y ? d->pupil_shift_y[p] : 0.0;
+      for (int i = 0; i < N; ++i) {
+        const double y = (double)(i - N / 2) * pl->delta;
+        auto inside = [&](int j) {
+          const double x = (double)(j - N / 2) * pl->delta;
+          return (x - psx) * (x - psx) + (y + psy) * (y + psy) <= R * R;
+        };
+        int jc = (int)std::lround(psx / pl->delta) + N / 2;
+        jc = std::min(N - 1, std::max(0, jc));
+        int2 iv = make_int2(1, 0);
+        if (inside(jc)) {
+          int lo = 0, hi = jc;  // first inside in [0, jc]
+          while (lo < hi) {
+            const int m = (lo + hi) / 2;
+            if (inside(m)) hi = m; else lo = m + 1;
+          }
+          iv.x = lo;
+          lo = jc;
+          hi = N - 1;  // last inside in [jc, N-1]
+          while (lo < hi) {
+            const int m = (lo + hi + 1) / 2;
+            if (inside(m)) lo = m; else hi = m - 1;
+          }
+          iv.y = lo;
+        }
+        rows[(size_t)p * N + i] = iv;
+      }
+    }
+    if (int rc = upload(pl->pupil_rows, rows)) return rc;
+  }
+  if (pl->n_tracked > 0) {
+    if (int rc = upload(pl->tracked_r, pl->tracked_radius)) return rc;
+  }
+  return ATM_OK;
+}
+
+int choose_low_block(AtmPlan* pl, const AtmChannelDesc* d) {
+  double cut = d->cheb_cut > 0 ? d->cheb_cut : 4.0;
+  const double xh = 0.5 * (pl->N - 1) * pl->delta;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    const double fcut = cut / (pl->N * pl->delta);
+    int PL = 0;
+    while (PL < pl->P && (double)d->f_base[PL] <= fcut) ++PL;
+    const double amax = 2.0 * kPi * fcut * xh;
+    // smallest D with 2 |J_n(amax)| < 1e-10 for all n >= D (checked to D + 16)
+    double J[96];
+    atm::bessel_j(amax, 96, J);
+    int D = 2;
+    for (int n = 95; n >= 1; --n)
+      if (2.0 * std::fabs(J[n]) >= 1e-10) {
+        D = n + 1;
+        break;
+      }
+    D = std::max(D, 2);
+    if (D <= 64) {
+      pl->P_L = PL;
+      pl->D = PL > 0 ? D : 2;
+      return ATM_OK;
+    }
+    cut *= 0.5;
+  }
+  return fail(ATM_ERR_UNSUPPORTED, "could not fit the low-frequency block into 64 Chebyshev terms");
+}
+
+int validate(const AtmChannelDesc* d) {
+  if (!d) return fail(ATM_ERR_INVALID, "descriptor is NULL");
+  if (d->abi_version != ATM_ABI_VERSION)
+    return fail(ATM_ERR_INVALID, "descriptor abi_version %d, library %d", d->abi_version, ATM_ABI_VERSION);
+  if (!atm::supported_n(d->resolution))
+    return fail(ATM_ERR_UNSUPPORTED, "resolution %d unsupported: need a power of two in [128, 4096]",
+                d->resolution);
+  if (!(d->delta > 0)) return fail(ATM_ERR_INVALID, "delta must be > 0");
+  if (d->source_kind != ATM_SOURCE_GAUSSIAN && d->source_kind != ATM_SOURCE_PLANE)
+    return fail(ATM_ERR_INVALID, "unknown source_kind %d", d->source_kind);
+  if (d->source_kind == ATM_SOURCE_GAUSSIAN && !(d->w0 > 0)) return fail(ATM_ERR_INVALID, "w0 must be > 0");
+  if (!(d->wvl > 0)) return fail(ATM_ERR_INVALID, "wvl must be > 0");
+  if (d->n_screens < 0 || d->n_screens > 256) return fail(ATM_ERR_INVALID, "n_screens %d out of range", d->n_screens);
+  if (d->n_screens > 0) {
+    if (!d->positions) return fail(ATM_ERR_INVALID, "positions is NULL");
+    if (d->points < 1 || !d->f_base) return fail(ATM_ERR_INVALID, "points / f_base missing");
+  }
+  if (d->n_pupils < 0 || d->n_pupils > ATM_MAX_PUPILS)
+    return fail(ATM_ERR_INVALID, "n_pupils %d out of range [0, %d]", d->n_pupils, ATM_MAX_PUPILS);
+  if (d->n_pupils > 0 && !d->pupil_radius) return fail(ATM_ERR_INVALID, "pupil_radius is NULL");
+  if (d->n_tracked < 0 || d->n_pupils + d->n_tracked > 32) return fail(ATM_ERR_INVALID, "n_tracked out of range");
+  if (d->n_tracked > 0 && !d->tracked_radius) return fail(ATM_ERR_INVALID, "tracked_radius is NULL");
+  if (d->batch < 1 || d->batch > 65535) return fail(ATM_ERR_INVALID, "batch %d out of range", d->batch);
+  return ATM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int atm_abi_version(void) { return ATM_ABI_VERSION; }
+
+const char* atm_last_error(void) { return g_err.c_str(); }
+
+int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
+  if (!out) return fail(ATM_ERR_INVALID, "plan output pointer is NULL");
+  *out = nullptr;
+  if (int rc = validate(d)) return rc;
+  AtmPlan* pl = new AtmPlan();
+  cudaGetDevice(&pl->device);
+  pl->N = d->resolution;
+  pl->n = d->n_screens;
+  pl->P = d->n_screens > 0 ? d->points : 0;
+  pl->B = d->batch;
+  pl->delta = d->delta;
+  pl->wvl = d->wvl;
+  pl->w0 = d->w0;
+  pl->F0 = d->F0;
+  pl->length = d->length;
+  pl->losses_db = d->losses_db;
+  pl->kw = 2.0 * kPi / d->wvl;
+  pl->sx = d->shift_x;
+  pl->sy = d->shift_y;
+  pl->path_output_loss = d->path_output_loss;
+  pl->source_kind = d->source_kind;
+  pl->n_pupils = d->n_pupils;
+  pl->n_tracked = d->n_tracked;
+  pl->col_tile = d->col_tile > 0 ? d->col_tile : atm::col_tile_default(pl->N);
+  for (int i = 0; i < d->n_tracked; ++i) pl->tracked_radius.push_back(d->tracked_radius[i]);
+  // steps: dz[0] = z_0, dz[i] = z_i - z_{i-1}, dz[n] = L - z_{n-1} (pathes.py:68-75)
+  if (pl->n > 0) {
+    pl->positions.assign(d->positions, d->positions + pl->n);
+    pl->dz.push_back(pl->positions[0]);
+    for (int i = 1; i < pl->n; ++i) pl->dz.push_back(pl->positions[i] - pl->positions[i - 1]);
+    pl->dz.push_back(pl->length - pl->positions[pl->n - 1]);
+  } else {
+    pl->dz.push_back(pl->length);
+  }
+  // losses: a step whose share is 0 falls back to the full path loss
+  // (append_losses: `losses_db or self.losses_db`, pathes.py:19-21)
+  for (int i = 0; i < pl->n; ++i) {
+    double ld = pl->losses_db * pl->dz[i] / pl->length;
+    if (ld == 0.0) ld = pl->losses_db;
+    pl->loss.push_back(ld != 0.0 ? (float)std::pow(10.0, -ld / 20.0) : 1.f);
+  }
+  pl->final_loss = (pl->path_output_loss && pl->losses_db != 0.0) ? (float)std::pow(10.0, -pl->losses_db / 20.0) : 1.f;
+
+  int rc = ATM_OK;
+  if (pl->n > 0) rc = choose_low_block(pl, d);
+  if (rc) {
+    delete pl;
+    return rc;
+  }
+  pl->P_H = pl->P - pl->P_L;
+  pl->KH = ((2 * pl->P_H + 7) / 8) * 8;
+  pl->KC = pl->P_L > 0 ? ((pl->D - 1 + 7) / 8) * 8 : 0;
+  if (pl->n > 0 && pl->KH + pl->KC == 0) pl->KH = 8;  // keep the GEMM well-formed
+  if (pl->n > 0 && atm::prep_smem_bytes(pl->P_L, pl->D) > 220 * 1024) {
+    delete pl;
+    return fail(ATM_ERR_UNSUPPORTED, "too many low-frequency annuli (%d) for the prep kernel", pl->P_L);
+  }
+  pl->rows = atm::row_pass_rows(pl->N);
+  pl->n_parts = pl->N / pl->rows;
+  pl->n_meas = 6 + pl->n_pupils;
+  pl->n_out = ATM_OUT_PUPIL0 + pl->n_pupils + pl->n_tracked;
+
+  const size_t N = pl->N, B = pl->B, K = pl->KH + pl->KC;
+  const size_t plane = N * N;
+  auto& v = pl->bufs;
+  if ((rc = dev_alloc(pl->field, B * plane * sizeof(float2), v)) ||
+      (rc = dev_alloc(pl->tw, N * sizeof(float2), v)) || (rc = dev_alloc(pl->ay, N * sizeof(float2), v)) ||
+      (rc = dev_alloc(pl->ax, N * sizeof(float2), v)) ||
+      (rc = dev_alloc(pl->hy, (size_t)std::max(pl->n, 1) * N * sizeof(float2), v)) ||
+      (rc = dev_alloc(pl->hx, (size_t)std::max(pl->n, 1) * N * sizeof(float2), v)) ||
+      (rc = dev_alloc(pl->vac_h, 2 * N * sizeof(float2), v)) ||
+      (rc = dev_alloc(pl->partials, B * pl->n_parts * pl->n_meas * sizeof(double), v)) ||
+      (rc = dev_alloc(pl->center, B * sizeof(float), v)) ||
+      (rc = dev_alloc(pl->pupil_rows, (size_t)pl->n_pupils * N * sizeof(int2), v)) ||
+      (rc = dev_alloc(pl->tracked_r, (size_t)pl->n_tracked * sizeof(double), v)) ||
+      (rc = dev_alloc(pl->intensity, pl->n_tracked > 0 ? B * plane * sizeof(float) : 0, v))) {
+    delete pl;
+    return rc;
+  }
+  if (pl->n > 0) {
+    if ((rc = dev_alloc(pl->phi, B * plane * sizeof(float), v)) ||
+        (rc = dev_alloc(pl->At, B * pl->KH * N * sizeof(float), v)) ||
+        (rc = dev_alloc(pl->Bt, B * K * N * sizeof(float), v)) ||
+        (rc = dev_alloc(pl->Ach, (size_t)pl->KC * N * sizeof(float), v)) ||
+        (rc = dev_alloc(pl->ht, B * (pl->KH / 2) * sizeof(atm::HighTerm), v)) ||
+        (rc = dev_alloc(pl->Py, B * N * sizeof(float2), v)) || (rc = dev_alloc(pl->Px, B * N * sizeof(float2), v)) ||
+        (rc = dev_alloc(pl->Gy, B * N * sizeof(double), v)) || (rc = dev_alloc(pl->Hx, B * N * sizeof(double), v))) {
+      delete pl;
+      return rc;
+    }
+  }
+  if ((rc = plan_tables(pl, d))) {
+    delete pl;
+    return rc;
+  }
+  *out = pl;
+  return ATM_OK;
+}
+
+int atm_plan_destroy(AtmPlan* pl) {
+  if (!pl) return ATM_OK;
+  cudaDeviceSynchronize();
+  delete pl;
+  return ATM_OK;
+}
+
+int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
+  if (!pl || !info) return fail(ATM_ERR_INVALID, "NULL argument");
+  info->n_out = pl->n_out;
+  info->low_annuli = pl->P_L;
+  info->cheb_terms = pl->D;
+  info->gemm_k = pl->KH + pl->KC;
+  info->workspace_bytes = pl->bytes();
+  int launches = 0;
+  for (int i = 0; i < pl->n; ++i) launches += 4 + (pl->dz[i + 1] > 0 ? 1 : 0);
+  launches += (pl->n == 0 || pl->dz[pl->n] > 0) ? 1 : 0;
+  launches += 1;  // finalize
+  info->launches_per_run = launches;
+  info->row_parts = pl->n_parts;
+  return ATM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// brackets one launch with an event pair when the plan is profiling
+struct Prof {
+  AtmPlan* pl;
+  int kind;
+  cudaStream_t st;
+  int slot = -1;
+  Prof(AtmPlan* p, int k, cudaStream_t s) : pl(p), kind(k), st(s) {
+    if (pl->profiling && pl->ev_used < pl->ev_cap) {
+      slot = pl->ev_used++;
+      pl->ev_kind[slot] = kind;
+      cudaEventRecord(pl->ev[2 * slot], st);
+    }
+  }
+  ~Prof() {
+    if (slot >= 0) cudaEventRecord(pl->ev[2 * slot + 1], st);
+  }
+};
+
+atm::ScreenArgs screen_args(AtmPlan* pl, const float* rho, const float* theta, const void* value, int screen) {
+  atm::ScreenArgs s{};
+  s.rho = rho;
+  s.theta = theta;
+  s.value = reinterpret_cast<const float2*>(value);
+  s.n_screens = pl->n;
+  s.screen = screen;
+  s.P = pl->P;
+  s.N = pl->N;
+  s.delta = pl->delta;
+  s.sx = pl->sx;
+  s.sy = pl->sy;
+  s.P_L = pl->P_L;
+  s.D = pl->D;
+  s.P_H = pl->P_H;
+  s.KH = pl->KH;
+  s.KC = pl->KC;
+  s.hterms = (atm::HighTerm*)pl->ht.p;
+  s.Py = (float2*)pl->Py.p;
+  s.Px = (float2*)pl->Px.p;
+  s.At = (float*)pl->At.p;
+  s.Bt = (float*)pl->Bt.p;
+  s.Gy = nullptr;
+  s.Hx = nullptr;
+  return s;
+}
+
+int run_screen(AtmPlan* pl, const atm::ScreenArgs& s, int B, cudaStream_t st) {
+  {
+    Prof p(pl, ATM_KIND_SCREEN_PREP, st);
+    ATM_CUDA(atm::launch_screen_prep(B, s, st));
+  }
+  if (pl->P_H > 0) {
+    Prof p(pl, ATM_KIND_SCREEN_TABLE, st);
+    ATM_CUDA(atm::launch_screen_table(B, s, st));
+  }
+  atm::GemmArgs g{};
+  g.At = (const float*)pl->At.p;
+  g.Ach = (const float*)pl->Ach.p;
+  g.Bt = (const float*)pl->Bt.p;
+  g.phi = (float*)pl->phi.p;
+  g.N = pl->N;
+  g.KH = pl->KH;
+  g.KC = pl->KC;
+  Prof p(pl, ATM_KIND_SCREEN_GEMM, st);
+  ATM_CUDA(atm::launch_screen_gemm(B, g, st));
+  return ATM_OK;
+}
+
+atm::RowArgs row_args(AtmPlan* pl, float* mean_intensity, void* field_out) {
+  atm::RowArgs ra{};
+  ra.field = (float2*)pl->field.p;
+  ra.tw = (const float2*)pl->tw.p;
+  ra.ay = (const float2*)pl->ay.p;
+  ra.ax = (const float2*)pl->ax.p;
+  ra.Py = (const float2*)pl->Py.p;
+  ra.Px = (const float2*)pl->Px.p;
+  ra.phi = (const float*)pl->phi.p;
+  ra.partials = (double*)pl->partials.p;
+  ra.center = (float*)pl->center.p;
+  ra.pupil_rows = (const int2*)pl->pupil_rows.p;
+  ra.mean_I = mean_intensity;
+  ra.intensity = (float*)pl->intensity.p;
+  ra.n_pupils = pl->n_pupils;
+  ra.n_meas = pl->n_meas;
+  ra.delta = (float)pl->delta;
+  ra.delta64 = pl->delta;
+  ra.out = (float2*)field_out;
+  return ra;
+}
+
+int finish_measures(AtmPlan* pl, int batch, double* measures, cudaStream_t st) {
+  atm::FinalArgs fa{};
+  fa.partials = (const double*)pl->partials.p;
+  fa.center = (const float*)pl->center.p;
+  fa.out = measures;
+  fa.n_parts = pl->n_parts;
+  fa.n_meas = pl->n_meas;
+  fa.n_out = pl->n_out;
+  fa.n_pupils = pl->n_pupils;
+  fa.delta = pl->delta;
+  {
+    Prof p(pl, ATM_KIND_FINALIZE, st);
+    ATM_CUDA(atm::launch_finalize(batch, fa, st));
+  }
+  if (pl->n_tracked > 0) {
+    Prof p(pl, ATM_KIND_TRACKED, st);
+    atm::TrackedArgs ta{};
+    ta.intensity = (const float*)pl->intensity.p;
+    ta.out = measures;
+    ta.radii = (const double*)pl->tracked_r.p;
+    ta.n_tracked = pl->n_tracked;
+    ta.n_out = pl->n_out;
+    ta.slot0 = ATM_OUT_PUPIL0 + pl->n_pupils;
+    ta.N = pl->N;
+    ta.delta = pl->delta;
+    ATM_CUDA(atm::launch_tracked(batch, ta, st));
+  }
+  return ATM_OK;
+}
+
+int check_device(const AtmPlan* pl) {
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != pl->device) return fail(ATM_ERR_INVALID, "plan belongs to device %d, current device is %d", pl->device, dev);
+  return ATM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value, int32_t batch, double* measures,
+            void* field_out, float* mean_intensity, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
+  if (!measures) return fail(ATM_ERR_INVALID, "measures_out is NULL");
+  if (pl->n > 0 && (!rho || !theta || !value)) return fail(ATM_ERR_INVALID, "spectra pointers are NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = pl->N, n = pl->n;
+
+  atm::RowArgs ra = row_args(pl, mean_intensity, field_out);
+
+  atm::ColArgs ca{};
+  ca.field = (float2*)pl->field.p;
+  ca.tw = (const float2*)pl->tw.p;
+
+  bool measured = false;
+  for (int i = 0; i < n; ++i) {
+    atm::ScreenArgs s = screen_args(pl, rho, theta, value, i);
+    if (int rc = run_screen(pl, s, batch, st)) return rc;
+    int flags = (i == 0 ? atm::ROW_GEN : (pl->dz[i] > 0 ? atm::ROW_INV : 0)) | atm::ROW_PHASOR;
+    const bool next_vac = pl->dz[i + 1] > 0;
+    if (next_vac) {
+      flags |= atm::ROW_FWD | atm::ROW_STORE;
+    } else if (i == n - 1) {
+      flags |= atm::ROW_MEAS | (field_out ? atm::ROW_STORE : 0);
+      measured = true;
+    } else {
+      flags |= atm::ROW_STORE;
+    }
+    ra.flags = flags;
+    ra.loss = pl->loss[i] * ((i == n - 1 && !next_vac) ? pl->final_loss : 1.f);
+    ra.store_out = (flags & atm::ROW_MEAS) ? 1 : 0;
+    {
+      Prof p(pl, ATM_KIND_ROW_PASS, st);
+      ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
+    }
+    if (next_vac) {
+      ca.hy = (const float2*)pl->hy.p + (size_t)i * N;
+      ca.hx = (const float2*)pl->hx.p + (size_t)i * N;
+      Prof p(pl, ATM_KIND_COL_PASS, st);
+      ATM_CUDA(atm::launch_col_pass(N, batch, pl->col_tile, ca, st));
+    }
+  }
+  if (!measured) {
+    // last row pass: inverse row FFT (or the analytic field of a vacuum path)
+    ra.flags = (n == 0 ? atm::ROW_GEN : atm::ROW_INV) | atm::ROW_MEAS | (field_out ? atm::ROW_STORE : 0);
+    ra.loss = pl->final_loss;
+    ra.store_out = 1;
+    Prof p(pl, ATM_KIND_ROW_PASS, st);
+    ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
+  }
+  return finish_measures(pl, batch, measures, st);
+}
+
+int atm_measures(AtmPlan* pl, const void* field, int32_t batch, double* measures, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
+  if (!field || !measures) return fail(ATM_ERR_INVALID, "field / measures_out is NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  atm::RowArgs ra = row_args(pl, nullptr, nullptr);
+  ra.field = (float2*)field;
+  ra.flags = atm::ROW_MEAS;
+  ra.loss = 1.f;
+  {
+    Prof p(pl, ATM_KIND_ROW_PASS, st);
+    ATM_CUDA(atm::launch_row_pass(pl->N, batch, ra, st));
+  }
+  return finish_measures(pl, batch, measures, st);
+}
+
+int atm_screen(AtmPlan* pl, const float* rho, const float* theta, const void* value, int32_t batch, int32_t screen,
+               float* phi_out, void* phasor_out, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (pl->n < 1) return fail(ATM_ERR_INVALID, "plan has no screens");
+  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
+  if (screen < 0 || screen >= pl->n) return fail(ATM_ERR_INVALID, "screen %d out of range", screen);
+  if (!rho || !theta || !value) return fail(ATM_ERR_INVALID, "spectra pointers are NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  atm::ScreenArgs s = screen_args(pl, rho, theta, value, screen);
+  s.Gy = (double*)pl->Gy.p;
+  s.Hx = (double*)pl->Hx.p;
+  if (int rc = run_screen(pl, s, batch, st)) return rc;
+  ATM_CUDA(atm::launch_compose_screen(batch, pl->N, (const double*)pl->Gy.p, (const double*)pl->Hx.p,
+                                      (const float*)pl->phi.p, (const float2*)pl->Py.p, (const float2*)pl->Px.p,
+                                      phi_out, (float2*)phasor_out, st));
+  return ATM_OK;
+}
+
+int atm_vacuum(AtmPlan* pl, void* field, int32_t batch, double dz, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (!field) return fail(ATM_ERR_INVALID, "field is NULL");
+  if (batch < 1) return fail(ATM_ERR_INVALID, "batch must be >= 1");
+  if (!(dz > 0)) return ATM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = pl->N;
+  std::vector<cd> h = transfer_1d(N, pl->delta, pl->kw, dz);
+  const cd ph = global_phase(pl->kw, dz) / ((double)N * (double)N);
+  std::vector<float2> tab(2 * (size_t)N);
+  for (int k = 0; k < N; ++k) {
+    const cd y = ph * h[k];
+    tab[k] = make_float2((float)y.real(), (float)y.imag());
+    tab[N + k] = make_float2((float)h[k].real(), (float)h[k].imag());
+  }
+  // the source is pageable: cudaMemcpyAsync returns once it has been staged
+  ATM_CUDA(cudaMemcpyAsync(pl->vac_h.p, tab.data(), tab.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+  atm::RowArgs ra{};
+  ra.field = (float2*)field;
+  ra.tw = (const float2*)pl->tw.p;
+  ra.loss = 1.f;
+  ra.delta = (float)pl->delta;
+  ra.delta64 = pl->delta;
+  ra.flags = atm::ROW_FWD | atm::ROW_STORE;
+  ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
+  atm::ColArgs ca{};
+  ca.field = (float2*)field;
+  ca.tw = (const float2*)pl->tw.p;
+  ca.hy = (const float2*)pl->vac_h.p;
+  ca.hx = (const float2*)pl->vac_h.p + N;
+  ATM_CUDA(atm::launch_col_pass(N, batch, pl->col_tile, ca, st));
+  ra.flags = atm::ROW_INV | atm::ROW_STORE;
+  ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
+  return ATM_OK;
+}
+
+int atm_profile_begin(AtmPlan* pl, int32_t max_launches) {
+  if (!pl || max_launches < 1) return fail(ATM_ERR_INVALID, "bad profile arguments");
+  if (int rc = check_device(pl)) return rc;
+  if ((int)pl->ev.size() < 2 * max_launches) {
+    for (auto e : pl->ev) cudaEventDestroy(e);
+    pl->ev.assign(2 * (size_t)max_launches, nullptr);
+    for (auto& e : pl->ev) ATM_CUDA(cudaEventCreate(&e));
+  }
+  pl->ev_kind.assign(max_launches, 0);
+  pl->ev_cap = max_launches;
+  pl->ev_used = 0;
+  pl->profiling = true;
+  return ATM_OK;
+}
+
+int atm_profile_end(AtmPlan* pl, double* ms, int32_t* count, int32_t n_kinds) {
+  if (!pl || !ms || !count || n_kinds < 1) return fail(ATM_ERR_INVALID, "bad profile arguments");
+  for (int k = 0; k < n_kinds; ++k) {
+    ms[k] = 0.0;
+    count[k] = 0;
+  }
+  pl->profiling = false;
+  for (int i = 0; i < pl->ev_used; ++i) {
+    ATM_CUDA(cudaEventSynchronize(pl->ev[2 * i + 1]));
+    float t = 0.f;
+    ATM_CUDA(cudaEventElapsedTime(&t, pl->ev[2 * i], pl->ev[2 * i + 1]));
+    const int k = pl->ev_kind[i];
+    if (k < n_kinds) {
+      ms[k] += t;
+      count[k] += 1;
+    }
+  }
+  pl->ev_used = 0;
+  return ATM_OK;
+}
+
+int atm_fma_probe(int32_t blocks, int32_t iters, double* ms, void* stream) {
+  if (blocks < 1 || iters < 1 || !ms) return fail(ATM_ERR_INVALID, "bad probe arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t a, b;
+  ATM_CUDA(cudaEventCreate(&a));
+  ATM_CUDA(cudaEventCreate(&b));
+  ATM_CUDA(cudaEventRecord(a, st));
+  ATM_CUDA(atm::launch_fma_probe(blocks, iters, st));
+  ATM_CUDA(cudaEventRecord(b, st));
+  ATM_CUDA(cudaEventSynchronize(b));
+  float t = 0.f;
+  ATM_CUDA(cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = t;
+  return ATM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,309 @@
+// Shared device/host building blocks of the GB300 split-step engine.
+//
+// Everything in this header is __host__ __device__ so that the FFT stage
+// arithmetic, the Bessel / Chebyshev coefficients of the low-frequency screen
+// block and the fixed-point phase reduction can be exercised on the CPU
+// (atm_selftest.cu) with exactly the code the kernels run.
+#pragma once
+
+#include <cstdint>
+#include <cmath>
+#include <cuda_runtime.h>
+
+#if defined(__CUDACC__)
+#define ATM_HD __host__ __device__ __forceinline__
+#else
+#define ATM_HD inline
+#endif
+
+namespace atm {
+
+// ---------------------------------------------------------------------------
+// complex helpers (complex64 = float2, complex128 = double2)
+// ---------------------------------------------------------------------------
+ATM_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+ATM_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+ATM_HD float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+ATM_HD float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+ATM_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by -i (DIR=-1, forward) or +i (DIR=+1, inverse)
+template <int DIR>
+ATM_HD float2 cmul_i(float2 a) {
+  return DIR < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+}
+
+// ---------------------------------------------------------------------------
+// small DFTs, b_q = sum_m a_m exp(DIR * 2 pi i m q / R)
+// ---------------------------------------------------------------------------
+template <int DIR>
+ATM_HD void dft2(float2& a0, float2& a1) {
+  float2 t = a0;
+  a0 = cadd(t, a1);
+  a1 = csub(t, a1);
+}
+
+template <int DIR>
+ATM_HD void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  float2 s02 = cadd(a0, a2), d02 = csub(a0, a2);
+  float2 s13 = cadd(a1, a3), d13 = cmul_i<DIR>(csub(a1, a3));
+  a0 = cadd(s02, s13);
+  a2 = csub(s02, s13);
+  a1 = cadd(d02, d13);
+  a3 = csub(d02, d13);
+}
+
+template <int DIR>
+ATM_HD void dft8(float2 (&a)[8]) {
+  // even / odd split: E = DFT4(a0,a2,a4,a6), O = DFT4(a1,a3,a5,a7)
+  dft4<DIR>(a[0], a[2], a[4], a[6]);
+  dft4<DIR>(a[1], a[3], a[5], a[7]);
+  const float h = 0.70710678118654752440f;
+  // twiddles w^q, w = exp(DIR 2 pi i / 8), applied to O_q (q = 1,2,3)
+  float2 o1 = a[3], o2 = a[5], o3 = a[7];
+  o1 = cmul(o1, make_float2(h, DIR * h));
+  o2 = cmul_i<DIR>(o2);  // w^2 = exp(DIR i pi/2) = DIR * i
+  o3 = cmul(o3, make_float2(-h, DIR * h));
+  float2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6], o0 = a[1];
+  a[0] = cadd(e0, o0);
+  a[4] = csub(e0, o0);
+  a[1] = cadd(e1, o1);
+  a[5] = csub(e1, o1);
+  a[2] = cadd(e2, o2);
+  a[6] = csub(e2, o2);
+  a[3] = cadd(e3, o3);
+  a[7] = csub(e3, o3);
+}
+
+template <int DIR>
+ATM_HD void dft16(float2 (&a)[16]) {
+  // m = m1 + 4 m2, q = 4 q1 + q2:
+  //   c[m1][q2] = sum_m2 a[m1 + 4 m2] W4^(m2 q2)   (DFT4 over stride-4 inputs)
+  //   c[m1][q2] *= W16^(m1 q2)
+  //   b[4 q1 + q2] = sum_m1 c[m1][q2] W4^(m1 q1)
+  for (int m1 = 0; m1 < 4; ++m1) dft4<DIR>(a[m1], a[m1 + 4], a[m1 + 8], a[m1 + 12]);
+  // after the first DFT4, a[m1 + 4 q2] holds c[m1][q2]
+  const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
+  const float h = 0.70710678118654752440f;
+  // W16^1, W16^2, W16^3, W16^4(=W4^1), W16^6, W16^9 with W16 = exp(DIR 2 pi i/16)
+  const float2 w1 = make_float2(c1, DIR * s1);
+  const float2 w2 = make_float2(h, DIR * h);
+  const float2 w3 = make_float2(s1, DIR * c1);
+  const float2 w6 = make_float2(-h, DIR * h);
+  const float2 w9 = make_float2(-c1, -DIR * s1);
+  a[1 + 4 * 1] = cmul(a[1 + 4 * 1], w1);
+  a[1 + 4 * 2] = cmul(a[1 + 4 * 2], w2);
+  a[1 + 4 * 3] = cmul(a[1 + 4 * 3], w3);
+  a[2 + 4 * 1] = cmul(a[2 + 4 * 1], w2);
+  a[2 + 4 * 2] = cmul_i<DIR>(a[2 + 4 * 2]);  // W16^4 = DIR * i
+  a[2 + 4 * 3] = cmul(a[2 + 4 * 3], w6);
+  a[3 + 4 * 1] = cmul(a[3 + 4 * 1], w3);
+  a[3 + 4 * 2] = cmul(a[3 + 4 * 2], w6);
+  a[3 + 4 * 3] = cmul(a[3 + 4 * 3], w9);
+  float2 b[16];
+  for (int q2 = 0; q2 < 4; ++q2) {
+    float2 x0 = a[0 + 4 * q2], x1 = a[1 + 4 * q2], x2 = a[2 + 4 * q2], x3 = a[3 + 4 * q2];
+    dft4<DIR>(x0, x1, x2, x3);
+    b[0 * 4 + q2] = x0;
+    b[1 * 4 + q2] = x1;
+    b[2 * 4 + q2] = x2;
+    b[3 * 4 + q2] = x3;
+  }
+  for (int q = 0; q < 16; ++q) a[q] = b[q];
+}
+
+template <int R, int DIR>
+ATM_HD void dft(float2 (&a)[R]);
+template <>
+ATM_HD void dft<2, -1>(float2 (&a)[2]) { dft2<-1>(a[0], a[1]); }
+template <>
+ATM_HD void dft<2, 1>(float2 (&a)[2]) { dft2<1>(a[0], a[1]); }
+template <>
+ATM_HD void dft<4, -1>(float2 (&a)[4]) { dft4<-1>(a[0], a[1], a[2], a[3]); }
+template <>
+ATM_HD void dft<4, 1>(float2 (&a)[4]) { dft4<1>(a[0], a[1], a[2], a[3]); }
+template <>
+ATM_HD void dft<8, -1>(float2 (&a)[8]) { dft8<-1>(a); }
+template <>
+ATM_HD void dft<8, 1>(float2 (&a)[8]) { dft8<1>(a); }
+template <>
+ATM_HD void dft<16, -1>(float2 (&a)[16]) { dft16<-1>(a); }
+template <>
+ATM_HD void dft<16, 1>(float2 (&a)[16]) { dft16<1>(a); }
+
+// ---------------------------------------------------------------------------
+// Stockham FFT of length N held by T = N/16 threads, 16 elements each.
+//
+// Radix plan: radix-16 stages first, the remainder (2, 4, 8 or 16) last.
+// Register convention at the first stage's input and the last stage's
+// output: v[m] holds element t + m*T.  So an inverse FFT followed by a
+// forward FFT of the same row needs no exchange in between, and global loads
+// and stores are coalesced across t.
+//
+// Stage (radix R, L = product of earlier radices), butterfly k in [0, N/R):
+//   i = k mod L; inputs x[k + m N/R]; twiddle x_m *= W_{LR}^{i m};
+//   DFT_R; outputs y[(k - i) R + i + q L].
+// A thread runs butterflies k = t + b T, b in [0, 16/R).
+// ---------------------------------------------------------------------------
+template <int N>
+struct FftPlan;
+template <> struct FftPlan<64>   { static constexpr int S = 2; static constexpr int last = 4; };
+template <> struct FftPlan<128>  { static constexpr int S = 2; static constexpr int last = 8; };
+template <> struct FftPlan<256>  { static constexpr int S = 2; static constexpr int last = 16; };
+template <> struct FftPlan<512>  { static constexpr int S = 3; static constexpr int last = 2; };
+template <> struct FftPlan<1024> { static constexpr int S = 3; static constexpr int last = 4; };
+template <> struct FftPlan<2048> { static constexpr int S = 3; static constexpr int last = 8; };
+template <> struct FftPlan<4096> { static constexpr int S = 3; static constexpr int last = 16; };
+
+template <int N, int s>
+struct StageRadix {
+  static constexpr int value = (s == FftPlan<N>::S - 1) ? FftPlan<N>::last : 16;
+};
+template <int N, int s>
+struct StageL {
+  static constexpr int value = (s == 0) ? 1 : StageL<N, s - 1>::value * StageRadix<N, s - 1>::value;
+};
+template <int N>
+struct StageL<N, -1> {
+  static constexpr int value = 1;
+};
+
+// shared-memory slot of element j: one pad slot per 16 elements
+ATM_HD int pad16(int j) { return j + (j >> 4); }
+template <int N>
+struct Padded {
+  static constexpr int value = N + N / 16;
+};
+
+// twiddle W_{LR}^{e} for e < L*R, from the length-N table tw[n] = exp(-2 pi i n / N)
+template <int N, int LR, int DIR>
+ATM_HD float2 twiddle(const float2* tw, int e) {
+  float2 w = tw[e * (N / LR)];
+  return DIR < 0 ? w : cconj(w);
+}
+
+// butterflies of stage s on register inputs; results to shared memory
+template <int N, int s, int DIR>
+ATM_HD void stage_to_smem(float2 (&v)[16], float2* sm, int t, const float2* tw) {
+  constexpr int R = StageRadix<N, s>::value;
+  constexpr int L = StageL<N, s>::value;
+  constexpr int T = N / 16;
+  constexpr int B = 16 / R;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int k = t + b * T;
+    const int i = k & (L - 1);
+    float2 a[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
+    if (L > 1) {
+#pragma unroll
+      for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR>(tw, i * m));
+    }
+    dft<R, DIR>(a);
+    const int j = (k - i) * R + i;
+#pragma unroll
+    for (int q = 0; q < R; ++q) sm[pad16(j + q * L)] = a[q];
+  }
+}
+
+// inputs of stage s from shared memory
+template <int N, int s>
+ATM_HD void stage_from_smem(float2 (&v)[16], const float2* sm, int t) {
+  constexpr int R = StageRadix<N, s>::value;
+  constexpr int T = N / 16;
+  constexpr int B = 16 / R;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+#pragma unroll
+    for (int m = 0; m < R; ++m) v[b + B * m] = sm[pad16(t + b * T + m * (N / R))];
+  }
+}
+
+// last stage: outputs stay in registers, v[m] = element t + m T
+template <int N, int DIR>
+ATM_HD void stage_last(float2 (&v)[16], int t, const float2* tw) {
+  constexpr int s = FftPlan<N>::S - 1;
+  constexpr int R = StageRadix<N, s>::value;
+  constexpr int L = StageL<N, s>::value;
+  constexpr int T = N / 16;
+  constexpr int B = 16 / R;
+  float2 o[16];
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int k = t + b * T;
+    const int i = k & (L - 1);  // == k, since k < N/R == L
+    float2 a[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
+#pragma unroll
+    for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR>(tw, i * m));
+    dft<R, DIR>(a);
+#pragma unroll
+    for (int q = 0; q < R; ++q) o[b + B * q] = a[q];
+  }
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = o[m];
+}
+
+// ---------------------------------------------------------------------------
+// fixed-point phase: turns(j) = frac(j * S + O) held as a 64-bit binary
+// fraction; the product wraps modulo one turn exactly.  Returned as
+// half-turns in [-1, 1) for sincospif.
+// ---------------------------------------------------------------------------
+ATM_HD uint64_t turns_to_fixed(double turns) {
+  double f = turns - floor(turns);  // [0, 1)
+  // split to keep all 64 bits: hi 32 bits then the remainder
+  double hi = floor(f * 4294967296.0);
+  double lo = (f * 4294967296.0 - hi) * 4294967296.0;
+  uint64_t h = (uint64_t)hi;
+  uint64_t l = (uint64_t)lo;
+  return (h << 32) + l;
+}
+
+ATM_HD float fixed_to_halfturns(uint64_t x) {
+  int32_t top = (int32_t)(uint32_t)(x >> 32);
+  return (float)top * 4.656612873077392578125e-10f;  // 2^-31
+}
+
+// ---------------------------------------------------------------------------
+// Bessel J_0..J_{D-1}(a) by Miller's backward recurrence, normalised with
+// J_0 + 2 sum_k J_2k = 1.  Used for the Jacobi-Anger (Chebyshev) expansion
+//   exp(i a t) = J_0(a) + 2 sum_{n>=1} i^n J_n(a) T_n(t),  |t| <= 1.
+// ---------------------------------------------------------------------------
+ATM_HD void bessel_j(double a, int D, double* J /* [D] */) {
+  const double sgn = a < 0 ? -1.0 : 1.0;
+  a = fabs(a);
+  if (a < 1e-30) {
+    J[0] = 1.0;
+    for (int n = 1; n < D; ++n) J[n] = 0.0;
+    return;
+  }
+  const int n0 = D + (int)a + 40;
+  double jp1 = 0.0, j = 1e-200, norm = 0.0;
+  for (int n = 0; n < D; ++n) J[n] = 0.0;
+  for (int n = n0; n >= 1; --n) {
+    // j = J_n (unnormalised), jp1 = J_{n+1}
+    if (n < D) J[n] = j;
+    if ((n & 1) == 0) norm += 2.0 * j;
+    const double jm1 = (2.0 * n / a) * j - jp1;
+    jp1 = j;
+    j = jm1;
+    if (fabs(j) > 1e200) {  // rescale to stay in range
+      j *= 1e-200;
+      jp1 *= 1e-200;
+      norm *= 1e-200;
+      for (int m = 0; m < D; ++m) J[m] *= 1e-200;
+    }
+  }
+  // j = J_0
+  norm += j;
+  J[0] = j;
+  const double inv = 1.0 / norm;
+  for (int n = 0; n < D; ++n) J[n] *= inv;
+  if (sgn < 0)
+    for (int n = 1; n < D; n += 2) J[n] = -J[n];
+}
+
+}  // namespace atm

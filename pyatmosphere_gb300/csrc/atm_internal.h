@@ -1,0 +1,133 @@
+// Structures shared by the kernels (atm_kernels.cu) and the plan / C-ABI
+// layer (atm_abi.cu).  Not part of the public interface (include/atm.h).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace atm {
+
+// row-pass flags
+enum : int {
+  ROW_GEN = 1,      // generate the row from the separable tables ay[y] * ax[x]
+  ROW_INV = 2,      // inverse row FFT first (input in the row-frequency domain)
+  ROW_PHASOR = 4,   // multiply by the screen phasor Py[y] Px[x] exp(-i phi[y,x]) * loss
+  ROW_FWD = 8,      // forward row FFT after the multiply
+  ROW_STORE = 16,   // write the row back
+  ROW_MEAS = 32,    // accumulate the measure partial sums (spatial domain)
+};
+
+constexpr int kMaxPupils = 8;
+// measure slots accumulated by the last row pass (before the delta^2 scale)
+enum : int {
+  MS_I = 0, MS_IX, MS_IMY, MS_IX2, MS_IMXY, MS_IY2, MS_PUPIL0,
+};
+// per-realisation output layout (doubles)
+enum : int {
+  MO_ETA_TOTAL = 0, MO_MEAN_X, MO_MEAN_Y, MO_MEAN_X2, MO_MEAN_XY, MO_MEAN_Y2,
+  MO_MEAN_X2_R, MO_I_CENTER, MO_PUPIL0,
+};
+
+struct RowArgs {
+  float2* field;            // [B][N][N]
+  const float2* tw;         // exp(-2 pi i n / N), n < N
+  const float2* ay;         // [N] (ROW_GEN)
+  const float2* ax;         // [N] (ROW_GEN)
+  const float2* Py;         // [B][N] screen phasor, rows
+  const float2* Px;         // [B][N] screen phasor, columns
+  const float* phi;         // [B][N][N] screen GEMM part
+  float loss;               // amplitude factor of this step
+  double* partials;         // [B][gridDim.x][n_meas]
+  float* center;            // [B] intensity at the grid origin
+  const int2* pupil_rows;   // [n_pupils][N] inclusive column interval per row
+  float* mean_I;            // [N][N] intensity accumulator (nullable)
+  float* intensity;         // [B][N][N] stored intensity (nullable)
+  float2* out;              // [B][N][N] destination of ROW_STORE when store_out != 0
+  int store_out;
+  int n_pupils;
+  int n_meas;
+  int flags;
+  float delta;
+  double delta64;
+};
+
+struct ColArgs {
+  float2* field;            // [B][N][N]
+  const float2* tw;
+  const float2* hy;         // [N] transfer function along y incl. exp(i k dz) / N^2
+  const float2* hx;         // [N] transfer function along x
+};
+
+// one high-frequency spectral term, phases as 64-bit binary fractions of a turn
+struct HighTerm {
+  uint64_t sx, ox;          // x phase: turns = j * sx + ox  (mod 1)
+  uint64_t sy, oy;          // y phase
+  float2 v;                 // complex amplitude
+  float2 pad_;
+};
+
+struct ScreenArgs {
+  const float* rho;         // [B][n][P]
+  const float* theta;       // [B][n][P]
+  const float2* value;      // [B][n][P]
+  int n_screens, screen, P;
+  int N;
+  double delta, sx, sy;     // grid step and screen shift
+  int P_L;                  // annuli collapsed into the Chebyshev block
+  int D;                    // Chebyshev terms 0..D-1
+  int P_H;                  // high-frequency terms = P - P_L
+  int KH;                   // GEMM rows of the high part (2 P_H padded)
+  int KC;                   // GEMM rows of the Chebyshev part (D-1 padded)
+  HighTerm* hterms;         // [B][KH/2]
+  float2* Py;               // [B][N]
+  float2* Px;               // [B][N]
+  float* At;                // [B][KH][N]  A^T, high part (per screen)
+  float* Bt;                // [B][KH+KC][N]
+  double* Gy;               // [B][N] FP64 phase of the y-only part (nullable)
+  double* Hx;               // [B][N] FP64 phase of the x-only part (nullable)
+};
+
+// GEMM: phi[s][y][x] = sum_k At[s][k][y] B[s][k][x], k < KH from At, then the
+// shared Chebyshev rows Ach[k-KH][y]
+struct GemmArgs {
+  const float* At;          // [B][KH][N]
+  const float* Ach;         // [KC][N]
+  const float* Bt;          // [B][KH+KC][N]
+  float* phi;               // [B][N][N]
+  int N, KH, KC;
+};
+
+struct FinalArgs {
+  const double* partials;   // [B][n_parts][n_meas]
+  const float* center;      // [B]
+  double* out;              // [B][n_out]
+  int n_parts, n_meas, n_out, n_pupils;
+  double delta;
+};
+
+struct TrackedArgs {
+  const float* intensity;   // [B][N][N]
+  double* out;              // [B][n_out] (reads mean_x/mean_y, writes tracked etas)
+  const double* radii;      // [n_tracked]
+  int n_tracked, n_out, slot0, N;
+  double delta;
+};
+
+// kernel launchers (atm_kernels.cu); return cudaGetLastError()
+cudaError_t launch_row_pass(int N, int B, const RowArgs& a, cudaStream_t st);
+cudaError_t launch_col_pass(int N, int B, int col_tile, const ColArgs& a, cudaStream_t st);
+cudaError_t launch_screen_prep(int B, const ScreenArgs& a, cudaStream_t st);
+cudaError_t launch_screen_table(int B, const ScreenArgs& a, cudaStream_t st);
+cudaError_t launch_screen_gemm(int B, const GemmArgs& a, cudaStream_t st);
+cudaError_t launch_compose_screen(int B, int N, const double* Gy, const double* Hx, const float* phiG,
+                                  const float2* Py, const float2* Px, float* phi_out, float2* phasor_out,
+                                  cudaStream_t st);
+cudaError_t launch_finalize(int B, const FinalArgs& a, cudaStream_t st);
+cudaError_t launch_tracked(int B, const TrackedArgs& a, cudaStream_t st);
+cudaError_t launch_fma_probe(int blocks, int iters, cudaStream_t st);
+int row_pass_rows(int N);          // rows per CTA of the row pass
+int col_tile_default(int N);
+bool supported_n(int N);
+size_t prep_smem_bytes(int P_L, int D);
+
+}  // namespace atm

@@ -1,0 +1,82 @@
+// Host-only emulation of the engine's FFT stages, Bessel coefficients and
+// fixed-point phase reduction (libatm_selftest.so).  The functions called
+// here are the same __host__ __device__ code the kernels run; the Stockham
+// stages are executed thread by thread between the points where the kernels
+// synchronise.  Used by the CPU test suite; needs no GPU.
+#include <vector>
+
+#include "atm_common.cuh"
+
+namespace {
+
+struct Regs {
+  float2 v[16];
+};
+
+template <int N, int DIR, int s>
+void host_stages(std::vector<Regs>& R, float2* sm, const float2* tw) {
+  constexpr int T = N / 16;
+  if constexpr (s == atm::FftPlan<N>::S - 1) {
+    for (int t = 0; t < T; ++t) atm::stage_last<N, DIR>(R[t].v, t, tw);
+  } else {
+    for (int t = 0; t < T; ++t) atm::stage_to_smem<N, s, DIR>(R[t].v, sm, t, tw);
+    for (int t = 0; t < T; ++t) atm::stage_from_smem<N, s + 1>(R[t].v, sm, t);
+    host_stages<N, DIR, s + 1>(R, sm, tw);
+  }
+}
+
+template <int N>
+int host_fft(int dir, const float* in, float* out) {
+  constexpr int T = N / 16;
+  std::vector<float2> tw(N), sm(atm::Padded<N>::value);
+  for (int i = 0; i < N; ++i) {
+    const double a = -2.0 * 3.14159265358979323846 * i / N;
+    tw[i] = make_float2((float)cos(a), (float)sin(a));
+  }
+  std::vector<Regs> R(T);
+  for (int t = 0; t < T; ++t)
+    for (int m = 0; m < 16; ++m) R[t].v[m] = make_float2(in[2 * (t + m * T)], in[2 * (t + m * T) + 1]);
+  if (dir < 0)
+    host_stages<N, -1, 0>(R, sm.data(), tw.data());
+  else
+    host_stages<N, 1, 0>(R, sm.data(), tw.data());
+  for (int t = 0; t < T; ++t)
+    for (int m = 0; m < 16; ++m) {
+      out[2 * (t + m * T)] = R[t].v[m].x;
+      out[2 * (t + m * T) + 1] = R[t].v[m].y;
+    }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// length-N FFT (dir = -1 forward, +1 unnormalised inverse) of interleaved complex data
+int atm_selftest_fft(int N, int dir, const float* in, float* out) {
+  switch (N) {
+    case 64: return host_fft<64>(dir, in, out);
+    case 128: return host_fft<128>(dir, in, out);
+    case 256: return host_fft<256>(dir, in, out);
+    case 512: return host_fft<512>(dir, in, out);
+    case 1024: return host_fft<1024>(dir, in, out);
+    case 2048: return host_fft<2048>(dir, in, out);
+    case 4096: return host_fft<4096>(dir, in, out);
+  }
+  return -1;
+}
+
+int atm_selftest_bessel(double a, int D, double* J) {
+  if (D < 1 || D > 256) return -1;
+  atm::bessel_j(a, D, J);
+  return 0;
+}
+
+// half-turns of frac(j * S + O) for j < N through the 64-bit fixed-point path
+int atm_selftest_turns(double S, double O, int N, float* half_turns) {
+  const uint64_t s = atm::turns_to_fixed(S), o = atm::turns_to_fixed(O);
+  for (int j = 0; j < N; ++j) half_turns[j] = atm::fixed_to_halfturns(s * (uint64_t)j + o);
+  return 0;
+}
+
+}  // extern "C"

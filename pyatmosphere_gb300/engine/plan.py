@@ -1,0 +1,185 @@
+"""Python handle on an engine plan (one channel geometry, one batch size).
+
+All tensors handed to the engine are CUDA tensors on the plan's device;
+calls are ordered on the current torch stream of that device.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, load
+
+
+def _dptr(arr: Optional[np.ndarray], ctype):
+    if arr is None:
+        return None
+    return arr.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def _tptr(t: Optional[torch.Tensor]):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(device) -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class EnginePlan:
+    """Owns an ``AtmPlan`` (include/atm.h)."""
+
+    def __init__(self, N: int, delta: float, wvl: float, w0: float, F0: float,
+                 positions: Sequence[float], length: float, f_base: Optional[np.ndarray] = None,
+                 losses_db: float = 0.0, path_output_loss: bool = False,
+                 shift: Sequence[float] = (0.0, 0.0), pupils: Sequence[tuple] = (),
+                 tracked: Sequence[float] = (), batch: int = 1, source: str = "gaussian",
+                 cheb_cut: float = 0.0, col_tile: int = 0, device=None):
+        if not torch.cuda.is_available():
+            raise _lib.EngineError("the GB300 engine needs a CUDA device; none is available")
+        self.lib = load()
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None
+                                   else torch.device(device).index or 0)
+        self.N = int(N)
+        self.n_screens = len(positions)
+        self.batch = int(batch)
+        self.P = 0 if f_base is None else int(len(f_base))
+        self._pos = np.ascontiguousarray(positions, dtype=np.float64)
+        self._base = None if f_base is None else np.ascontiguousarray(f_base, dtype=np.float32)
+        pupils = list(pupils)
+        self.n_pupils = len(pupils)
+        self._pr = np.ascontiguousarray([p[0] for p in pupils] or [0.0], dtype=np.float64)
+        self._psx = np.ascontiguousarray([p[1] if len(p) > 1 else 0.0 for p in pupils] or [0.0], dtype=np.float64)
+        self._psy = np.ascontiguousarray([p[2] if len(p) > 2 else 0.0 for p in pupils] or [0.0], dtype=np.float64)
+        self._tr = np.ascontiguousarray(list(tracked) or [0.0], dtype=np.float64)
+        self.n_tracked = len(tracked)
+        d = _lib.AtmChannelDesc()
+        d.abi_version = _lib.ABI_VERSION
+        d.resolution = self.N
+        d.delta = float(delta)
+        d.source_kind = _lib.SOURCE_PLANE if source == "plane" else _lib.SOURCE_GAUSSIAN
+        d.wvl = float(wvl)
+        d.w0 = float(w0) if w0 else 0.0
+        d.F0 = float(F0)
+        d.n_screens = self.n_screens
+        d.positions = _dptr(self._pos, ctypes.c_double)
+        d.length = float(length)
+        d.losses_db = float(losses_db or 0.0)
+        d.path_output_loss = 1 if path_output_loss else 0
+        d.points = self.P
+        d.f_base = _dptr(self._base, ctypes.c_float)
+        d.shift_x, d.shift_y = float(shift[0]), float(shift[1])
+        d.n_pupils = self.n_pupils
+        d.pupil_radius = _dptr(self._pr, ctypes.c_double)
+        d.pupil_shift_x = _dptr(self._psx, ctypes.c_double)
+        d.pupil_shift_y = _dptr(self._psy, ctypes.c_double)
+        d.n_tracked = self.n_tracked
+        d.tracked_radius = _dptr(self._tr, ctypes.c_double)
+        d.batch = self.batch
+        d.cheb_cut = float(cheb_cut)
+        d.col_tile = int(col_tile)
+        d.flags = 0
+        self._handle = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_plan_create(ctypes.byref(d), ctypes.byref(self._handle)))
+        info = _lib.AtmPlanInfo()
+        check(self.lib.atm_plan_info(self._handle, ctypes.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in _lib.AtmPlanInfo._fields_}
+        self.n_out = info.n_out
+
+    # ------------------------------------------------------------------
+    def close(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            with torch.cuda.device(self.device):
+                self.lib.atm_plan_destroy(h)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------
+    def _spectra(self, rho, theta, value, batch):
+        if self.n_screens == 0:
+            return None, None, None
+        for t, dt in ((rho, torch.float32), (theta, torch.float32), (value, torch.complex64)):
+            if t.device != self.device or t.dtype != dt or not t.is_contiguous():
+                raise ValueError("spectra must be contiguous CUDA tensors (float32, float32, complex64) "
+                                 f"on {self.device}")
+            if tuple(t.shape) != (batch, self.n_screens, self.P):
+                raise ValueError(f"spectra shape {tuple(t.shape)} != {(batch, self.n_screens, self.P)}")
+        return _tptr(rho), _tptr(theta), _tptr(value)
+
+    def run(self, rho, theta, value, out: Optional[torch.Tensor] = None, field_out=None,
+            mean_intensity=None) -> torch.Tensor:
+        batch = self.batch if rho is None else int(rho.shape[0])
+        r, t, v = self._spectra(rho, theta, value, batch)
+        if out is None:
+            out = torch.empty((batch, self.n_out), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_run(self._handle, r, t, v, batch, _tptr(out), _tptr(field_out),
+                                   _tptr(mean_intensity), _stream(self.device)))
+        return out
+
+    def screen(self, rho, theta, value, screen: int, phi_out=None, phasor_out=None):
+        batch = int(rho.shape[0])
+        r, t, v = self._spectra(rho, theta, value, batch)
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_screen(self._handle, r, t, v, batch, int(screen), _tptr(phi_out),
+                                      _tptr(phasor_out), _stream(self.device)))
+        return phi_out, phasor_out
+
+    def vacuum(self, field: torch.Tensor, dz: float) -> torch.Tensor:
+        if field.dtype != torch.complex64 or not field.is_contiguous() or field.device != self.device:
+            raise ValueError("field must be a contiguous complex64 tensor on the plan's device")
+        batch = field.numel() // (self.N * self.N)
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_vacuum(self._handle, _tptr(field), batch, float(dz), _stream(self.device)))
+        return field
+
+    def measures(self, field: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        if field.dtype != torch.complex64 or not field.is_contiguous() or field.device != self.device:
+            raise ValueError("field must be a contiguous complex64 tensor on the plan's device")
+        batch = field.numel() // (self.N * self.N)
+        if out is None:
+            out = torch.empty((batch, self.n_out), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_measures(self._handle, _tptr(field), batch, _tptr(out), _stream(self.device)))
+        return out
+
+    # ------------------------------------------------------------------
+    def profile_begin(self, max_launches: int):
+        check(self.lib.atm_profile_begin(self._handle, int(max_launches)))
+
+    def profile_end(self) -> dict:
+        n = len(_lib.KIND_NAMES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int32 * n)()
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_profile_end(self._handle, ms, cnt, n))
+        return {k: {"ms": ms[i], "launches": cnt[i]} for i, k in enumerate(_lib.KIND_NAMES)}
+
+
+def fma_peak_tflops(device=None, blocks: int = 0, iters: int = 4096) -> float:
+    """Measured FP32 FMA throughput of the device (TFLOP/s), from the
+    engine's probe kernel; best of three launches after a warm-up."""
+    lib = load()
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else torch.device(device).index or 0)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks = blocks or sms * 8
+    best = None
+    with torch.cuda.device(dev):
+        for i in range(4):
+            ms = ctypes.c_double()
+            check(lib.atm_fma_probe(blocks, iters, ctypes.byref(ms), _stream(dev)))
+            if i > 0:
+                best = ms.value if best is None else min(best, ms.value)
+    flops = blocks * 256.0 * iters * 16.0
+    return flops / (best * 1e-3) / 1e12

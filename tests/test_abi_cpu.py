@@ -1,0 +1,88 @@
+"""CPU checks of the native layer: the library loads and exports every entry
+point of include/atm.h, and the kernels' FFT / Bessel / phase arithmetic (run
+on the host through libatm_selftest.so) is right."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def built():
+    from pyatmosphere_gb300 import build
+    return build.build()
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "atm.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(atm_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = ctypes.CDLL(built["libatm"])
+    names = declared_symbols()
+    assert len(names) >= 8
+    for n in names:
+        assert hasattr(lib, n), n
+    from pyatmosphere_gb300.engine import _lib
+    assert set(names) == set(_lib.SIGNATURES), "ctypes signatures must cover include/atm.h"
+    lib.atm_abi_version.restype = ctypes.c_int
+    assert lib.atm_abi_version() == 1
+
+
+def test_plan_create_rejects_bad_descriptors_without_gpu(built):
+    from pyatmosphere_gb300.engine import _lib
+    lib = _lib.load(built["libatm"])
+    d = _lib.AtmChannelDesc()
+    d.abi_version = 1
+    d.resolution = 100          # not a power of two
+    d.delta, d.wvl, d.w0, d.batch = 1e-3, 8e-7, 0.1, 1
+    h = ctypes.c_void_p()
+    assert lib.atm_plan_create(ctypes.byref(d), ctypes.byref(h)) == -2
+    assert b"resolution" in lib.atm_last_error()
+    d.resolution, d.abi_version = 256, 7
+    assert lib.atm_plan_create(ctypes.byref(d), ctypes.byref(h)) == -1
+
+
+@pytest.mark.parametrize("N", [64, 128, 256, 512, 1024, 2048, 4096])
+def test_kernel_fft_arithmetic_on_host(built, N):
+    from pyatmosphere_gb300.engine._lib import load_selftest
+    lib = load_selftest(built["selftest"])
+    rng = np.random.default_rng(N)
+    x = (rng.standard_normal(N) + 1j * rng.standard_normal(N)).astype(np.complex64)
+    for d in (-1, 1):
+        out = np.zeros(N, np.complex64)
+        assert lib.atm_selftest_fft(N, d, x.ctypes.data, out.ctypes.data) == 0
+        ref = np.fft.fft(x.astype(np.complex128)) if d < 0 else np.fft.ifft(x.astype(np.complex128)) * N
+        assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 3e-7
+
+
+def test_bessel_coefficients_on_host(built):
+    from scipy.special import jv
+    from pyatmosphere_gb300.engine._lib import load_selftest
+    lib = load_selftest(built["selftest"])
+    J = np.zeros(64)
+    for a in [1e-9, 1e-3, 0.7, 3.1, -9.4, 25.0]:
+        assert lib.atm_selftest_bessel(a, 64, J.ctypes.data) == 0
+        np.testing.assert_allclose(J, jv(np.arange(64), a), atol=1e-14)
+
+
+def test_fixed_point_phase_wrap_on_host(built):
+    """frac(j S + O) through 64-bit fixed point agrees with exact rational
+    arithmetic to float32 resolution, including phases of ~1e3 turns."""
+    from pyatmosphere_gb300.engine._lib import load_selftest
+    lib = load_selftest(built["selftest"])
+    from fractions import Fraction
+    for S, O in [(0.4999321, -512.25), (1e-7, 3.3), (0.123456789, -0.7)]:
+        out = np.zeros(4096, np.float32)
+        lib.atm_selftest_turns(S, O, 4096, out.ctypes.data)
+        for j in [0, 1, 17, 2047, 4095]:
+            t = Fraction(S) * j + Fraction(O)
+            frac = float(t - (t.numerator // t.denominator))
+            ref = frac if frac < 0.5 else frac - 1.0
+            got = out[j] / 2.0
+            assert abs(((got - ref) + 0.5) % 1.0 - 0.5) < 2e-7

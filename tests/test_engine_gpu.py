@@ -1,0 +1,182 @@
+"""Parity of the CUDA engine (through the C ABI) with the FP64 oracle.
+
+Tolerances: field rel-L2 <= 1e-4 against FP64 (the engine computes in
+complex64 / FP32 with FP64 phase arguments); moments to 1e-5 relative."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import atm_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return torch
+
+
+def make_plan(spec, batch=1, pupils=None, tracked=(), **kw):
+    from pyatmosphere_gb300.engine import EnginePlan
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    positions = o.screen_positions(spec.length, spec.count, spec.position) if spec.count else []
+    pupils = [(spec.pupil_radius,)] if pupils is None else pupils
+    return EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, positions, spec.length,
+                      f_base=base, losses_db=spec.losses_db, pupils=pupils, tracked=tracked,
+                      batch=batch, **kw), base
+
+
+def spectra(spec, base, seed, R):
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    return o.draw_spectra(seed, range(R), spec.count, base, psd)
+
+
+def to_dev(torch, *arrs):
+    return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrs]
+
+
+@pytest.mark.parametrize("N", [128, 256, 512, 1024, 2048, 4096])
+def test_vacuum_step_matches_oracle(torch_cuda, N):
+    torch = torch_cuda
+    d = 3.0 / N
+    spec = o.ChannelSpec(N=N, delta=d, w0=0.3, count=0, length=2e3)
+    plan, _ = make_plan(spec, batch=2, pupils=[])
+    rng = np.random.default_rng(N)
+    u0 = o.gaussian_source(N, d, spec.wvl, 0.3, math.inf)
+    noise = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * 0.2 * np.abs(u0)
+    fields = np.stack([u0, u0 + noise]).astype(np.complex64)
+    dev = torch.from_numpy(fields).cuda()
+    plan.vacuum(dev, 1234.5)
+    got = dev.cpu().numpy()
+    for b in range(2):
+        ref = o.vacuum(fields[b].astype(np.complex128), 1234.5, spec.k, d)
+        assert o.rel_l2(got[b], ref) < 2e-6
+
+
+@pytest.mark.parametrize("N,P,Cn2", [(128, 256, 1e-14), (512, 1024, 1e-15), (2048, 1024, 5e-16)])
+def test_screen_matches_oracle(torch_cuda, N, P, Cn2):
+    torch = torch_cuda
+    d = 1.0 / N if N < 2048 else 1.5e-3
+    spec = o.ChannelSpec(N=N, delta=d, points=P, Cn2=Cn2, count=2, length=10e3)
+    plan, base = make_plan(spec, batch=2)
+    rho, theta, value = spectra(spec, base, seed=N, R=2)
+    r, t, v = to_dev(torch, rho, theta, value)
+    phi = torch.empty((2, N, N), dtype=torch.float32, device="cuda")
+    ph = torch.empty((2, N, N), dtype=torch.complex64, device="cuda")
+    plan.screen(r, t, v, 1, phi_out=phi, phasor_out=ph)
+    phi, ph = phi.cpu().numpy(), ph.cpu().numpy()
+    for b in range(2):
+        ref = o.ss_screen(rho[b, 1], theta[b, 1], value[b, 1], N, d)
+        assert o.rel_l2(ph[b], np.exp(-1j * ref)) < 1e-5
+        # float32 output of a screen whose piston reaches ~1e3 rad
+        assert np.abs(phi[b] - ref).max() < 2e-4 * max(1.0, np.abs(ref).max() / 1e3)
+
+
+def run_engine(torch, spec, rho, theta, value, pupils=None, tracked=()):
+    R = rho.shape[0]
+    plan, _ = make_plan(spec, batch=R, pupils=pupils, tracked=tracked)
+    r, t, v = to_dev(torch, rho, theta, value)
+    field = torch.empty((R, spec.N, spec.N), dtype=torch.complex64, device="cuda")
+    meas = plan.run(r, t, v, field_out=field)
+    return plan, meas.cpu().numpy(), field.cpu().numpy()
+
+
+@pytest.mark.parametrize("position", ["middle", "before", "after"])
+def test_channel_run_matches_oracle(torch_cuda, position):
+    torch = torch_cuda
+    spec = o.ChannelSpec(N=256, delta=4e-3, w0=0.08, length=8e3, count=4, points=512, Cn2=2e-15,
+                         pupil_radius=0.1, position=position)
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    rho, theta, value = spectra(spec, base, seed=5, R=3)
+    plan, meas, field = run_engine(torch, spec, rho, theta, value)
+    for b in range(3):
+        res, u = o.simulate(spec, rho[b:b + 1], theta[b:b + 1], value[b:b + 1], return_field=True)
+        assert o.rel_l2(field[b], u) < FIELD_TOL
+        m = res[0]
+        for k, slot in [("eta_total", 0), ("mean_x", 1), ("mean_y", 2), ("mean_x2", 3), ("mean_xy", 4),
+                        ("mean_y2", 5), ("mean_x2_r", 6), ("eta_0", 8)]:
+            assert meas[b, slot] == pytest.approx(m[k], rel=2e-5, abs=2e-9), k
+
+
+def test_config1_realisations_match_oracle(torch_cuda):
+    """512^2, 5 screens, 1024 spectral points, pupil 0.12 m (config 1 geometry)."""
+    torch = torch_cuda
+    spec = o.ChannelSpec()
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    rho, theta, value = spectra(spec, base, seed=1234, R=4)
+    plan, meas, field = run_engine(torch, spec, rho, theta, value, tracked=(0.12,))
+    res, u = o.simulate(spec, rho[3:4], theta[3:4], value[3:4], return_field=True)
+    assert o.rel_l2(field[3], u) < FIELD_TOL
+    ref = o.simulate(spec, rho, theta, value)
+    for b in range(4):
+        assert meas[b, 8] == pytest.approx(ref[b]["eta_0"], rel=1e-5)
+        assert meas[b, 1] == pytest.approx(ref[b]["mean_x"], rel=1e-4, abs=1e-8)
+        # tracked pupil: mask centred on the engine's own centroid
+        I = np.abs(field[b].astype(np.complex128)) ** 2
+        mask = o.pupil_mask(spec.N, spec.delta, 0.12, shift=(meas[b, 1], meas[b, 2]))
+        assert meas[b, 9] == pytest.approx((I * mask).sum() * spec.delta ** 2, rel=1e-5)
+
+
+def test_measures_entry_matches_oracle(torch_cuda):
+    torch = torch_cuda
+    spec = o.ChannelSpec(N=512, delta=2e-3, count=0, length=3e3)
+    plan, _ = make_plan(spec, batch=2, pupils=[(0.05,), (0.1, 0.02, -0.01)], tracked=(0.07,))
+    rng = np.random.default_rng(3)
+    u = o.vacuum(o.gaussian_source(512, 2e-3, spec.wvl, 0.09, math.inf), 3e3, spec.k, 2e-3)
+    fields = np.stack([u, u * np.exp(1j * rng.standard_normal((512, 512)) * 0.1)]).astype(np.complex64)
+    got = plan.measures(torch.from_numpy(fields).cuda()).cpu().numpy()
+    for b in range(2):
+        f64 = fields[b].astype(np.complex128)
+        m = o.measures(f64, 2e-3, [0.05])
+        assert got[b, 0] == pytest.approx(m["eta_total"], rel=1e-6)
+        assert got[b, 3] == pytest.approx(m["mean_x2"], rel=1e-5)
+        I = np.abs(f64) ** 2
+        shifted = o.pupil_mask(512, 2e-3, 0.1, shift=(0.02, -0.01))
+        assert got[b, 9] == pytest.approx((I * shifted).sum() * 4e-6, rel=1e-6)
+
+
+def test_vacuum_known_answers_engine(torch_cuda):
+    """itest_vacuum_propagation cells 4-7 through the engine (VacuumPath channel)."""
+    torch = torch_cuda
+    N, d, wvl, w0, L = 256, 2e-3, 809e-9, 0.02, 4e3
+    spec = o.ChannelSpec(N=N, delta=d, wvl=wvl, w0=w0, count=0, length=L)
+    plan, _ = make_plan(spec, pupils=[])
+    field = torch.empty((1, N, N), dtype=torch.complex64, device="cuda")
+    m = plan.run(None, None, None, field_out=field).cpu().numpy()[0]
+    u = field.cpu().numpy()[0].astype(np.complex128)
+    assert m[0] == pytest.approx(1, abs=1e-6)
+    assert abs(u.sum()) * d ** 2 == pytest.approx(np.sqrt(2 * np.pi) * w0, abs=1e-7)
+    zR = np.pi * w0 ** 2 / wvl
+    assert np.sqrt(2 * (m[3] + m[5])) == pytest.approx(w0 * np.sqrt(1 + (L / zR) ** 2), abs=1e-7)
+
+
+@pytest.mark.parametrize("F0", [20000.0, 6000.0, -6000.0])
+def test_focused_beam_width(torch_cuda, F0):
+    """itest_sources cell 4 as assertions: sqrt(2 mean_r2) = GaussianBeam.get_w(L)."""
+    torch = torch_cuda
+    N, d, wvl, w0 = 512, 5e-3, 809e-9, 0.2
+    for L in [2000.0, 4000.0]:
+        spec = o.ChannelSpec(N=N, delta=d, wvl=wvl, w0=w0, F0=F0, count=0, length=L)
+        plan, _ = make_plan(spec, pupils=[])
+        m = plan.run(None, None, None).cpu().numpy()[0]
+        k = 2 * np.pi / wvl
+        theta0, lam0 = 1 - L / F0, 2 * L / k / w0 ** 2
+        w = w0 * np.sqrt(theta0 ** 2 + lam0 ** 2)
+        assert np.sqrt(2 * (m[3] + m[5])) == pytest.approx(w, rel=1e-4)
+
+
+def test_config2_geometry_matches_oracle(torch_cuda):
+    """2048^2, delta 1.5 mm, 50 km, 5 screens (config 2), one realisation vs FP64."""
+    torch = torch_cuda
+    spec = o.ChannelSpec(N=2048, delta=1.5e-3, w0=0.12, length=50e3, Cn2=5e-16, pupil_radius=0.2)
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    rho, theta, value = spectra(spec, base, seed=99, R=1)
+    plan, meas, field = run_engine(torch, spec, rho, theta, value)
+    res, u = o.simulate(spec, rho, theta, value, return_field=True)
+    assert o.rel_l2(field[0], u) < FIELD_TOL
+    assert meas[0, 8] == pytest.approx(res[0]["eta_0"], rel=1e-5)
