@@ -281,13 +281,14 @@ ATM_HD void bessel_j(double a, int D, double* J /* [D] */) {
     return;
   }
   const int n0 = D + (int)a + 40;
+  const double two_over_a = 2.0 / a;  // one FP64 divide, not one per step
   double jp1 = 0.0, j = 1e-200, norm = 0.0;
   for (int n = 0; n < D; ++n) J[n] = 0.0;
   for (int n = n0; n >= 1; --n) {
     // j = J_n (unnormalised), jp1 = J_{n+1}
     if (n < D) J[n] = j;
     if ((n & 1) == 0) norm += 2.0 * j;
-    const double jm1 = (2.0 * n / a) * j - jp1;
+    const double jm1 = ((double)n * two_over_a) * j - jp1;
     jp1 = j;
     j = jm1;
     if (fabs(j) > 1e200) {  // rescale to stay in range

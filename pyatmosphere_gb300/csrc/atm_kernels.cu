@@ -282,7 +282,7 @@ cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t 
 // is accumulated in FP64, the interior in FP32 per chunk of 32 annuli.
 // ---------------------------------------------------------------------------
 constexpr int kPrepThreads = 256;
-constexpr int kPrepChunk = 32;
+constexpr int kPrepChunk = 64;
 constexpr int kMaxD = 64;
 
 struct LowTerm {
@@ -370,33 +370,37 @@ __global__ void __launch_bounds__(kPrepThreads) screen_prep_kernel(ScreenArgs a)
       bessel_j(low[p0 + tid].ay, D, Jy + tid * D);
       for (int n = 0; n < D; ++n) Jyf[tid * D + n] = (float)Jy[tid * D + n];
       vf[tid] = make_float2((float)low[p0 + tid].vr, (float)low[p0 + tid].vi);
-    } else if (tid >= 64 && tid - 64 < np) {
-      const int q = tid - 64;
+    } else if (tid >= kPrepChunk && tid - kPrepChunk < np) {
+      const int q = tid - kPrepChunk;
       bessel_j(low[p0 + q].ax, D, Jx + q * D);
       for (int n = 0; n < D; ++n) Jxf[q * D + n] = (float)Jx[q * D + n];
     }
     __syncthreads();
-    for (int ed = tid; ed < D * D; ed += blockDim.x) {
-      const int e = ed / D, d = ed - e * D;
-      if (e == 0 || d == 0) {
-        double ar = 0.0, ai = 0.0;
-        for (int q = 0; q < np; ++q) {
-          const double w = Jy[q * D + e] * Jx[q * D + d];
-          ar = fma(low[p0 + q].vr, w, ar);
-          ai = fma(low[p0 + q].vi, w, ai);
-        }
-        S[ed].x += ar;
-        S[ed].y += ai;
-      } else {
-        float ar = 0.f, ai = 0.f;
-        for (int q = 0; q < np; ++q) {
-          const float w = Jyf[q * D + e] * Jxf[q * D + d];
-          ar = fmaf(vf[q].x, w, ar);
-          ai = fmaf(vf[q].y, w, ai);
-        }
-        S[ed].x += (double)ar;
-        S[ed].y += (double)ai;
+    // interior (e, d >= 1) in FP32 per chunk; one FP64 add per chunk
+    const int Di = D - 1;
+    for (int idx = tid; idx < Di * Di; idx += blockDim.x) {
+      const int e = 1 + idx / Di, d = 1 + idx % Di;
+      float ar = 0.f, ai = 0.f;
+      for (int q = 0; q < np; ++q) {
+        const float w = Jyf[q * D + e] * Jxf[q * D + d];
+        ar = fmaf(vf[q].x, w, ar);
+        ai = fmaf(vf[q].y, w, ai);
       }
+      S[e * D + d].x += (double)ar;
+      S[e * D + d].y += (double)ai;
+    }
+    // edge row e = 0 and column d = 0 (piston and tilts) in FP64, by
+    // dedicated threads so no warp carries both paths
+    for (int idx = tid; idx < 2 * D - 1; idx += blockDim.x) {
+      const int e = idx < D ? 0 : idx - D + 1, d = idx < D ? idx : 0;
+      double ar = 0.0, ai = 0.0;
+      for (int q = 0; q < np; ++q) {
+        const double w = Jy[q * D + e] * Jx[q * D + d];
+        ar = fma(low[p0 + q].vr, w, ar);
+        ai = fma(low[p0 + q].vi, w, ai);
+      }
+      S[e * D + d].x += ar;
+      S[e * D + d].y += ai;
     }
     __syncthreads();
   }
