@@ -177,6 +177,23 @@ int atm_profile_end(AtmPlan* plan, double* ms_by_kind, int32_t* launches_by_kind
  * the roofline denominator for the FP32 screen GEMM. */
 int atm_fma_probe(int32_t blocks, int32_t iters, double* ms, void* stream);
 
+/* Allocation-free variant of atm_vacuum, for callers that cannot allocate
+ * device memory where they propagate (their framework's caching allocator
+ * owns the memory budget, or they cannot afford cudaFree's implicit device
+ * synchronisation).  No counterpart in the reference: it exists for such
+ * callers of this library.  One vacuum step of length dz, in place on the
+ * caller's spatial field [batch][N][N] complex64 (device), for a grid of
+ * step `delta` and wavelength `wvl`; dz <= 0 leaves the field unchanged.
+ * Needs no plan and calls no cudaMalloc / cudaFree: its tables live in one
+ * static device array of 3 x 4096 complex64 (96 KiB) held by every GPU that
+ * loads the library, so N must be a power of two in [128, 4096] (larger N:
+ * ATM_ERR_UNSUPPORTED).  The first call on a device looks up that array's
+ * address (cudaGetSymbolAddress, once per device); make it before capturing
+ * any stream.  All calls share the array: calls whose GPU work overlaps
+ * (unordered streams) race on it. */
+int atm_vacuum_noalloc(void* field, int32_t N, int32_t batch, double delta, double wvl, double dz,
+                       void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,6 +112,16 @@ std::vector<float2> to_c64(const std::vector<cd>& v) {
 
 }  // namespace
 
+int atm::set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
 struct AtmPlan {
   int device = 0;
   int N = 0, n = 0, P = 0, B = 0, n_pupils = 0, n_tracked = 0;

@@ -129,5 +129,7 @@ int row_pass_rows(int N);          // rows per CTA of the row pass
 int col_tile_default(int N);
 bool supported_n(int N);
 size_t prep_smem_bytes(int P_L, int D);
+// records the message returned by atm_last_error() on this host thread; returns code
+int set_error(int code, const char* fmt, ...);
 
 }  // namespace atm

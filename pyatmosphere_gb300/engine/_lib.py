@@ -99,6 +99,8 @@ SIGNATURES = {
     "atm_profile_end": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "atm_fma_probe": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                      ctypes.c_void_p]),
+    "atm_vacuum_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
 }
 
 KIND_NAMES = ["screen_prep", "screen_table", "screen_gemm", "row_pass", "col_pass", "finalize", "tracked"]
