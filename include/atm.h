@@ -152,6 +152,19 @@ int atm_vacuum(AtmPlan* plan, void* field, int32_t batch, double dz, void* strea
  * (pupils.py:12-13) and BeamResult.mean_x2_r (simulations/beam.py:26-33). */
 int atm_measures(AtmPlan* plan, const void* field, int32_t batch, double* measures_out, void* stream);
 
+/* FFT phase screens with subharmonics for every realisation in the batch.
+ * Replaces FFTPhaseScreen.generate(complex=True) (phase_screens.py:37-67):
+ * spectrum (a + i b) amp on the centred frequency grid (DC = 0), centred
+ * inverse 2-D FFT times N^2, plus the 3x3 subharmonic levels, minus the
+ * mean.  The engine's own FFT passes run it without shift copies; the
+ * subharmonic sum sum_j X_j(x) Y_j(y) comes as FP64-built 1-D factors.
+ *   normals    [batch][2][N][N] float32 (real, imaginary draws of the main grid)
+ *   amp        [N][N] float32 sqrt(Phi_phi(|f|)) 2 pi df, centred order
+ *   sub_x, sub_y [batch][n_sub][N] complex64; sub_mean [batch][2] float64
+ *   screen_out [batch][N][N] complex64 (its real part is the phase) */
+int atm_fft_screen(AtmPlan* plan, const float* normals, const float* amp, const void* sub_x, const void* sub_y,
+                   const double* sub_mean, int32_t n_sub, int32_t batch, void* screen_out, void* stream);
+
 /* Launch categories reported by atm_profile_end. */
 #define ATM_KIND_SCREEN_PREP 0
 #define ATM_KIND_SCREEN_TABLE 1

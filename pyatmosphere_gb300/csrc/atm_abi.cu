@@ -708,6 +708,49 @@ int atm_vacuum(AtmPlan* pl, void* field, int32_t batch, double dz, void* stream)
   return ATM_OK;
 }
 
+int atm_fft_screen(AtmPlan* pl, const float* normals, const float* amp, const void* sub_x, const void* sub_y,
+                   const double* sub_mean, int32_t n_sub, int32_t batch, void* screen_out, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
+  if (!normals || !amp || !screen_out) return fail(ATM_ERR_INVALID, "NULL input / output");
+  if (n_sub < 0 || (n_sub > 0 && (!sub_x || !sub_y))) return fail(ATM_ERR_INVALID, "bad subharmonic tables");
+  if (!sub_mean) return fail(ATM_ERR_INVALID, "sub_mean is NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  atm::FftScreenArgs fa{};
+  fa.normals = normals;
+  fa.amp = amp;
+  fa.sub_x = (const float2*)sub_x;
+  fa.sub_y = (const float2*)sub_y;
+  fa.sub_mean = sub_mean;
+  fa.n_sub = n_sub;
+  fa.N = pl->N;
+  fa.field = (float2*)pl->field.p;
+  fa.out = (float2*)screen_out;
+  ATM_CUDA(atm::launch_fft_screen_spectrum(batch, fa, st));
+  atm::RowArgs ra{};
+  ra.field = (float2*)pl->field.p;
+  ra.tw = (const float2*)pl->tw.p;
+  ra.loss = 1.f;
+  ra.delta = (float)pl->delta;
+  ra.delta64 = pl->delta;
+  ra.flags = atm::ROW_INV | atm::ROW_STORE;
+  {
+    Prof p(pl, ATM_KIND_ROW_PASS, st);
+    ATM_CUDA(atm::launch_row_pass(pl->N, batch, ra, st));
+  }
+  atm::ColArgs ca{};
+  ca.field = (float2*)pl->field.p;
+  ca.tw = (const float2*)pl->tw.p;
+  ca.inv_only = 1;
+  {
+    Prof p(pl, ATM_KIND_COL_PASS, st);
+    ATM_CUDA(atm::launch_col_pass(pl->N, batch, pl->col_tile, ca, st));
+  }
+  ATM_CUDA(atm::launch_fft_screen_finish(batch, fa, st));
+  return ATM_OK;
+}
+
 int atm_profile_begin(AtmPlan* pl, int32_t max_launches) {
   if (!pl || max_launches < 1) return fail(ATM_ERR_INVALID, "bad profile arguments");
   if (int rc = check_device(pl)) return rc;

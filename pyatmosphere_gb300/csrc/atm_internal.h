@@ -56,6 +56,20 @@ struct ColArgs {
   const float2* tw;
   const float2* hy;         // [N] transfer function along y incl. exp(i k dz) / N^2
   const float2* hx;         // [N] transfer function along x
+  int inv_only;             // 1: inverse column FFT only (no forward FFT, no H)
+};
+
+// FFT screen (phase_screens.py:42-67) without shifts: screen[y][x] =
+// (-1)^(x+y) IFFT2((-1)^(kx+ky) cn) + sum_j X_j[x] Y_j[y] - mean
+struct FftScreenArgs {
+  const float* normals;     // [B][2][N][N] real / imaginary standard normals (main grid)
+  const float* amp;         // [N][N] sqrt(Phi_phi(|f|)) 2 pi df, centred order, DC = 0
+  const float2* sub_x;      // [B][n_sub][N] subharmonic x factors (FP64-computed)
+  const float2* sub_y;      // [B][n_sub][N] subharmonic y factors
+  const double* sub_mean;   // [B][2] mean of the subharmonic part (re, im)
+  int n_sub, N;
+  float2* field;            // [B][N][N] workspace
+  float2* out;              // [B][N][N] complex screen
 };
 
 // one high-frequency spectral term, phases as 64-bit binary fractions of a turn
@@ -122,6 +136,8 @@ cudaError_t launch_screen_gemm(int B, const GemmArgs& a, cudaStream_t st);
 cudaError_t launch_compose_screen(int B, int N, const double* Gy, const double* Hx, const float* phiG,
                                   const float2* Py, const float2* Px, float* phi_out, float2* phasor_out,
                                   cudaStream_t st);
+cudaError_t launch_fft_screen_spectrum(int B, const FftScreenArgs& a, cudaStream_t st);
+cudaError_t launch_fft_screen_finish(int B, const FftScreenArgs& a, cudaStream_t st);
 cudaError_t launch_finalize(int B, const FinalArgs& a, cudaStream_t st);
 cudaError_t launch_tracked(int B, const TrackedArgs& a, cudaStream_t st);
 cudaError_t launch_fma_probe(int blocks, int iters, cudaStream_t st);

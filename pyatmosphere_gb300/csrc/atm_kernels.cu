@@ -7,6 +7,9 @@
 //   row_pass      (inverse row FFT, exp(-i phi) multiply, forward row FFT)
 //   col_pass      (forward column FFT, H(fy,fx,dz), inverse column FFT)
 // and one last row_pass with the pupil / moment reductions, then finalize.
+#include <algorithm>
+#include <cstdint>
+
 #include "atm_common.cuh"
 #include "atm_internal.h"
 
@@ -26,6 +29,19 @@ __device__ __forceinline__ void fft_dev(float2 (&v)[16], float2* sm, int t, cons
     __syncthreads();
     fft_dev<N, DIR, s + 1>(v, sm, t, tw);
   }
+}
+
+// ---------------------------------------------------------------------------
+// asynchronous global -> shared copies (16 bytes, L1 bypass)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int n>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory");
 }
 
 // rows per CTA of the row pass: about 256 threads per CTA
@@ -53,7 +69,8 @@ bool supported_n(int N) { return row_pass_rows(N) > 0; }
 // reduction; one partial vector per CTA and realisation
 // ---------------------------------------------------------------------------
 template <int N, int ROWS>
-__device__ __forceinline__ void measure_row(const RowArgs& a, const float2 (&v)[16], int t, int y, int r) {
+__device__ __forceinline__ void measure_row(const RowArgs& a, const float2 (&v)[16], int t, int y, int r,
+                                            int part, int n_parts) {
   constexpr int T = N / 16;
   constexpr int NT = ROWS * T;
   constexpr int NW = (NT + 31) / 32;
@@ -108,8 +125,9 @@ __device__ __forceinline__ void measure_row(const RowArgs& a, const float2 (&v)[
     double s = 0.0;
 #pragma unroll
     for (int i = 0; i < NW; ++i) s += red[i][threadIdx.x];
-    a.partials[((size_t)r * gridDim.x + blockIdx.x) * a.n_meas + threadIdx.x] = s;
+    a.partials[((size_t)r * n_parts + part) * a.n_meas + threadIdx.x] = s;
   }
+  __syncthreads();  // red[] is reused by the next row of a persistent CTA
 }
 
 // ---------------------------------------------------------------------------
@@ -161,11 +179,134 @@ row_pass_kernel(RowArgs a) {
 #pragma unroll
     for (int m = 0; m < 16; ++m) dst[rowoff + t + m * T] = v[m];
   }
-  if (flags & ROW_MEAS) measure_row<N, ROWS>(a, v, t, y, r);
+  if (flags & ROW_MEAS) measure_row<N, ROWS>(a, v, t, y, r, blockIdx.x, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// persistent row pass: each CTA walks (realisation, row block) items and
+// prefetches the next item's rows (and screen rows) with cp.async into the
+// other half of a double buffer while it transforms the current one.  The
+// stage buffer doubles as the FFT exchange area once its rows are in
+// registers.
+// ---------------------------------------------------------------------------
+template <int N>
+struct RowPipe {
+  static constexpr int ROWS = RowRows<N>::value;
+  static constexpr size_t FIELD = (size_t)ROWS * Padded<N>::value * sizeof(float2);
+  static constexpr size_t PHI = (size_t)ROWS * N * sizeof(float);
+  static constexpr size_t STAGE = FIELD + PHI;
+  static constexpr size_t SMEM = 2 * STAGE;
+};
+
+template <int N>
+__global__ void __launch_bounds__(RowRows<N>::value * (N / 16))
+row_pass_pipe_kernel(RowArgs a, int n_items) {
+  constexpr int T = N / 16;
+  constexpr int ROWS = RowRows<N>::value;
+  constexpr int P = Padded<N>::value;
+  constexpr int NT = ROWS * T;
+  constexpr int NRB = N / ROWS;  // row blocks per realisation
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x;
+  const int rl = tid / T, t = tid - rl * T;
+  const int flags = a.flags;
+  const bool load_field = !(flags & ROW_GEN);
+  const bool load_phi = (flags & ROW_PHASOR) != 0;
+
+  auto fbuf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * RowPipe<N>::STAGE); };
+  auto pbuf = [&](int s) { return reinterpret_cast<float*>(smem_raw + s * RowPipe<N>::STAGE + RowPipe<N>::FIELD); };
+  auto prefetch = [&](int item, int s) {
+    const int r = item / NRB, y0 = (item - r * NRB) * ROWS;
+    const size_t off = (size_t)r * N * N + (size_t)y0 * N;
+    if (load_field) {
+      const float2* src = a.field + off;
+      float2* dst = fbuf(s);
+      for (int c = tid; c < ROWS * N / 2; c += NT) {
+        const int row = c / (N / 2), col = (c - row * (N / 2)) * 2;
+        cp_async16(dst + row * P + col, src + (size_t)row * N + col);
+      }
+    }
+    if (load_phi) {
+      const float* src = a.phi + off;
+      float* dst = pbuf(s);
+      for (int c = tid; c < ROWS * N / 4; c += NT) cp_async16(dst + c * 4, src + c * 4);
+    }
+  };
+
+  int item = blockIdx.x, s = 0;
+  if (item < n_items) prefetch(item, 0);
+  cp_async_commit();
+  for (; item < n_items; item += gridDim.x, s ^= 1) {
+    const int next = item + gridDim.x;
+    if (next < n_items) prefetch(next, s ^ 1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const int r = item / NRB, rb = item - r * NRB;
+    const int y = rb * ROWS + rl;
+    float2* sm = fbuf(s) + rl * P;
+    const size_t rowoff = (size_t)r * N * N + (size_t)y * N;
+    float2 v[16];
+    if (!load_field) {
+      const float2 gy = a.ay[y];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(gy, a.ax[t + m * T]);
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = sm[t + m * T];
+    }
+    __syncthreads();  // the exchange below overwrites the staged rows
+    if (flags & ROW_INV) fft_dev<N, 1>(v, sm, t, a.tw);
+    if (load_phi) {
+      const float2 py = cscale(a.Py[(size_t)r * N + y], a.loss);
+      const float* ph = pbuf(s) + rl * N;
+      const float2* px = a.Px + (size_t)r * N;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int x = t + m * T;
+        float sn, cs;
+        sincosf(ph[x], &sn, &cs);
+        v[m] = cmul(v[m], cmul(cmul(py, px[x]), make_float2(cs, -sn)));
+      }
+    } else if (a.loss != 1.0f) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cscale(v[m], a.loss);
+    }
+    if (flags & ROW_FWD) fft_dev<N, -1>(v, sm, t, a.tw);
+    if (flags & ROW_STORE) {
+      float2* dst = (a.store_out && a.out) ? a.out : a.field;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) dst[rowoff + t + m * T] = v[m];
+    }
+    if (flags & ROW_MEAS) measure_row<N, ROWS>(a, v, t, y, r, rb, NRB);
+    __syncthreads();  // stage s is refilled by the next iteration's prefetch
+  }
+  cp_async_wait<0>();
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+template <int N>
+static cudaError_t row_pipe_launch(int B, const RowArgs& a, cudaStream_t st) {
+  constexpr int ROWS = RowRows<N>::value;
+  const int threads = ROWS * (N / 16);
+  const size_t smem = RowPipe<N>::SMEM;
+  cudaError_t e = cudaFuncSetAttribute(row_pass_pipe_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_pass_pipe_kernel<N>, threads, smem);
+  if (e != cudaSuccess) return e;
+  const int n_items = B * (N / ROWS);
+  const int grid = std::max(1, std::min(n_items, sms * std::max(per_sm, 1)));
+  row_pass_pipe_kernel<N><<<grid, threads, smem, st>>>(a, n_items);
+  return cudaGetLastError();
 }
 
 template <int N>
-static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
+static cudaError_t row_plain_launch(int B, const RowArgs& a, cudaStream_t st) {
   constexpr int ROWS = RowRows<N>::value;
   const int threads = ROWS * (N / 16);
   const size_t smem = (size_t)ROWS * Padded<N>::value * sizeof(float2);
@@ -176,6 +317,14 @@ static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   dim3 grid(N / ROWS, B);
   row_pass_kernel<N><<<grid, threads, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
+  const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
+  const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
+  if (field_ok && phi_ok) return row_pipe_launch<N>(B, a, st);
+  return row_plain_launch<N>(B, a, st);
 }
 
 cudaError_t launch_row_pass(int N, int B, const RowArgs& a, cudaStream_t st) {
@@ -215,17 +364,103 @@ col_pass_kernel(ColArgs a) {
   float2 v[16];
 #pragma unroll
   for (int m = 0; m < 16; ++m) v[m] = f[(size_t)(t + m * T) * N];
-  fft_dev<N, -1>(v, sm, t, a.tw);
-  const float2 hx = a.hx[x];
+  if (!a.inv_only) {
+    fft_dev<N, -1>(v, sm, t, a.tw);
+    const float2 hx = a.hx[x];
 #pragma unroll
-  for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(a.hy[t + m * T], hx));
+    for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(a.hy[t + m * T], hx));
+  }
   fft_dev<N, 1>(v, sm, t, a.tw);
 #pragma unroll
   for (int m = 0; m < 16; ++m) f[(size_t)(t + m * T) * N] = v[m];
 }
 
+// ---------------------------------------------------------------------------
+// persistent column pass: each CTA walks (realisation, column tile) items;
+// the next tile (N rows x C columns) is prefetched with cp.async into the
+// other half of a double buffer while the current one is transformed.  The
+// staged tile is row-major [y][c]; once in registers the buffer is reused as
+// the padded column-major FFT exchange area.
+// ---------------------------------------------------------------------------
 template <int N, int C>
-static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
+struct ColPipe {
+  static constexpr size_t TILE = (size_t)N * C * sizeof(float2);
+  static constexpr size_t EXCH = (size_t)C * ColStride<N, C>::value * sizeof(float2);
+  static constexpr size_t STAGE = ((TILE > EXCH ? TILE : EXCH) + 127) / 128 * 128;
+  static constexpr size_t SMEM = 2 * STAGE;
+};
+
+template <int N, int C>
+__global__ void __launch_bounds__(C * (N / 16))
+col_pass_pipe_kernel(ColArgs a, int n_items) {
+  constexpr int T = N / 16;
+  constexpr int S = ColStride<N, C>::value;
+  constexpr int NT = C * T;
+  constexpr int NCT = N / C;  // column tiles per realisation
+  constexpr int CH = C / 2;   // 16-byte chunks per tile row
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  auto buf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * ColPipe<N, C>::STAGE); };
+  auto prefetch = [&](int item, int s) {
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
+    const float2* src = a.field + (size_t)r * N * N + x0;
+    float2* dst = buf(s);
+    for (int q = threadIdx.x; q < N * CH; q += NT) {
+      const int row = q / CH, part = q - row * CH;
+      cp_async16(dst + row * C + part * 2, src + (size_t)row * N + part * 2);
+    }
+  };
+  int item = blockIdx.x, s = 0;
+  if (item < n_items) prefetch(item, 0);
+  cp_async_commit();
+  for (; item < n_items; item += gridDim.x, s ^= 1) {
+    const int next = item + gridDim.x;
+    if (next < n_items) prefetch(next, s ^ 1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const int r = item / NCT, x = (item - r * NCT) * C + c;
+    float2* tile = buf(s);
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = tile[(t + m * T) * C + c];
+    __syncthreads();  // the exchange below overwrites the staged tile
+    float2* sm = tile + c * S;
+    if (!a.inv_only) {
+      fft_dev<N, -1>(v, sm, t, a.tw);
+      const float2 hx = a.hx[x];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(a.hy[t + m * T], hx));
+    }
+    fft_dev<N, 1>(v, sm, t, a.tw);
+    float2* f = a.field + (size_t)r * N * N + x;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) f[(size_t)(t + m * T) * N] = v[m];
+    __syncthreads();  // stage s is refilled by the next iteration's prefetch
+  }
+  cp_async_wait<0>();
+}
+
+template <int N, int C>
+static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
+  const int threads = C * (N / 16);
+  const size_t smem = ColPipe<N, C>::SMEM;
+  cudaError_t e = cudaFuncSetAttribute(col_pass_pipe_kernel<N, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_pass_pipe_kernel<N, C>, threads, smem);
+  if (e != cudaSuccess) return e;
+  const int n_items = B * (N / C);
+  const int grid = std::max(1, std::min(n_items, sms * std::max(per_sm, 1)));
+  col_pass_pipe_kernel<N, C><<<grid, threads, smem, st>>>(a, n_items);
+  return cudaGetLastError();
+}
+
+template <int N, int C>
+static cudaError_t col_plain_launch(int B, const ColArgs& a, cudaStream_t st) {
   const int threads = C * (N / 16);
   const size_t smem = (size_t)C * ColStride<N, C>::value * sizeof(float2);
   if (smem > 48 * 1024) {
@@ -235,6 +470,12 @@ static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
   dim3 grid(N / C, B);
   col_pass_kernel<N, C><<<grid, threads, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int N, int C>
+static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
+  if (C >= 2 && aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024) return col_pipe_launch<N, C>(B, a, st);
+  return col_plain_launch<N, C>(B, a, st);
 }
 
 // largest tile that keeps the CTA at <= 512 threads (no register spills)
@@ -599,6 +840,51 @@ cudaError_t launch_compose_screen(int B, int N, const double* Gy, const double* 
                                   cudaStream_t st) {
   dim3 grid((N + 255) / 256, N, B);
   compose_screen_kernel<<<grid, 256, 0, st>>>(Gy, Hx, phiG, Py, Px, phi_out, phasor_out, N);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FFT screen: spectrum with the (-1)^(kx+ky) factor, then (after an
+// unnormalised inverse 2-D FFT by the row and column passes) the (-1)^(x+y)
+// factor, the separable subharmonic sum and the mean
+// ---------------------------------------------------------------------------
+__global__ void fft_screen_spectrum_kernel(FftScreenArgs a) {
+  const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ky = blockIdx.y, r = blockIdx.z, N = a.N;
+  if (kx >= N) return;
+  const size_t plane = (size_t)N * N, o = (size_t)ky * N + kx;
+  const float sgn = ((kx + ky) & 1) ? -1.f : 1.f;
+  const float amp = a.amp[o] * sgn;
+  const float* nr = a.normals + (size_t)r * 2 * plane;
+  a.field[(size_t)r * plane + o] = make_float2(nr[o] * amp, nr[plane + o] * amp);
+}
+
+cudaError_t launch_fft_screen_spectrum(int B, const FftScreenArgs& a, cudaStream_t st) {
+  dim3 grid((a.N + 255) / 256, a.N, B);
+  fft_screen_spectrum_kernel<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+__global__ void fft_screen_finish_kernel(FftScreenArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, r = blockIdx.z, N = a.N;
+  if (x >= N) return;
+  const size_t plane = (size_t)N * N, o = (size_t)y * N + x;
+  float2 v = a.field[(size_t)r * plane + o];
+  if ((x + y) & 1) v = make_float2(-v.x, -v.y);
+  const float2* sx = a.sub_x + (size_t)r * a.n_sub * N;
+  const float2* sy = a.sub_y + (size_t)r * a.n_sub * N;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int j = 0; j < a.n_sub; ++j) acc = cadd(acc, cmul(sx[(size_t)j * N + x], sy[(size_t)j * N + y]));
+  v = cadd(v, acc);
+  v.x -= (float)a.sub_mean[2 * r];
+  v.y -= (float)a.sub_mean[2 * r + 1];
+  a.out[(size_t)r * plane + o] = v;
+}
+
+cudaError_t launch_fft_screen_finish(int B, const FftScreenArgs& a, cudaStream_t st) {
+  dim3 grid((a.N + 255) / 256, a.N, B);
+  fft_screen_finish_kernel<<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 

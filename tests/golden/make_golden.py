@@ -211,6 +211,27 @@ def main(ref_path):
     g["fft_normals"] = np.stack([np.stack(draws[0:2])], 0)
     g["fft_sub_normals"] = np.stack([np.stack(draws[2 + 2 * i:4 + 2 * i]) for i in range(3)], 0)
 
+    # 8. seeded runs through the public API (numpy global RNG, no injection):
+    #    Channel.run and a Simulation with Beam / PDT / TrackedPDT results
+    spec = orc.ChannelSpec(N=128, delta=3e-3, w0=0.06, length=5e3, count=3, points=256, Cn2=2e-15,
+                           pupil_radius=0.08)
+    np.random.seed(123)
+    ch = make_channel(pa, **spec_kwargs(spec))
+    u = ch.run(pupil=False)
+    g["seeded_run_field"] = np.asarray(u, np.complex64)
+    from pyatmosphere import simulations
+    np.random.seed(321)
+    ch = make_channel(pa, **spec_kwargs(spec))
+    beam = simulations.BeamResult(ch, max_size=3)
+    pdt = simulations.PDTResult(ch, max_size=5)
+    tpdt = simulations.TrackedPDTResult(ch, max_size=5)
+    sim = simulations.Simulation([beam, pdt, tpdt])
+    sim.run()
+    for i, nm in enumerate(["mean_x", "mean_y", "mean_x2", "mean_xy", "mean_y2", "mean_x2_r"]):
+        g[f"seeded_sim_{nm}"] = np.array(beam.measures[i].data)
+    g["seeded_sim_eta"] = np.array(pdt.measures[0].data)
+    g["seeded_sim_tracked_eta"] = np.array(tpdt.measures[2].data)
+
     out = os.path.join(HERE, "golden.npz")
     np.savez_compressed(out, **{k: np.asarray(v) for k, v in g.items()})
     print("wrote", out, os.path.getsize(out), "bytes")

@@ -1,0 +1,75 @@
+"""Host-side pieces of the API mirror: spectra drawing, PSD weights, result
+CSV persistence, measure classification for the batched path."""
+import numpy as np
+import pytest
+
+from oracle import atm_oracle as o
+
+
+def test_spectrum_draws_match_oracle():
+    from pyatmosphere_gb300.engine.spectra import draw_spectra
+    spec = o.ChannelSpec()
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    a = draw_spectra(9, range(3), 5, base, psd)
+    b = o.draw_spectra(9, range(3), 5, base, psd)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_psd_weights_match_reference(golden):
+    from pyatmosphere_gb300.engine.spectra import annulus_psd
+    from pyatmosphere_gb300.theory.models import MVKModel
+    for cfg, (Cn2, L) in {"c1": (1e-15, 10e3), "c2": (5e-16, 50e3)}.items():
+        m = MVKModel(Cn2=Cn2, l0=6e-3, L0=1e3)
+        psd = annulus_psd(golden[f"{cfg}_base"], m.psd_phi_f, 2 * np.pi / 808e-9, L / 5)
+        np.testing.assert_allclose(psd, golden[f"{cfg}_psd"], rtol=2e-7)
+
+
+def test_screen_spectrum_follows_reference_rng_order():
+    """SSPhaseScreen._get_spectrum draws u, then P uniforms, then 2P normals
+    from numpy's global RNG (grids.py:98-107, phase_screens.py:98-103)."""
+    import pyatmosphere_gb300 as pa
+    fg = pa.RandLogPolarGrid(points=64, f_min=1e-4, f_max=300)
+    ps = pa.SSPhaseScreen(fg, pa.MVKModel(1e-15, 6e-3, 1e3), thickness=1e3, wvl=808e-9,
+                          grid=pa.RectGrid(128, 2e-3))
+    np.random.seed(4)
+    sp = ps._get_spectrum(False)
+    np.random.seed(4)
+    u = np.random.random(size=(1,)).astype(np.float32)
+    t = np.random.random(size=(64,)).astype(np.float32)
+    ab = np.random.normal(size=(2, 64))
+    base = fg.base
+    fp = np.insert(base, 0, 0)[:-1]
+    assert np.array_equal(sp.rho, np.sqrt(fp ** 2 + u * (base ** 2 - fp ** 2)))
+    assert np.array_equal(sp.theta, 2 * np.pi * t)
+    assert np.array_equal(sp.value, (ab[0] + 1j * ab[1]).astype(np.complex64) * np.sqrt(ps._get_psd()))
+
+
+def test_result_csv_round_trip(tmp_path):
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import simulations
+    ch = pa.QuickChannel()
+    path = str(tmp_path / "pdt.csv")
+    r = simulations.PDTResult(ch, max_size=10, save_path=path)
+    r.measures[0].data = [0.123456, 0.5, 1e-7]
+    r.save_output()
+    text = open(path).read().splitlines()
+    assert text[0] == "0.02" and text[1] == "1.235e-01"
+    r2 = simulations.PDTResult(ch, max_size=10, save_path=path)
+    assert r2.measures[0].data == pytest.approx([0.1235, 0.5, 1e-7], rel=1e-3)
+
+
+def test_batched_path_classification():
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import measures, simulations
+    ch = pa.QuickChannel()
+    sim = simulations.Simulation([simulations.BeamResult(ch, max_size=2), simulations.PDTResult(ch, max_size=2),
+                                  simulations.TrackedPDTResult(ch, max_size=2)])
+    plans = sim._batch_plan()
+    kinds = sorted({k[0] for _, k in plans[ch]})
+    assert kinds == ["pupil", "slot", "tracked"]
+    sim2 = simulations.Simulation(measures_list=[simulations.Measure(ch, "atmosphere", lambda c, output: 0.0)])
+    assert sim2._batch_plan() is None
+    sim3 = simulations.Simulation(measures_list=[simulations.Measure(ch, "pupil", measures.eta, time=[0, 1])])
+    assert sim3._batch_plan() is None

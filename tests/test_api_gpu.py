@@ -1,0 +1,152 @@
+"""The reference-facing Python API on the engine: seeded runs reproduce the
+reference's own realisations (same numpy RNG order), the batched Simulation
+path agrees with the per-realisation path, and the step-by-step path object
+agrees with the fused channel run."""
+import numpy as np
+import pytest
+
+from oracle import atm_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+# the reference computes screens with float32 phase arguments: ~2-5e-4 field error
+REF_TOL = 2e-3
+
+
+def small_channel(pa):
+    return pa.Channel(
+        grid=pa.RectGrid(resolution=128, delta=3e-3),
+        source=pa.GaussianSource(wvl=808e-9, w0=0.06, F0=np.inf),
+        path=pa.IdenticalPhaseScreensPath(
+            phase_screen=pa.SSPhaseScreen(model=pa.MVKModel(Cn2=2e-15, l0=6e-3, L0=1e3),
+                                          f_grid=pa.RandLogPolarGrid(points=256, f_min=1 / 1e3 / 15,
+                                                                     f_max=2 / 6e-3)),
+            length=5e3, count=3),
+        pupil=pa.CirclePupil(radius=0.08))
+
+
+def test_seeded_channel_run_reproduces_reference(golden):
+    import pyatmosphere_gb300 as pa
+    np.random.seed(123)
+    u = small_channel(pa).run(pupil=False).cpu().numpy()
+    assert o.rel_l2(u, golden["seeded_run_field"]) < REF_TOL
+
+
+def test_seeded_simulation_reproduces_reference(golden):
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import simulations
+    np.random.seed(321)
+    ch = small_channel(pa)
+    beam = simulations.BeamResult(ch, max_size=3)
+    pdt = simulations.PDTResult(ch, max_size=5)
+    tpdt = simulations.TrackedPDTResult(ch, max_size=5)
+    sim = simulations.Simulation([beam, pdt, tpdt])
+    assert sim._batch_plan() is not None, "Beam / PDT / tracked PDT must take the batched path"
+    sim.run()
+    np.testing.assert_allclose(pdt.measures[0].data, golden["seeded_sim_eta"], rtol=1e-3)
+    np.testing.assert_allclose(tpdt.measures[2].data, golden["seeded_sim_tracked_eta"], rtol=1e-3)
+    for i, nm in enumerate(["mean_x", "mean_y", "mean_x2", "mean_xy", "mean_y2", "mean_x2_r"]):
+        np.testing.assert_allclose(beam.measures[i].data, golden[f"seeded_sim_{nm}"], rtol=2e-2, atol=2e-5)
+    assert len(beam.measures[0]) == 3 and len(pdt.measures[0]) == 5
+
+
+def test_batched_simulation_equals_per_realisation_path():
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import gpu, simulations
+    results = []
+    for batched in (True, False):
+        np.random.seed(7)
+        ch = small_channel(pa)
+        beam = simulations.BeamResult(ch, max_size=4)
+        pdt = simulations.PDTResult(ch, max_size=4)
+        sim = simulations.Simulation([beam, pdt])
+        if batched:
+            gpu.config["batch"] = 3     # two engine calls: 3 + 1 realisations
+            sim.run()
+        else:
+            while not sim.is_measures_done():
+                sim.iter()
+        results.append((np.array(pdt.measures[0].data, float), np.array(beam.measures[0].data, float),
+                        np.array(beam.measures[5].data, float)))
+    gpu.config["batch"] = 256
+    for a, b in zip(*results):
+        np.testing.assert_allclose(a, b, rtol=2e-5, atol=1e-8)
+
+
+def test_path_generator_matches_fused_run():
+    import torch
+    import pyatmosphere_gb300 as pa
+    np.random.seed(11)
+    ch = small_channel(pa)
+    fused = ch.run(pupil=False)
+    np.random.seed(11)
+    ch2 = small_channel(pa)
+    steps = list(ch2.generator(pupil=False))
+    assert len(steps) == 3
+    assert tuple(steps[0][1].shape) == (128, 128)
+    assert o.rel_l2(ch2.output.cpu().numpy(), fused.cpu().numpy()) < 1e-5
+
+
+def test_measures_on_field_match_oracle():
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import measures
+    np.random.seed(5)
+    ch = small_channel(pa)
+    u = ch.run(pupil=False)
+    ref = o.measures(u.cpu().numpy().astype(np.complex128), 3e-3, [0.08])
+    assert measures.eta(ch, output=u) == pytest.approx(ref["eta_total"], rel=1e-6)
+    assert measures.mean_x(ch, output=u) == pytest.approx(ref["mean_x"], rel=1e-5, abs=1e-10)
+    assert measures.mean_xy(ch, output=u) == pytest.approx(ref["mean_xy"], rel=1e-5, abs=1e-12)
+    assert measures.eta(ch, output=ch.pupil.output(u)) == pytest.approx(ref["eta_0"], rel=1e-5)
+
+
+def test_vacuum_channel_length_override_and_known_answer():
+    """itest_sources: mean_r2(channel, length=L, pupil=False) on a VacuumPath."""
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import measures
+    ch = pa.Channel(grid=pa.RectGrid(512, 5e-3), source=pa.GaussianSource(wvl=809e-9, w0=0.2, F0=np.inf),
+                    path=pa.VacuumPath(length=4e3), pupil=pa.CirclePupil(0.1))
+    for L in [0.0, 5000.0, 20000.0]:
+        w = np.sqrt(2 * measures.mean_r2(ch, length=L, pupil=False))
+        assert w == pytest.approx(ch.source.get_w(L), rel=1e-3)
+
+
+def test_screen_generate_matches_oracle():
+    import pyatmosphere_gb300 as pa
+    ch = small_channel(pa)
+    ch.path.init_phase_screens()
+    ps = ch.path.phase_screens[0]
+    np.random.seed(2)
+    phi = ps.generate().cpu().numpy()
+    np.random.seed(2)
+    sp = ps._get_spectrum(False)
+    ref = o.ss_screen(sp.rho, sp.theta, sp.value, 128, 3e-3)
+    assert np.abs(phi - ref).max() < 2e-4
+
+
+def test_fft_screen_matches_oracle():
+    """FFTPhaseScreen with 3 subharmonic levels (phase_screens.py:42-67)."""
+    import pyatmosphere_gb300 as pa
+    N, d = 256, 2e-3
+    ps = pa.FFTPhaseScreen(3, model=pa.MVKModel(Cn2=1e-14, l0=6e-3, L0=1e3), thickness=1e3, wvl=808e-9,
+                           grid=pa.RectGrid(N, d))
+    rng = np.random.default_rng(8)
+    normals = [rng.standard_normal((2, N, N))] + [rng.standard_normal((2, 3, 3)) for _ in range(3)]
+    got = ps.generate(complex=True, normals=normals).cpu().numpy()
+    ref = o.fft_screen(normals, N, d, 2 * np.pi / 808e-9, 1e3, 1e-14, 6e-3, 1e3, 3)
+    assert o.rel_l2(got, ref) < 1e-5
+    real = ps.generate(normals=normals).cpu().numpy()
+    assert np.abs(real - ref.real).max() < 1e-4 * np.abs(ref.real).max()
+
+
+def test_fft_screen_channel_conserves_energy():
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import measures
+    ch = pa.Channel(grid=pa.RectGrid(256, 4e-3), source=pa.GaussianSource(wvl=808e-9, w0=0.08, F0=np.inf),
+                    path=pa.IdenticalPhaseScreensPath(
+                        phase_screen=pa.FFTPhaseScreen(2, model=pa.MVKModel(2e-15, 6e-3, 1e3)),
+                        length=5e3, count=3),
+                    pupil=pa.CirclePupil(0.1))
+    np.random.seed(1)
+    u = ch.run(pupil=False)
+    assert measures.eta(ch, output=u) == pytest.approx(1.0, abs=2e-5)
