@@ -176,15 +176,17 @@ struct Padded {
   static constexpr int value = N + N / 16;
 };
 
-// twiddle W_{LR}^{e} for e < L*R, from the length-N table tw[n] = exp(-2 pi i n / N)
-template <int N, int LR, int DIR>
+// twiddle W_{LR}^{e} for e < L*R, from the length-N table tw[n] = exp(-2 pi i n / N);
+// TWPAD = 1: the table is stored with one pad slot per 16 entries (shared memory)
+template <int N, int LR, int DIR, int TWPAD = 0>
 ATM_HD float2 twiddle(const float2* tw, int e) {
-  float2 w = tw[e * (N / LR)];
+  const int n = e * (N / LR);
+  float2 w = tw[TWPAD ? pad16(n) : n];
   return DIR < 0 ? w : cconj(w);
 }
 
 // butterflies of stage s on register inputs; results to shared memory
-template <int N, int s, int DIR>
+template <int N, int s, int DIR, int TWPAD = 0>
 ATM_HD void stage_to_smem(float2 (&v)[16], float2* sm, int t, const float2* tw) {
   constexpr int R = StageRadix<N, s>::value;
   constexpr int L = StageL<N, s>::value;
@@ -199,7 +201,7 @@ ATM_HD void stage_to_smem(float2 (&v)[16], float2* sm, int t, const float2* tw) 
     for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
     if (L > 1) {
 #pragma unroll
-      for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR>(tw, i * m));
+      for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR, TWPAD>(tw, i * m));
     }
     dft<R, DIR>(a);
     const int j = (k - i) * R + i;
@@ -222,7 +224,7 @@ ATM_HD void stage_from_smem(float2 (&v)[16], const float2* sm, int t) {
 }
 
 // last stage: outputs stay in registers, v[m] = element t + m T
-template <int N, int DIR>
+template <int N, int DIR, int TWPAD = 0>
 ATM_HD void stage_last(float2 (&v)[16], int t, const float2* tw) {
   constexpr int s = FftPlan<N>::S - 1;
   constexpr int R = StageRadix<N, s>::value;
@@ -238,7 +240,7 @@ ATM_HD void stage_last(float2 (&v)[16], int t, const float2* tw) {
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
 #pragma unroll
-    for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR>(tw, i * m));
+    for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR, TWPAD>(tw, i * m));
     dft<R, DIR>(a);
 #pragma unroll
     for (int q = 0; q < R; ++q) o[b + B * q] = a[q];

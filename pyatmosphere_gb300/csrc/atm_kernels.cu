@@ -18,17 +18,23 @@ namespace atm {
 // ---------------------------------------------------------------------------
 // FFT driver over the stages of FftPlan<N> (see atm_common.cuh)
 // ---------------------------------------------------------------------------
-template <int N, int DIR, int s = 0>
+template <int N, int DIR, int s = 0, int TWPAD = 0>
 __device__ __forceinline__ void fft_dev(float2 (&v)[16], float2* sm, int t, const float2* __restrict__ tw) {
   if constexpr (s == FftPlan<N>::S - 1) {
-    stage_last<N, DIR>(v, t, tw);
+    stage_last<N, DIR, TWPAD>(v, t, tw);
   } else {
-    stage_to_smem<N, s, DIR>(v, sm, t, tw);
+    stage_to_smem<N, s, DIR, TWPAD>(v, sm, t, tw);
     __syncthreads();
     stage_from_smem<N, s + 1>(v, sm, t);
     __syncthreads();
-    fft_dev<N, DIR, s + 1>(v, sm, t, tw);
+    fft_dev<N, DIR, s + 1, TWPAD>(v, sm, t, tw);
   }
+}
+
+// twiddle table copied into shared memory with the pad16 layout
+template <int N>
+__device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restrict__ tw) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) dst[pad16(i)] = tw[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -166,7 +172,7 @@ row_pass_kernel(RowArgs a) {
     for (int m = 0; m < 16; ++m) {
       const int x = t + m * T;
       float s, c;
-      sincosf(ph[x], &s, &c);
+      sincospif(2.f * ph[x], &s, &c);  // phi_G is stored in turns
       v[m] = cmul(v[m], cmul(cmul(py, px[x]), make_float2(c, -s)));
     }
   } else if (a.loss != 1.0f) {
@@ -192,10 +198,9 @@ row_pass_kernel(RowArgs a) {
 template <int N>
 struct RowPipe {
   static constexpr int ROWS = RowRows<N>::value;
-  static constexpr size_t FIELD = (size_t)ROWS * Padded<N>::value * sizeof(float2);
-  static constexpr size_t PHI = (size_t)ROWS * N * sizeof(float);
-  static constexpr size_t STAGE = FIELD + PHI;
-  static constexpr size_t SMEM = 2 * STAGE;
+  static constexpr size_t STAGE = (size_t)ROWS * Padded<N>::value * sizeof(float2);
+  static constexpr size_t TW = (size_t)Padded<N>::value * sizeof(float2);
+  static constexpr size_t SMEM = 2 * STAGE + TW;
 };
 
 template <int N>
@@ -214,7 +219,8 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
   const bool load_phi = (flags & ROW_PHASOR) != 0;
 
   auto fbuf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * RowPipe<N>::STAGE); };
-  auto pbuf = [&](int s) { return reinterpret_cast<float*>(smem_raw + s * RowPipe<N>::STAGE + RowPipe<N>::FIELD); };
+  float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * RowPipe<N>::STAGE);
+  load_twiddles<N>(tws, a.tw);
   auto prefetch = [&](int item, int s) {
     const int r = item / NRB, y0 = (item - r * NRB) * ROWS;
     const size_t off = (size_t)r * N * N + (size_t)y0 * N;
@@ -225,11 +231,6 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
         const int row = c / (N / 2), col = (c - row * (N / 2)) * 2;
         cp_async16(dst + row * P + col, src + (size_t)row * N + col);
       }
-    }
-    if (load_phi) {
-      const float* src = a.phi + off;
-      float* dst = pbuf(s);
-      for (int c = tid; c < ROWS * N / 4; c += NT) cp_async16(dst + c * 4, src + c * 4);
     }
   };
 
@@ -255,24 +256,31 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = sm[t + m * T];
     }
+    // screen phase (turns) of this row straight into registers; its latency
+    // hides behind the inverse FFT
+    float ph[16];
+    if (load_phi) {
+      const float* src = a.phi + rowoff;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) ph[m] = src[t + m * T];
+    }
     __syncthreads();  // the exchange below overwrites the staged rows
-    if (flags & ROW_INV) fft_dev<N, 1>(v, sm, t, a.tw);
+    if (flags & ROW_INV) fft_dev<N, 1, 0, 1>(v, sm, t, tws);
     if (load_phi) {
       const float2 py = cscale(a.Py[(size_t)r * N + y], a.loss);
-      const float* ph = pbuf(s) + rl * N;
       const float2* px = a.Px + (size_t)r * N;
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
         const int x = t + m * T;
         float sn, cs;
-        sincosf(ph[x], &sn, &cs);
+        sincospif(2.f * ph[m], &sn, &cs);
         v[m] = cmul(v[m], cmul(cmul(py, px[x]), make_float2(cs, -sn)));
       }
     } else if (a.loss != 1.0f) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cscale(v[m], a.loss);
     }
-    if (flags & ROW_FWD) fft_dev<N, -1>(v, sm, t, a.tw);
+    if (flags & ROW_FWD) fft_dev<N, -1, 0, 1>(v, sm, t, tws);
     if (flags & ROW_STORE) {
       float2* dst = (a.store_out && a.out) ? a.out : a.field;
 #pragma unroll
@@ -387,7 +395,8 @@ struct ColPipe {
   static constexpr size_t TILE = (size_t)N * C * sizeof(float2);
   static constexpr size_t EXCH = (size_t)C * ColStride<N, C>::value * sizeof(float2);
   static constexpr size_t STAGE = ((TILE > EXCH ? TILE : EXCH) + 127) / 128 * 128;
-  static constexpr size_t SMEM = 2 * STAGE;
+  static constexpr size_t TW = (size_t)Padded<N>::value * sizeof(float2);
+  static constexpr size_t SMEM = 2 * STAGE + TW;
 };
 
 template <int N, int C>
@@ -401,6 +410,8 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
   auto buf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * ColPipe<N, C>::STAGE); };
+  float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * ColPipe<N, C>::STAGE);
+  load_twiddles<N>(tws, a.tw);
   auto prefetch = [&](int item, int s) {
     const int r = item / NCT, x0 = (item - r * NCT) * C;
     const float2* src = a.field + (size_t)r * N * N + x0;
@@ -427,12 +438,12 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
     __syncthreads();  // the exchange below overwrites the staged tile
     float2* sm = tile + c * S;
     if (!a.inv_only) {
-      fft_dev<N, -1>(v, sm, t, a.tw);
+      fft_dev<N, -1, 0, 1>(v, sm, t, tws);
       const float2 hx = a.hx[x];
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(a.hy[t + m * T], hx));
     }
-    fft_dev<N, 1>(v, sm, t, a.tw);
+    fft_dev<N, 1, 0, 1>(v, sm, t, tws);
     float2* f = a.field + (size_t)r * N * N + x;
 #pragma unroll
     for (int m = 0; m < 16; ++m) f[(size_t)(t + m * T) * N] = v[m];
@@ -799,6 +810,12 @@ __global__ void __launch_bounds__(256, 2) screen_gemm_kernel(GemmArgs a) {
     __syncthreads();
     buf ^= 1;
   }
+  // stored in turns (phi / 2 pi): the row pass reduces it exactly with sincospif
+  const float inv2pi = 0.15915494309189533577f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] *= inv2pi;
   float* C = a.phi + (size_t)s * N * N;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -827,10 +844,11 @@ __global__ void compose_screen_kernel(const double* Gy, const double* Hx, const 
   const int y = blockIdx.y, r = blockIdx.z;
   if (x >= N) return;
   const size_t o = ((size_t)r * N + y) * N + x;
-  if (phi_out) phi_out[o] = (float)(Gy[(size_t)r * N + y] + Hx[(size_t)r * N + x] + (double)phiG[o]);
+  if (phi_out)
+    phi_out[o] = (float)(Gy[(size_t)r * N + y] + Hx[(size_t)r * N + x] + 6.283185307179586477 * (double)phiG[o]);
   if (phasor_out) {
     float s, c;
-    sincosf(phiG[o], &s, &c);
+    sincospif(2.f * phiG[o], &s, &c);
     phasor_out[o] = cmul(cmul(Py[(size_t)r * N + y], Px[(size_t)r * N + x]), make_float2(c, -s));
   }
 }

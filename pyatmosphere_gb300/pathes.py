@@ -88,11 +88,14 @@ class PhaseScreensPath(AbstractPath):
         self.init_phase_screens()
         for i, phase_screen in enumerate(self.phase_screens):
             vacuum_path.length = self.positions[i] - self.positions[i - 1] if i > 0 else self.positions[0]
-            screen = phase_screen.generate(*args, **kwargs)
+            import torch
+            if hasattr(phase_screen, "generate_with_phasor"):
+                screen, phasor = phase_screen.generate_with_phasor(*args, **kwargs)
+            else:
+                screen = phase_screen.generate(*args, **kwargs)
+                phasor = torch.polar(torch.ones_like(screen), -screen)  # exp(-i phi), complex64
             part_losses_db = self.losses_db * vacuum_path.length / self.length
             field = _as_field(self.channel, vacuum_path.output(input))
-            import torch
-            phasor = torch.polar(torch.ones_like(screen), -screen)  # exp(-i phi), complex64
             input = self.append_losses(phasor * field, losses_db=part_losses_db)
             yield input, screen
         return vacuum_path.output(input, length=self.length - self.positions[-1])

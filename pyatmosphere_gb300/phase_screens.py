@@ -95,9 +95,11 @@ class SSPhaseScreen(PhaseScreen):
             self._plan_key = key
         return self._plan
 
-    def generate_phase_screen(self, shift: Tuple[float, float] = (0, 0), wind: bool = False, phasor: bool = False):
-        """float32 screen [N, N] (torch, on the engine device).  With
-        ``phasor=True`` returns exp(-i phi) as the path applies it."""
+    def generate_with_phasor(self, shift: Tuple[float, float] = (0, 0), wind: bool = False):
+        """(phi, exp(-i phi)) of one spectrum draw: the float32 screen the
+        reference returns and the phasor the path applies, which the engine
+        builds from FP64 phases (more accurate than exp(-i phi) of the float32
+        screen, whose piston reaches ~1e3 rad)."""
         import torch
         from .engine.runner import to_device
         sp = self._get_spectrum(use_cached_spectrum=wind)
@@ -106,16 +108,17 @@ class SSPhaseScreen(PhaseScreen):
                                       np.asarray(sp.theta, np.float32).reshape(1, 1, -1),
                                       np.asarray(sp.value, np.complex64).reshape(1, 1, -1))
         N = plan.N
-        if phasor:
-            out = torch.empty((1, N, N), dtype=torch.complex64, device=plan.device)
-            plan.screen(rho, theta, value, 0, phasor_out=out)
-        else:
-            out = torch.empty((1, N, N), dtype=torch.float32, device=plan.device)
-            plan.screen(rho, theta, value, 0, phi_out=out)
+        phi = torch.empty((1, N, N), dtype=torch.float32, device=plan.device)
+        ph = torch.empty((1, N, N), dtype=torch.complex64, device=plan.device)
+        plan.screen(rho, theta, value, 0, phi_out=phi, phasor_out=ph)
         if wind:
-            self._cached_phase_screen = out[0]
+            self._cached_phase_screen = phi[0]
             self._cached_phase_screen_shift = shift[0]
-        return out[0]
+        return phi[0], ph[0]
+
+    def generate_phase_screen(self, shift: Tuple[float, float] = (0, 0), wind: bool = False):
+        """float32 screen [N, N] (torch, on the engine device)."""
+        return self.generate_with_phasor(shift=shift, wind=wind)[0]
 
 
 class FFTPhaseScreen(PhaseScreen):
