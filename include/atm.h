@@ -165,6 +165,44 @@ int atm_measures(AtmPlan* plan, const void* field, int32_t batch, double* measur
 int atm_fft_screen(AtmPlan* plan, const float* normals, const float* amp, const void* sub_x, const void* sub_y,
                    const double* sub_mean, int32_t n_sub, int32_t batch, void* screen_out, void* stream);
 
+/* Re-targets a plan to another channel of the same grid, screen count,
+ * spectral grid, pupil counts and batch (source, positions, length, losses,
+ * shift and pupil radii may change) without reallocating; waits for the
+ * device first.  Replaces building a new Channel for each parameter point
+ * of a sweep (channels.py:17-29). */
+int atm_plan_update(AtmPlan* plan, const AtmChannelDesc* desc);
+
+/* Seeded spectra on the device: rho, theta [batch][n][P] float32 and value
+ * [batch][n][P] complex64 for realisations first_realisation .. +batch-1,
+ * drawn with a counter-based Philox4x32-10 generator keyed by `seed` (one
+ * uniform per screen for the annulus radii, per annulus a uniform angle and
+ * two normals) and formed with the reference's formulas (grids.py:98-107,
+ * phase_screens.py:98-103); sqrt_psd [n][P] (device) holds sqrt of each
+ * screen's annulus weights.  The stream of numbers differs from numpy's:
+ * use host-drawn spectra where realisations must match the reference. */
+int atm_draw_spectra(AtmPlan* plan, uint64_t seed, uint64_t first_realisation, const float* sqrt_psd,
+                     int32_t batch, float* rho, float* theta, void* value, void* stream);
+
+/* ---- PDT surrogate MLP (no reference counterpart: the learned part of the
+ * engine; it answers PDTResult-style queries, simulations/pdt.py:11-66,
+ * without running the channel).  widths[0..n_layers]; hidden layers use
+ * GELU; BF16 weights in the GEMMs, FP32 accumulation, FP32 master weights
+ * for Adam.  Arrays passed to forward / loss / backward / infer are device
+ * arrays; parameters are packed W0 [w1][w0], b0 [w1], W1, b1, ... */
+typedef struct AtmMlp AtmMlp;
+int atm_mlp_create(int32_t n_layers, const int32_t* widths, int32_t max_batch, AtmMlp** mlp);
+int atm_mlp_destroy(AtmMlp* mlp);
+int64_t atm_mlp_num_params(const AtmMlp* mlp);
+int atm_mlp_set_params(AtmMlp* mlp, const float* host_params);
+int atm_mlp_get_params(AtmMlp* mlp, float* host_params, float* host_grads);
+int atm_mlp_forward(AtmMlp* mlp, const float* x, int32_t batch, float* y, void* stream);
+int atm_mlp_loss(AtmMlp* mlp, const float* target, int32_t batch, int32_t n_hist, float w_mse, double* loss_out,
+                 float* dy, void* stream);
+int atm_mlp_backward(AtmMlp* mlp, const float* dy, int32_t batch, float* grads, void* stream);
+int atm_mlp_adam(AtmMlp* mlp, float lr, float beta1, float beta2, float eps, int32_t step, void* stream);
+int atm_mlp_infer(AtmMlp* mlp, const float* x, int32_t batch, const float* lo, const float* hi, int32_t n_hist,
+                  float* y, int32_t* out_of_range, void* stream);
+
 /* Launch categories reported by atm_profile_end. */
 #define ATM_KIND_SCREEN_PREP 0
 #define ATM_KIND_SCREEN_TABLE 1

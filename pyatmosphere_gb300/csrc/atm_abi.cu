@@ -122,6 +122,14 @@ int atm::set_error(int code, const char* fmt, ...) {
   return code;
 }
 
+namespace {
+struct AtmPlanFwd;
+}
+struct AtmPlan;
+namespace {
+int check_device(const AtmPlan* pl);
+}
+
 struct AtmPlan {
   int device = 0;
   int N = 0, n = 0, P = 0, B = 0, n_pupils = 0, n_tracked = 0;
@@ -141,7 +149,9 @@ struct AtmPlan {
   bool profiling = false;
 
   DevBuf field, phi, At, Bt, Ach, ht, Py, Px, Gy, Hx, tw, ay, ax, hy, hx, vac_h, partials, center, pupil_rows,
-      intensity, tracked_r;
+      intensity, tracked_r, fbase;
+  std::vector<float> f_base;
+  double cheb_cut = 0.0;
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
     int64_t s = 0;
@@ -290,6 +300,41 @@ int choose_low_block(AtmPlan* pl, const AtmChannelDesc* d) {
   return fail(ATM_ERR_UNSUPPORTED, "could not fit the low-frequency block into 64 Chebyshev terms");
 }
 
+// source / path / loss state that atm_plan_update may change
+void set_geometry(AtmPlan* pl, const AtmChannelDesc* d) {
+  pl->wvl = d->wvl;
+  pl->w0 = d->w0;
+  pl->F0 = d->F0;
+  pl->length = d->length;
+  pl->losses_db = d->losses_db;
+  pl->kw = 2.0 * kPi / d->wvl;
+  pl->sx = d->shift_x;
+  pl->sy = d->shift_y;
+  pl->path_output_loss = d->path_output_loss;
+  pl->source_kind = d->source_kind;
+  pl->tracked_radius.assign(d->tracked_radius, d->tracked_radius + d->n_tracked);
+  // steps: dz[0] = z_0, dz[i] = z_i - z_{i-1}, dz[n] = L - z_{n-1} (pathes.py:68-75)
+  pl->positions.clear();
+  pl->dz.clear();
+  if (pl->n > 0) {
+    pl->positions.assign(d->positions, d->positions + pl->n);
+    pl->dz.push_back(pl->positions[0]);
+    for (int i = 1; i < pl->n; ++i) pl->dz.push_back(pl->positions[i] - pl->positions[i - 1]);
+    pl->dz.push_back(pl->length - pl->positions[pl->n - 1]);
+  } else {
+    pl->dz.push_back(pl->length);
+  }
+  // losses: a step whose share is 0 falls back to the full path loss
+  // (append_losses: `losses_db or self.losses_db`, pathes.py:19-21)
+  pl->loss.clear();
+  for (int i = 0; i < pl->n; ++i) {
+    double ld = pl->losses_db * pl->dz[i] / pl->length;
+    if (ld == 0.0) ld = pl->losses_db;
+    pl->loss.push_back(ld != 0.0 ? (float)std::pow(10.0, -ld / 20.0) : 1.f);
+  }
+  pl->final_loss = (pl->path_output_loss && pl->losses_db != 0.0) ? (float)std::pow(10.0, -pl->losses_db / 20.0) : 1.f;
+}
+
 int validate(const AtmChannelDesc* d) {
   if (!d) return fail(ATM_ERR_INVALID, "descriptor is NULL");
   if (d->abi_version != ATM_ABI_VERSION)
@@ -348,24 +393,7 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   pl->n_pupils = d->n_pupils;
   pl->n_tracked = d->n_tracked;
   pl->col_tile = d->col_tile > 0 ? d->col_tile : atm::col_tile_default(pl->N);
-  for (int i = 0; i < d->n_tracked; ++i) pl->tracked_radius.push_back(d->tracked_radius[i]);
-  // steps: dz[0] = z_0, dz[i] = z_i - z_{i-1}, dz[n] = L - z_{n-1} (pathes.py:68-75)
-  if (pl->n > 0) {
-    pl->positions.assign(d->positions, d->positions + pl->n);
-    pl->dz.push_back(pl->positions[0]);
-    for (int i = 1; i < pl->n; ++i) pl->dz.push_back(pl->positions[i] - pl->positions[i - 1]);
-    pl->dz.push_back(pl->length - pl->positions[pl->n - 1]);
-  } else {
-    pl->dz.push_back(pl->length);
-  }
-  // losses: a step whose share is 0 falls back to the full path loss
-  // (append_losses: `losses_db or self.losses_db`, pathes.py:19-21)
-  for (int i = 0; i < pl->n; ++i) {
-    double ld = pl->losses_db * pl->dz[i] / pl->length;
-    if (ld == 0.0) ld = pl->losses_db;
-    pl->loss.push_back(ld != 0.0 ? (float)std::pow(10.0, -ld / 20.0) : 1.f);
-  }
-  pl->final_loss = (pl->path_output_loss && pl->losses_db != 0.0) ? (float)std::pow(10.0, -pl->losses_db / 20.0) : 1.f;
+  set_geometry(pl, d);
 
   int rc = ATM_OK;
   if (pl->n > 0) rc = choose_low_block(pl, d);
@@ -415,12 +443,41 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
       return rc;
     }
   }
+  if (pl->n > 0) {
+    if ((rc = dev_alloc(pl->fbase, (size_t)pl->P * sizeof(float), v))) {
+      delete pl;
+      return rc;
+    }
+    pl->f_base.assign(d->f_base, d->f_base + pl->P);
+    if ((rc = upload(pl->fbase, pl->f_base))) {
+      delete pl;
+      return rc;
+    }
+  }
+  pl->cheb_cut = d->cheb_cut;
   if ((rc = plan_tables(pl, d))) {
     delete pl;
     return rc;
   }
   *out = pl;
   return ATM_OK;
+}
+
+int atm_plan_update(AtmPlan* pl, const AtmChannelDesc* d) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = validate(d)) return rc;
+  if (int rc = check_device(pl)) return rc;
+  if (d->resolution != pl->N || d->delta != pl->delta || d->n_screens != pl->n || d->n_pupils != pl->n_pupils ||
+      d->n_tracked != pl->n_tracked || d->batch > pl->B || d->cheb_cut != pl->cheb_cut)
+    return fail(ATM_ERR_INVALID, "atm_plan_update keeps grid, screen count, pupil counts, batch and cheb_cut");
+  if (pl->n > 0) {
+    if (d->points != pl->P) return fail(ATM_ERR_INVALID, "atm_plan_update keeps the spectral grid");
+    for (int p = 0; p < pl->P; ++p)
+      if (d->f_base[p] != pl->f_base[p]) return fail(ATM_ERR_INVALID, "atm_plan_update keeps the spectral grid");
+  }
+  ATM_CUDA(cudaDeviceSynchronize());  // tables may still be read by enqueued work
+  set_geometry(pl, d);
+  return plan_tables(pl, d);
 }
 
 int atm_plan_destroy(AtmPlan* pl) {
@@ -748,6 +805,18 @@ int atm_fft_screen(AtmPlan* pl, const float* normals, const float* amp, const vo
     ATM_CUDA(atm::launch_col_pass(pl->N, batch, pl->col_tile, ca, st));
   }
   ATM_CUDA(atm::launch_fft_screen_finish(batch, fa, st));
+  return ATM_OK;
+}
+
+int atm_draw_spectra(AtmPlan* pl, uint64_t seed, uint64_t first_realisation, const float* sqrt_psd, int32_t batch,
+                     float* rho, float* theta, void* value, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (pl->n < 1) return fail(ATM_ERR_INVALID, "plan has no screens");
+  if (batch < 1 || batch > 65535) return fail(ATM_ERR_INVALID, "batch %d out of range", batch);
+  if (!sqrt_psd || !rho || !theta || !value) return fail(ATM_ERR_INVALID, "NULL argument");
+  ATM_CUDA(atm::launch_draw_spectra(seed, first_realisation, pl->n, pl->P, (const float*)pl->fbase.p, sqrt_psd,
+                                    batch, rho, theta, (float2*)value, (cudaStream_t)stream));
   return ATM_OK;
 }
 

@@ -309,4 +309,37 @@ ATM_HD void bessel_j(double a, int D, double* J /* [D] */) {
     for (int n = 1; n < D; n += 2) J[n] = -J[n];
 }
 
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror and Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC 2011): 10 rounds of
+// multiply-xor with a Weyl key schedule.  Stateless: (key, counter) -> 4 words.
+// ---------------------------------------------------------------------------
+struct Philox4 {
+  uint32_t v[4];
+};
+
+ATM_HD uint32_t mulhi32(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32); }
+
+ATM_HD Philox4 philox4x32_10(Philox4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = mulhi32(M0, c.v[0]), lo0 = M0 * c.v[0];
+    const uint32_t hi1 = mulhi32(M1, c.v[2]), lo1 = M1 * c.v[2];
+    Philox4 n;
+    n.v[0] = hi1 ^ c.v[1] ^ k0;
+    n.v[1] = lo1;
+    n.v[2] = hi0 ^ c.v[3] ^ k1;
+    n.v[3] = lo0;
+    c = n;
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// uniform in [0, 1) from the top 24 bits
+ATM_HD float u01(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+// uniform in (0, 1]
+ATM_HD float u01_open0(uint32_t x) { return ((float)(x >> 8) + 1.0f) * 5.9604644775390625e-8f; }
+
 }  // namespace atm

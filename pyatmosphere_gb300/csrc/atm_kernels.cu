@@ -1030,4 +1030,43 @@ cudaError_t launch_fma_probe(int blocks, int iters, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// seeded spectra on the device: per (realisation r, screen i) one uniform u
+// for the annulus radii and per annulus p a uniform angle and two normals
+// (Box-Muller), formed with the reference's float32 formulas
+// (grids.py:98-107, phase_screens.py:98-103).  Counter = (p, i, r), key = seed.
+// ---------------------------------------------------------------------------
+__global__ void draw_spectra_kernel(uint32_t k0, uint32_t k1, uint64_t first, int n, int P, const float* fbase,
+                                    const float* sqrt_psd, float* rho, float* theta, float2* value) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y, b = blockIdx.z;
+  if (p >= P) return;
+  const uint64_t r = first + (uint64_t)b;
+  Philox4 c;
+  c.v[0] = 0xFFFFFFFFu;  // per-screen draw: annulus position u
+  c.v[1] = (uint32_t)i;
+  c.v[2] = (uint32_t)r;
+  c.v[3] = (uint32_t)(r >> 32);
+  const float u = u01(philox4x32_10(c, k0, k1).v[0]);
+  c.v[0] = (uint32_t)p;
+  const Philox4 x = philox4x32_10(c, k0, k1);
+  const float f = fbase[p], fp = p ? fbase[p - 1] : 0.f;
+  const size_t o = ((size_t)b * n + i) * P + p;
+  rho[o] = sqrtf(fp * fp + u * (f * f - fp * fp));
+  theta[o] = 6.28318530717958647692f * u01(x.v[1]);
+  const float rad = sqrtf(-2.f * logf(u01_open0(x.v[2])));
+  float s, cs;
+  sincospif(2.f * u01(x.v[3]), &s, &cs);
+  const float amp = sqrt_psd[(size_t)i * P + p];
+  value[o] = make_float2(rad * cs * amp, rad * s * amp);
+}
+
+cudaError_t launch_draw_spectra(uint64_t seed, uint64_t first, int n, int P, const float* fbase, const float* sqrt_psd,
+                                int B, float* rho, float* theta, float2* value, cudaStream_t st) {
+  dim3 grid((P + 255) / 256, n, B);
+  draw_spectra_kernel<<<grid, 256, 0, st>>>((uint32_t)seed, (uint32_t)(seed >> 32), first, n, P, fbase, sqrt_psd,
+                                            rho, theta, value);
+  return cudaGetLastError();
+}
+
 }  // namespace atm

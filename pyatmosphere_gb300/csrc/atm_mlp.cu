@@ -1,0 +1,398 @@
+// Kernels and C ABI of the PDT surrogate: a small MLP (8 -> 256 -> 256 ->
+// 256 -> 67, GELU) with BF16 weights, FP32 accumulation and FP32 master
+// weights for Adam.  Forward, backward, loss (KL on a softmax histogram + MSE
+// on moments), Adam and a fused inference pass with an out-of-range check.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/atm.h"
+#include "atm_internal.h"
+
+namespace {
+
+constexpr int kMaxLayers = 8;
+constexpr float kInvSqrt2 = 0.70710678118654752440f;
+constexpr float kInvSqrt2Pi = 0.39894228040143267794f;
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * kInvSqrt2)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+  return 0.5f * (1.f + erff(z * kInvSqrt2)) + z * kInvSqrt2Pi * expf(-0.5f * z * z);
+}
+
+template <typename T>
+__device__ __forceinline__ float ld(const T* p);
+template <>
+__device__ __forceinline__ float ld<float>(const float* p) { return *p; }
+template <>
+__device__ __forceinline__ float ld<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+
+enum Epi { EPI_NONE = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2, EPI_GELU_GRAD = 3 };
+
+// C[m][n] = sum_k A(m, k) B(k, n) (+ bias[n], GELU, or * gelu'(Z[m][n])),
+// A(m, k) = A[m sam + k sak], B(k, n) = B[k sbk + n sbn].  64 x 64 tiles,
+// 256 threads, 4 x 4 outputs per thread, K step 16.
+template <typename TA, typename TB, int EPI>
+__global__ void __launch_bounds__(256) mlp_gemm_kernel(int M, int N, int K, const TA* __restrict__ A, int sam,
+                                                       int sak, const TB* __restrict__ B, int sbk, int sbn,
+                                                       float* __restrict__ C, int ldc, const float* __restrict__ bias,
+                                                       float* __restrict__ Z) {
+  __shared__ float As[16][64 + 1];
+  __shared__ float Bs[16][64 + 1];
+  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  const int tid = threadIdx.x, tm = tid / 16, tn = tid % 16;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int e = tid; e < 16 * 64; e += 256) {
+      const int kk = e / 64, mm = e % 64;
+      const int m = m0 + mm, k = k0 + kk;
+      As[kk][mm] = (m < M && k < K) ? ld(A + (size_t)m * sam + (size_t)k * sak) : 0.f;
+      const int n = n0 + mm;
+      Bs[kk][mm] = (n < N && k < K) ? ld(B + (size_t)k * sbk + (size_t)n * sbn) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][tm + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tn + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + tm + 16 * i;
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int n = n0 + tn + 16 * j;
+      if (n >= N) continue;
+      float v = acc[i][j];
+      const size_t o = (size_t)m * ldc + n;
+      if (EPI == EPI_BIAS || EPI == EPI_BIAS_GELU) v += bias[n];
+      if (EPI == EPI_BIAS_GELU) {
+        Z[o] = v;
+        v = gelu(v);
+      }
+      if (EPI == EPI_GELU_GRAD) v *= gelu_grad(Z[o]);
+      C[o] = v;
+    }
+  }
+}
+
+template <typename TA, typename TB, int EPI>
+cudaError_t gemm(int M, int N, int K, const TA* A, int sam, int sak, const TB* B, int sbk, int sbn, float* C, int ldc,
+                 const float* bias, float* Z, cudaStream_t st) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  mlp_gemm_kernel<TA, TB, EPI><<<grid, 256, 0, st>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, Z);
+  return cudaGetLastError();
+}
+
+// db[n] = sum_m dZ[m][n]
+__global__ void col_sum_kernel(const float* __restrict__ dZ, int M, int N, float* __restrict__ db) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (int m = 0; m < M; ++m) s += dZ[(size_t)m * N + n];
+  db[n] = s;
+}
+
+// one warp per sample: softmax over the first H outputs against a target
+// histogram (KL), MSE on the remaining outputs; writes dY and adds the loss
+__global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict__ T, int B, int O, int H, float w_mse,
+                            float* __restrict__ dY, double* __restrict__ loss) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x & 31;
+  if (warp >= B) return;
+  const float* y = Y + (size_t)warp * O;
+  const float* t = T + (size_t)warp * O;
+  float* dy = dY + (size_t)warp * O;
+  float mx = -INFINITY;
+  for (int j = lane; j < H; j += 32) mx = fmaxf(mx, y[j]);
+  for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  float se = 0.f;
+  for (int j = lane; j < H; j += 32) se += expf(y[j] - mx);
+  for (int off = 16; off; off >>= 1) se += __shfl_xor_sync(0xffffffffu, se, off);
+  const float lse = mx + logf(se);
+  float l = 0.f;
+  const float invB = 1.f / (float)B;
+  for (int j = lane; j < H; j += 32) {
+    const float logp = y[j] - lse, tj = t[j];
+    if (tj > 0.f) l += tj * (logf(tj) - logp);
+    dy[j] = (expf(logp) - tj) * invB;
+  }
+  const int nm = O - H;
+  for (int j = H + lane; j < O; j += 32) {
+    const float d = y[j] - t[j];
+    l += w_mse * d * d / (float)nm;
+    dy[j] = 2.f * w_mse * d / (float)nm * invB;
+  }
+  for (int off = 16; off; off >>= 1) l += __shfl_xor_sync(0xffffffffu, l, off);
+  if (lane == 0) atomicAdd(loss, (double)l * (double)invB);
+}
+
+__global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, const float* __restrict__ g,
+                            float* __restrict__ m, float* __restrict__ v, int n, float lr, float b1, float b2,
+                            float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  w[i] = wi;
+  wb[i] = __float2bfloat16_rn(wi);
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ wb, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+// inference epilogue: softmax over the first H outputs (in place), flag
+// queries whose inputs leave the training box [lo, hi]
+__global__ void infer_finish_kernel(float* __restrict__ Y, const float* __restrict__ X, int B, int O, int H, int I,
+                                    const float* __restrict__ lo, const float* __restrict__ hi, int* __restrict__ oor) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x & 31;
+  if (warp >= B) return;
+  float* y = Y + (size_t)warp * O;
+  float mx = -INFINITY;
+  for (int j = lane; j < H; j += 32) mx = fmaxf(mx, y[j]);
+  for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  float se = 0.f;
+  for (int j = lane; j < H; j += 32) se += expf(y[j] - mx);
+  for (int off = 16; off; off >>= 1) se += __shfl_xor_sync(0xffffffffu, se, off);
+  const float inv = 1.f / se;
+  for (int j = lane; j < H; j += 32) y[j] = expf(y[j] - mx) * inv;
+  if (oor) {
+    int out = 0;
+    for (int j = lane; j < I; j += 32) {
+      const float x = X[(size_t)warp * I + j];
+      out |= !(x >= lo[j] && x <= hi[j]);
+    }
+    out = __any_sync(0xffffffffu, out);
+    if (lane == 0) oor[warp] = out;
+  }
+}
+
+}  // namespace
+
+struct AtmMlp {
+  int device = 0;
+  int L = 0;                       // layers
+  std::vector<int> width;          // L + 1
+  int max_batch = 0;
+  size_t n_params = 0;
+  std::vector<size_t> w_off, b_off;
+  float* w = nullptr;              // FP32 master parameters (W0, b0, W1, b1, ...)
+  __nv_bfloat16* wb = nullptr;     // BF16 copies used by the GEMMs
+  float* g = nullptr;              // gradients
+  float* m = nullptr;
+  float* v = nullptr;
+  std::vector<float*> act;         // act[0] = input copy ... act[L] = output
+  std::vector<float*> pre;         // pre-activations of hidden layers
+  float* d0 = nullptr;             // gradient work buffers
+  float* d1 = nullptr;
+  ~AtmMlp() {
+    cudaFree(w);
+    cudaFree(wb);
+    cudaFree(g);
+    cudaFree(m);
+    cudaFree(v);
+    for (auto p : act) cudaFree(p);
+    for (auto p : pre) cudaFree(p);
+    cudaFree(d0);
+    cudaFree(d1);
+  }
+};
+
+#define MLP_CUDA(call)                                                                              \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return atm::set_error(ATM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+extern "C" {
+
+int atm_mlp_create(int32_t n_layers, const int32_t* widths, int32_t max_batch, AtmMlp** out) {
+  if (!out || !widths) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (n_layers < 1 || n_layers > kMaxLayers) return atm::set_error(ATM_ERR_INVALID, "n_layers %d", n_layers);
+  if (max_batch < 1) return atm::set_error(ATM_ERR_INVALID, "max_batch %d", max_batch);
+  int maxw = 0;
+  for (int i = 0; i <= n_layers; ++i) {
+    if (widths[i] < 1 || widths[i] > 4096) return atm::set_error(ATM_ERR_INVALID, "width %d", widths[i]);
+    maxw = std::max(maxw, (int)widths[i]);
+  }
+  AtmMlp* p = new AtmMlp();
+  cudaGetDevice(&p->device);
+  p->L = n_layers;
+  p->width.assign(widths, widths + n_layers + 1);
+  p->max_batch = max_batch;
+  size_t off = 0;
+  for (int l = 0; l < n_layers; ++l) {
+    p->w_off.push_back(off);
+    off += (size_t)widths[l + 1] * widths[l];
+    p->b_off.push_back(off);
+    off += widths[l + 1];
+  }
+  p->n_params = off;
+  bool ok = cudaMalloc(&p->w, off * 4) == cudaSuccess && cudaMalloc(&p->wb, off * 2) == cudaSuccess &&
+            cudaMalloc(&p->g, off * 4) == cudaSuccess && cudaMalloc(&p->m, off * 4) == cudaSuccess &&
+            cudaMalloc(&p->v, off * 4) == cudaSuccess &&
+            cudaMalloc(&p->d0, (size_t)max_batch * maxw * 4) == cudaSuccess &&
+            cudaMalloc(&p->d1, (size_t)max_batch * maxw * 4) == cudaSuccess;
+  for (int l = 0; ok && l <= n_layers; ++l) {
+    float* a = nullptr;
+    ok = cudaMalloc(&a, (size_t)max_batch * widths[l] * 4) == cudaSuccess;
+    p->act.push_back(a);
+    float* z = nullptr;
+    if (ok && l > 0 && l < n_layers) ok = cudaMalloc(&z, (size_t)max_batch * widths[l] * 4) == cudaSuccess;
+    p->pre.push_back(z);
+  }
+  if (!ok) {
+    cudaGetLastError();
+    delete p;
+    return atm::set_error(ATM_ERR_NOMEM, "MLP allocation failed");
+  }
+  cudaMemset(p->m, 0, off * 4);
+  cudaMemset(p->v, 0, off * 4);
+  cudaMemset(p->g, 0, off * 4);
+  *out = p;
+  return ATM_OK;
+}
+
+int atm_mlp_destroy(AtmMlp* p) {
+  if (!p) return ATM_OK;
+  cudaDeviceSynchronize();
+  delete p;
+  return ATM_OK;
+}
+
+int64_t atm_mlp_num_params(const AtmMlp* p) { return p ? (int64_t)p->n_params : -1; }
+
+int atm_mlp_set_params(AtmMlp* p, const float* host) {
+  if (!p || !host) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  MLP_CUDA(cudaMemcpy(p->w, host, p->n_params * 4, cudaMemcpyHostToDevice));
+  to_bf16_kernel<<<(unsigned)((p->n_params + 255) / 256), 256>>>(p->w, p->wb, (int)p->n_params);
+  MLP_CUDA(cudaGetLastError());
+  MLP_CUDA(cudaMemset(p->m, 0, p->n_params * 4));
+  MLP_CUDA(cudaMemset(p->v, 0, p->n_params * 4));
+  MLP_CUDA(cudaDeviceSynchronize());
+  return ATM_OK;
+}
+
+int atm_mlp_get_params(AtmMlp* p, float* host, float* host_grad) {
+  if (!p || !host) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  MLP_CUDA(cudaDeviceSynchronize());
+  MLP_CUDA(cudaMemcpy(host, p->w, p->n_params * 4, cudaMemcpyDeviceToHost));
+  if (host_grad) MLP_CUDA(cudaMemcpy(host_grad, p->g, p->n_params * 4, cudaMemcpyDeviceToHost));
+  return ATM_OK;
+}
+
+// y [batch][out] = MLP(x [batch][in]) (raw outputs, no softmax); keeps the
+// activations for atm_mlp_backward
+int atm_mlp_forward(AtmMlp* p, const float* x, int32_t batch, float* y, void* stream) {
+  if (!p || !x) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  if (batch < 1 || batch > p->max_batch) return atm::set_error(ATM_ERR_INVALID, "batch %d", batch);
+  cudaStream_t st = (cudaStream_t)stream;
+  MLP_CUDA(cudaMemcpyAsync(p->act[0], x, (size_t)batch * p->width[0] * 4, cudaMemcpyDeviceToDevice, st));
+  for (int l = 0; l < p->L; ++l) {
+    const int I = p->width[l], O = p->width[l + 1];
+    const __nv_bfloat16* W = p->wb + p->w_off[l];
+    const float* b = p->w + p->b_off[l];
+    if (l < p->L - 1)
+      MLP_CUDA((gemm<float, __nv_bfloat16, EPI_BIAS_GELU>(batch, O, I, p->act[l], I, 1, W, 1, I, p->act[l + 1], O, b,
+                                                           p->pre[l + 1], st)));
+    else
+      MLP_CUDA((gemm<float, __nv_bfloat16, EPI_BIAS>(batch, O, I, p->act[l], I, 1, W, 1, I, p->act[l + 1], O, b,
+                                                      nullptr, st)));
+  }
+  if (y) MLP_CUDA(cudaMemcpyAsync(y, p->act[p->L], (size_t)batch * p->width[p->L] * 4, cudaMemcpyDeviceToDevice, st));
+  return ATM_OK;
+}
+
+// loss of the last forward pass against targets t [batch][out]: KL over the
+// first n_hist outputs (softmax) + w_mse * MSE over the rest; loss_out (device,
+// one double) is overwritten; dy [batch][out] (device) receives dLoss/dy
+int atm_mlp_loss(AtmMlp* p, const float* t, int32_t batch, int32_t n_hist, float w_mse, double* loss_out, float* dy,
+                 void* stream) {
+  if (!p || !t || !loss_out || !dy) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  const int O = p->width[p->L];
+  if (n_hist < 1 || n_hist > O) return atm::set_error(ATM_ERR_INVALID, "n_hist %d", n_hist);
+  cudaStream_t st = (cudaStream_t)stream;
+  MLP_CUDA(cudaMemsetAsync(loss_out, 0, sizeof(double), st));
+  loss_kernel<<<(batch * 32 + 255) / 256, 256, 0, st>>>(p->act[p->L], t, batch, O, n_hist, w_mse, dy, loss_out);
+  MLP_CUDA(cudaGetLastError());
+  return ATM_OK;
+}
+
+// gradients of the parameters (kept in the MLP; copied to `grads` if given)
+// from dy [batch][out] and the activations of the last forward pass
+int atm_mlp_backward(AtmMlp* p, const float* dy, int32_t batch, float* grads, void* stream) {
+  if (!p || !dy) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  if (batch < 1 || batch > p->max_batch) return atm::set_error(ATM_ERR_INVALID, "batch %d", batch);
+  cudaStream_t st = (cudaStream_t)stream;
+  const float* dz = dy;
+  float* bufs[2] = {p->d0, p->d1};
+  int which = 0;
+  for (int l = p->L - 1; l >= 0; --l) {
+    const int I = p->width[l], O = p->width[l + 1];
+    // dW[o][i] = sum_b dz[b][o] x[b][i]
+    MLP_CUDA((gemm<float, float, EPI_NONE>(O, I, batch, dz, 1, O, p->act[l], I, 1, p->g + p->w_off[l], I, nullptr,
+                                           nullptr, st)));
+    col_sum_kernel<<<(O + 255) / 256, 256, 0, st>>>(dz, batch, O, p->g + p->b_off[l]);
+    MLP_CUDA(cudaGetLastError());
+    if (l > 0) {
+      // dx[b][i] = sum_o dz[b][o] W[o][i], times gelu'(z) of layer l's input
+      const __nv_bfloat16* W = p->wb + p->w_off[l];
+      float* dx = bufs[which];
+      MLP_CUDA((gemm<float, __nv_bfloat16, EPI_GELU_GRAD>(batch, I, O, dz, O, 1, W, I, 1, dx, I, nullptr, p->pre[l],
+                                                          st)));
+      dz = dx;
+      which ^= 1;
+    }
+  }
+  if (grads) MLP_CUDA(cudaMemcpyAsync(grads, p->g, p->n_params * 4, cudaMemcpyDeviceToDevice, st));
+  return ATM_OK;
+}
+
+int atm_mlp_adam(AtmMlp* p, float lr, float b1, float b2, float eps, int32_t step, void* stream) {
+  if (!p || step < 1) return atm::set_error(ATM_ERR_INVALID, "bad Adam arguments");
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<(unsigned)((p->n_params + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      p->w, p->wb, p->g, p->m, p->v, (int)p->n_params, lr, b1, b2, eps, c1, c2);
+  MLP_CUDA(cudaGetLastError());
+  return ATM_OK;
+}
+
+// inference: y [batch][out] with a softmax over the first n_hist outputs;
+// out_of_range[b] = 1 where an input leaves [lo, hi] (device arrays; lo/hi
+// may be NULL to skip the check)
+int atm_mlp_infer(AtmMlp* p, const float* x, int32_t batch, const float* lo, const float* hi, int32_t n_hist,
+                  float* y, int32_t* out_of_range, void* stream) {
+  if (!p || !x || !y) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int O = p->width[p->L], I0 = p->width[0];
+  for (int b0 = 0; b0 < batch; b0 += p->max_batch) {
+    const int nb = std::min(p->max_batch, batch - b0);
+    if (int rc = atm_mlp_forward(p, x + (size_t)b0 * I0, nb, y + (size_t)b0 * O, stream)) return rc;
+    infer_finish_kernel<<<(nb * 32 + 255) / 256, 256, 0, st>>>(y + (size_t)b0 * O, x + (size_t)b0 * I0, nb, O, n_hist,
+                                                               I0, lo, hi,
+                                                               (lo && hi && out_of_range) ? out_of_range + b0 : nullptr);
+    MLP_CUDA(cudaGetLastError());
+  }
+  return ATM_OK;
+}
+
+}  // extern "C"

@@ -79,4 +79,12 @@ int atm_selftest_turns(double S, double O, int N, float* half_turns) {
   return 0;
 }
 
+int atm_selftest_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  atm::Philox4 c;
+  for (int i = 0; i < 4; ++i) c.v[i] = ctr[i];
+  const atm::Philox4 r = atm::philox4x32_10(c, key[0], key[1]);
+  for (int i = 0; i < 4; ++i) out[i] = r.v[i];
+  return 0;
+}
+
 }  // extern "C"

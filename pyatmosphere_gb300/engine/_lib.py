@@ -102,6 +102,27 @@ SIGNATURES = {
     "atm_fft_screen": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                       ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_plan_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AtmChannelDesc)]),
+    "atm_draw_spectra": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+                                        ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "atm_mlp_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                      ctypes.POINTER(ctypes.c_void_p)]),
+    "atm_mlp_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "atm_mlp_num_params": (ctypes.c_int64, [ctypes.c_void_p]),
+    "atm_mlp_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_mlp_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_mlp_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                       ctypes.c_void_p]),
+    "atm_mlp_loss": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_mlp_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "atm_mlp_adam": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_int32, ctypes.c_void_p]),
+    "atm_mlp_infer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p]),
     "atm_vacuum_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
 }

@@ -48,41 +48,14 @@ class EnginePlan:
         self.n_screens = len(positions)
         self.batch = int(batch)
         self.P = 0 if f_base is None else int(len(f_base))
-        self._pos = np.ascontiguousarray(positions, dtype=np.float64)
         self._base = None if f_base is None else np.ascontiguousarray(f_base, dtype=np.float32)
-        pupils = list(pupils)
-        self.n_pupils = len(pupils)
-        self._pr = np.ascontiguousarray([p[0] for p in pupils] or [0.0], dtype=np.float64)
-        self._psx = np.ascontiguousarray([p[1] if len(p) > 1 else 0.0 for p in pupils] or [0.0], dtype=np.float64)
-        self._psy = np.ascontiguousarray([p[2] if len(p) > 2 else 0.0 for p in pupils] or [0.0], dtype=np.float64)
-        self._tr = np.ascontiguousarray(list(tracked) or [0.0], dtype=np.float64)
+        self._kw = dict(N=self.N, delta=float(delta), source=source, cheb_cut=float(cheb_cut),
+                        col_tile=int(col_tile), batch=self.batch, shift=(float(shift[0]), float(shift[1])),
+                        losses_db=float(losses_db or 0.0), path_output_loss=bool(path_output_loss),
+                        tracked=list(tracked))
+        self.n_pupils = len(list(pupils))
         self.n_tracked = len(tracked)
-        d = _lib.AtmChannelDesc()
-        d.abi_version = _lib.ABI_VERSION
-        d.resolution = self.N
-        d.delta = float(delta)
-        d.source_kind = _lib.SOURCE_PLANE if source == "plane" else _lib.SOURCE_GAUSSIAN
-        d.wvl = float(wvl)
-        d.w0 = float(w0) if w0 else 0.0
-        d.F0 = float(F0)
-        d.n_screens = self.n_screens
-        d.positions = _dptr(self._pos, ctypes.c_double)
-        d.length = float(length)
-        d.losses_db = float(losses_db or 0.0)
-        d.path_output_loss = 1 if path_output_loss else 0
-        d.points = self.P
-        d.f_base = _dptr(self._base, ctypes.c_float)
-        d.shift_x, d.shift_y = float(shift[0]), float(shift[1])
-        d.n_pupils = self.n_pupils
-        d.pupil_radius = _dptr(self._pr, ctypes.c_double)
-        d.pupil_shift_x = _dptr(self._psx, ctypes.c_double)
-        d.pupil_shift_y = _dptr(self._psy, ctypes.c_double)
-        d.n_tracked = self.n_tracked
-        d.tracked_radius = _dptr(self._tr, ctypes.c_double)
-        d.batch = self.batch
-        d.cheb_cut = float(cheb_cut)
-        d.col_tile = int(col_tile)
-        d.flags = 0
+        d = self._desc(wvl, w0, F0, positions, length, pupils)
         self._handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             check(self.lib.atm_plan_create(ctypes.byref(d), ctypes.byref(self._handle)))
@@ -90,6 +63,57 @@ class EnginePlan:
         check(self.lib.atm_plan_info(self._handle, ctypes.byref(info)))
         self.info = {f: getattr(info, f) for f, _ in _lib.AtmPlanInfo._fields_}
         self.n_out = info.n_out
+
+    def _desc(self, wvl, w0, F0, positions, length, pupils):
+        k = self._kw
+        pupils = list(pupils)
+        # keep the arrays alive while the descriptor is in use
+        self._pos = np.ascontiguousarray(positions, dtype=np.float64)
+        self._pr = np.ascontiguousarray([p[0] for p in pupils] or [0.0], dtype=np.float64)
+        self._psx = np.ascontiguousarray([p[1] if len(p) > 1 else 0.0 for p in pupils] or [0.0], dtype=np.float64)
+        self._psy = np.ascontiguousarray([p[2] if len(p) > 2 else 0.0 for p in pupils] or [0.0], dtype=np.float64)
+        self._tr = np.ascontiguousarray(k["tracked"] or [0.0], dtype=np.float64)
+        d = _lib.AtmChannelDesc()
+        d.abi_version = _lib.ABI_VERSION
+        d.resolution = k["N"]
+        d.delta = k["delta"]
+        d.source_kind = _lib.SOURCE_PLANE if k["source"] == "plane" else _lib.SOURCE_GAUSSIAN
+        d.wvl = float(wvl)
+        d.w0 = float(w0) if w0 else 0.0
+        d.F0 = float(F0)
+        d.n_screens = len(self._pos)
+        d.positions = _dptr(self._pos, ctypes.c_double)
+        d.length = float(length)
+        d.losses_db = k["losses_db"]
+        d.path_output_loss = 1 if k["path_output_loss"] else 0
+        d.points = self.P
+        d.f_base = _dptr(self._base, ctypes.c_float)
+        d.shift_x, d.shift_y = k["shift"]
+        d.n_pupils = len(pupils)
+        d.pupil_radius = _dptr(self._pr, ctypes.c_double)
+        d.pupil_shift_x = _dptr(self._psx, ctypes.c_double)
+        d.pupil_shift_y = _dptr(self._psy, ctypes.c_double)
+        d.n_tracked = len(k["tracked"])
+        d.tracked_radius = _dptr(self._tr, ctypes.c_double)
+        d.batch = k["batch"]
+        d.cheb_cut = k["cheb_cut"]
+        d.col_tile = k["col_tile"]
+        d.flags = 0
+        return d
+
+    def update(self, wvl, w0, F0, positions, length, pupils=()):
+        """Re-targets the plan (atm_plan_update): same grid, screen count,
+        spectral grid, pupil count and batch; new source / path / pupil radii."""
+        d = self._desc(wvl, w0, F0, positions, length, pupils)
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_plan_update(self._handle, ctypes.byref(d)))
+
+    def draw_spectra(self, seed, first, sqrt_psd, rho, theta, value):
+        """Seeded spectra on the device (atm_draw_spectra) into the given tensors."""
+        batch = int(rho.shape[0])
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_draw_spectra(self._handle, int(seed), int(first), _tptr(sqrt_psd), batch, _tptr(rho),
+                                            _tptr(theta), _tptr(value), _stream(self.device)))
 
     # ------------------------------------------------------------------
     def close(self):

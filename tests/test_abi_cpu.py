@@ -19,7 +19,7 @@ def built():
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "atm.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(atm_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(atm_\w+)\s*\(", src, re.M)))
 
 
 def test_library_exports_every_declared_symbol(built):
