@@ -199,7 +199,8 @@ int atm_mlp_forward(AtmMlp* mlp, const float* x, int32_t batch, float* y, void* 
 int atm_mlp_loss(AtmMlp* mlp, const float* target, int32_t batch, int32_t n_hist, float w_mse, double* loss_out,
                  float* dy, void* stream);
 int atm_mlp_backward(AtmMlp* mlp, const float* dy, int32_t batch, float* grads, void* stream);
-int atm_mlp_adam(AtmMlp* mlp, float lr, float beta1, float beta2, float eps, int32_t step, void* stream);
+int atm_mlp_adam(AtmMlp* mlp, float lr, float beta1, float beta2, float eps, float weight_decay, int32_t step,
+                 void* stream);
 int atm_mlp_infer(AtmMlp* mlp, const float* x, int32_t batch, const float* lo, const float* hi, int32_t n_hist,
                   float* y, int32_t* out_of_range, void* stream);
 

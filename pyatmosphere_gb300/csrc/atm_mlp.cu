@@ -141,7 +141,7 @@ __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict
 
 __global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, const float* __restrict__ g,
                             float* __restrict__ m, float* __restrict__ v, int n, float lr, float b1, float b2,
-                            float eps, float c1, float c2) {
+                            float eps, float c1, float c2, float wd) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i];
@@ -149,7 +149,7 @@ __global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ w
   const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
   m[i] = mi;
   v[i] = vi;
-  const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  const float wi = w[i] * (1.f - lr * wd) - lr * (mi / c1) / (sqrtf(vi / c2) + eps);  // AdamW decay
   w[i] = wi;
   wb[i] = __float2bfloat16_rn(wi);
 }
@@ -367,11 +367,12 @@ int atm_mlp_backward(AtmMlp* p, const float* dy, int32_t batch, float* grads, vo
   return ATM_OK;
 }
 
-int atm_mlp_adam(AtmMlp* p, float lr, float b1, float b2, float eps, int32_t step, void* stream) {
+int atm_mlp_adam(AtmMlp* p, float lr, float b1, float b2, float eps, float weight_decay, int32_t step,
+                 void* stream) {
   if (!p || step < 1) return atm::set_error(ATM_ERR_INVALID, "bad Adam arguments");
   const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
   adam_kernel<<<(unsigned)((p->n_params + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-      p->w, p->wb, p->g, p->m, p->v, (int)p->n_params, lr, b1, b2, eps, c1, c2);
+      p->w, p->wb, p->g, p->m, p->v, (int)p->n_params, lr, b1, b2, eps, c1, c2, weight_decay);
   MLP_CUDA(cudaGetLastError());
   return ATM_OK;
 }

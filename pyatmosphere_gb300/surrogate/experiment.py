@@ -1,0 +1,156 @@
+"""Trains the PDT surrogate and measures it against fresh simulations.
+
+    python -m pyatmosphere_gb300.surrogate.experiment --points 4000 --realisations 512 \
+        --steps 6000 --holdout 100 --eval-realisations 8192 --out model.npz --report report.json
+
+1. Data: `points` parameter points in the Box, each simulated with
+   `realisations` realisations at N = 512 (N delta = 3 m, 5 screens).
+2. Training on 90 % of the points (engine MLP kernels, Adam).
+3. Held-out evaluation: for `holdout` fresh points the surrogate's CDF is
+   compared (KS) with the empirical CDF of `eval-realisations` new
+   realisations of that point; the same is done for the nearest training
+   point's histogram (the method without the network) for comparison.
+4. Speed: surrogate queries/s on 100,000 feature vectors against simulated
+   queries/s (one point = 256 realisations at N = 1024, the fallback).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+import torch
+
+from .model import (N_HIST, Box, PointSimulator, SimConfig, Surrogate, features, ks_binned, ks_hist,
+                    targets_from_measures)
+
+
+def save(s: Surrogate, path: str):
+    np.savez_compressed(path, params=s.mlp.get_params(), widths=np.array(s.mlp.widths), mom_mean=s.mom_mean,
+                        mom_std=s.mom_std)
+
+
+def load(path: str, device=None) -> Surrogate:
+    z = np.load(path)
+    s = Surrogate(widths=tuple(int(w) for w in z["widths"]), device=device)
+    s.mlp.set_params(z["params"])
+    s.mom_mean, s.mom_std = z["mom_mean"], z["mom_std"]
+    return s
+
+
+def evaluate(s: Surrogate, box: Box, n_points: int, n_real: int, seed: int, train=None, N=512):
+    """KS of the surrogate (and of nearest-training-point lookup) against fresh simulations."""
+    rng = np.random.default_rng(seed)
+    P = box.sample(n_points, rng)
+    P["l0"] = np.round(P["l0"] * 1e3) / 1e3
+    X = features(P, box)
+    probs, _, oor = s.predict(torch.from_numpy(X).to(s.device))
+    probs = probs.cpu().numpy()
+    cfg = SimConfig(N=N, realisations=min(n_real, 2048), seed=seed)
+    sim = PointSimulator(cfg, device=s.device)
+    ks, ks_nn, kb, kb_nn = [], [], [], []
+    for i in range(n_points):
+        q = {k: v[i] for k, v in P.items()}
+        etas = []
+        for c in range(max(1, n_real // cfg.realisations)):
+            _, eta = targets_from_measures(sim.run(q, 50_000_000 + i * 64 + c), q["aperture"])
+            etas.append(eta)
+        eta = np.concatenate(etas)
+        ks.append(ks_hist(probs[i], eta))
+        kb.append(ks_binned(probs[i], eta))
+        if train is not None:
+            Xt, Yt = train
+            j = int(np.argmin(((Xt - X[i]) ** 2).sum(axis=1)))
+            ks_nn.append(ks_hist(Yt[j, :N_HIST], eta))
+            kb_nn.append(ks_binned(Yt[j, :N_HIST], eta))
+    sim.plan.close()
+    return {"ks": np.array(ks), "ks_binned": np.array(kb), "ks_nn": np.array(ks_nn), "ks_binned_nn": np.array(kb_nn)}
+
+
+def speed(s: Surrogate, box: Box, n_queries=100_000, seed=3):
+    rng = np.random.default_rng(seed)
+    X = torch.from_numpy(features(box.sample(n_queries, rng), box)).to(s.device)
+    for _ in range(3):
+        s.predict(X)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    reps = 10
+    for _ in range(reps):
+        s.predict(X)
+    torch.cuda.synchronize()
+    q_per_s = n_queries * reps / (time.perf_counter() - t)
+    # simulation per query: the fallback configuration (N = 1024, 256 realisations)
+    cfg = SimConfig(N=1024, realisations=256)
+    sim = PointSimulator(cfg, device=s.device)
+    P = box.sample(4, np.random.default_rng(seed + 1))
+    P["l0"][:] = 6e-3
+    q0 = {k: v[0] for k, v in P.items()}
+    sim.run(q0, 0)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for i in range(1, 4):
+        m = sim.run({k: v[i] for k, v in P.items()}, i)
+        targets_from_measures(m, P["aperture"][i])
+    torch.cuda.synchronize()
+    sim_q_per_s = 3 / (time.perf_counter() - t)
+    sim.plan.close()
+    return q_per_s, sim_q_per_s
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--points", type=int, default=4000)
+    ap.add_argument("--realisations", type=int, default=512)
+    ap.add_argument("--steps", type=int, default=6000)
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--holdout", type=int, default=100)
+    ap.add_argument("--eval-realisations", type=int, default=8192)
+    ap.add_argument("--out", default="pdt_mlp.npz")
+    ap.add_argument("--report", default="surrogate_report.json")
+    ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--weight-decay", type=float, default=1e-4)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    a = ap.parse_args()
+    box = Box()
+    t0 = time.perf_counter()
+    P, X, Y, _ = Surrogate.generate(box, a.points, SimConfig(realisations=a.realisations), seed=a.seed)
+    t_gen = time.perf_counter() - t0
+    n_tr = int(0.9 * len(X))
+    perm = np.random.default_rng(a.seed).permutation(len(X))
+    tr, va = perm[:n_tr], perm[n_tr:]
+    s = Surrogate(box)
+    t0 = time.perf_counter()
+    losses = s.fit(X[tr], Y[tr], steps=a.steps, batch=a.batch, log_every=max(1, a.steps // 20), lr=a.lr,
+                   weight_decay=a.weight_decay)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    save(s, a.out)
+    # validation split of the generated data (noisy targets, informative only)
+    pv, _, _ = s.predict(torch.from_numpy(X[va]).to(s.device))
+    kl_val = float(np.mean(np.sum(np.where(Y[va, :N_HIST] > 0, Y[va, :N_HIST] *
+                                          (np.log(np.maximum(Y[va, :N_HIST], 1e-30)) -
+                                           np.log(np.maximum(pv.cpu().numpy(), 1e-30))), 0), axis=1)))
+    ev = evaluate(s, box, a.holdout, a.eval_realisations, seed=a.seed + 100, train=(X[tr], Y[tr]))
+    ks, ks_nn, kb, kb_nn = ev["ks"], ev["ks_nn"], ev["ks_binned"], ev["ks_binned_nn"]
+    q_s, sim_q_s = speed(s, box)
+    rep = {
+        "points": a.points, "realisations_per_point": a.realisations, "train_points": n_tr,
+        "generation_s": t_gen, "training_s": t_train, "steps": a.steps, "loss_curve": losses,
+        "val_kl": kl_val, "holdout_points": a.holdout, "eval_realisations": a.eval_realisations,
+        "ks_mean": float(ks.mean()), "ks_median": float(np.median(ks)), "ks_p90": float(np.quantile(ks, 0.9)),
+        "ks_frac_le_0.02": float((ks <= 0.02).mean()),
+        "ks_nearest_train_mean": float(ks_nn.mean()), "ks_nearest_train_median": float(np.median(ks_nn)),
+        "ks_binned_mean": float(kb.mean()), "ks_binned_median": float(np.median(kb)),
+        "ks_binned_frac_le_0.02": float((kb <= 0.02).mean()), "ks_binned_p90": float(np.quantile(kb, 0.9)),
+        "ks_binned_nearest_train_mean": float(kb_nn.mean()), "ks_binned_nearest_train_median": float(np.median(kb_nn)),
+        "ks_noise_floor": 0.87 / np.sqrt(a.eval_realisations),
+        "queries_per_s": q_s, "simulated_queries_per_s": sim_q_s, "speedup": q_s / sim_q_s,
+    }
+    with open(a.report, "w") as f:
+        json.dump(rep, f, indent=1)
+    print(json.dumps({k: v for k, v in rep.items() if k != "loss_curve"}))
+
+
+if __name__ == "__main__":
+    main()

@@ -67,9 +67,10 @@ class EngineMLP:
         check(self.lib.atm_mlp_backward(self._h, _vp(dy), B, None, self._stream()))
         return self._loss
 
-    def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+    def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, weight_decay=0.0):
         self._step += 1
-        check(self.lib.atm_mlp_adam(self._h, float(lr), float(b1), float(b2), float(eps), self._step, self._stream()))
+        check(self.lib.atm_mlp_adam(self._h, float(lr), float(b1), float(b2), float(eps), float(weight_decay),
+                                    self._step, self._stream()))
 
     def infer(self, x, lo=None, hi=None, n_hist=64):
         B = int(x.shape[0])

@@ -137,6 +137,13 @@ def targets_from_measures(m: torch.Tensor, aperture: float) -> np.ndarray:
     return np.concatenate([hist, [eta.mean(), np.log10(bw2 + 1e-12), np.log10(lt + 1e-12)]]).astype(np.float32), eta
 
 
+def ks_binned(probs: np.ndarray, samples: np.ndarray) -> float:
+    """KS distance at the histogram's own resolution: the two CDFs compared at
+    the 65 bin edges on [0, 1]."""
+    emp = np.histogram(np.clip(samples, 0, 1), bins=N_HIST, range=(0.0, 1.0))[0] / max(1, len(samples))
+    return float(np.max(np.abs(np.cumsum(probs) - np.cumsum(emp))))
+
+
 def ks_hist(probs: np.ndarray, samples: np.ndarray) -> float:
     """Kolmogorov-Smirnov distance between a 64-bin histogram on [0, 1]
     (CDF linear inside bins) and the empirical CDF of samples."""
@@ -188,7 +195,8 @@ class Surrogate:
         return P, features(P, box), Y, samples
 
     # --------------------------------------------------------------- train
-    def fit(self, X: np.ndarray, Y: np.ndarray, steps=3000, batch=512, lr=1e-3, w_mse=1.0, seed=0, log_every=0):
+    def fit(self, X: np.ndarray, Y: np.ndarray, steps=3000, batch=512, lr=1e-3, w_mse=1.0, seed=0, log_every=0,
+            weight_decay=0.0):
         self.mom_mean = Y[:, N_HIST:].mean(axis=0)
         self.mom_std = Y[:, N_HIST:].std(axis=0) + 1e-6
         Yn = Y.copy()
@@ -207,7 +215,7 @@ class Surrogate:
             yb = Yd.index_select(0, idx).contiguous()
             self.mlp.forward(xb)
             loss = self.mlp.loss_backward(yb, N_HIST, w_mse)
-            self.mlp.adam(lr=lr * (0.5 * (1 + math.cos(math.pi * s / steps))) + 1e-5)
+            self.mlp.adam(lr=lr * (0.5 * (1 + math.cos(math.pi * s / steps))) + 1e-5, weight_decay=weight_decay)
             if log_every and s % log_every == 0:
                 losses.append(float(loss.item()))
         return losses
