@@ -47,6 +47,10 @@ extern "C" {
 
 #define ATM_MAX_PUPILS 8
 
+/* AtmChannelDesc.flags */
+#define ATM_FLAG_SIMT_GEMM 1     /* screen GEMM on FP32 SIMT cores (no tensor cores) */
+#define ATM_FLAG_TC_GEMM 2       /* screen GEMM on tcgen05 tensor cores (N >= 256) */
+
 /* per-realisation doubles in measures_out (slot index) */
 #define ATM_OUT_ETA_TOTAL 0      /* measures.eta(pupil=False)      measures.py:7-8   */
 #define ATM_OUT_MEAN_X 1         /* measures.mean_x                measures.py:11-13 */
@@ -84,7 +88,7 @@ typedef struct AtmChannelDesc {
   int32_t batch;              /* maximum realisations per atm_run */
   double cheb_cut;            /* low-frequency block: annuli below cheb_cut/(N delta); 0 = 4 */
   int32_t col_tile;           /* column-pass tile (columns per CTA); 0 = default */
-  int32_t flags;              /* reserved, 0 */
+  int32_t flags;              /* ATM_FLAG_*; 0 = defaults */
 } AtmChannelDesc;
 
 typedef struct AtmPlanInfo {
@@ -203,6 +207,15 @@ int atm_mlp_adam(AtmMlp* mlp, float lr, float beta1, float beta2, float eps, flo
                  void* stream);
 int atm_mlp_infer(AtmMlp* mlp, const float* x, int32_t batch, const float* lo, const float* hi, int32_t n_hist,
                   float* y, int32_t* out_of_range, void* stream);
+
+/* Unit-test entry point of the tensor-core screen GEMM: out[s][m][n] =
+ * scale * sum_k A[s][m][k] B[s][n][k] for FP32 device arrays (row stride K),
+ * computed with tcgen05 MMAs on FP16 hi/lo slices; M % 128 == 0,
+ * N % 256 == 0.  Allocates its slice scratch; synchronises the stream.  No
+ * reference counterpart (the reference's screen product is a cupy/numpy
+ * complex GEMM, phase_screens.py:125-126). */
+int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32_t N, int32_t K, float scale,
+                     float* out, void* stream);
 
 /* Launch categories reported by atm_profile_end. */
 #define ATM_KIND_SCREEN_PREP 0

@@ -25,7 +25,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
 
-ENGINE_SOURCES = ["atm_kernels.cu", "atm_abi.cu", "atm_noalloc.cu", "atm_mlp.cu"]
+ENGINE_SOURCES = ["atm_kernels.cu", "atm_abi.cu", "atm_noalloc.cu", "atm_mlp.cu", "atm_tc.cu"]
 SELFTEST_SOURCES = ["atm_selftest.cu"]
 HEADERS = ["atm_common.cuh", "atm_internal.h"]
 

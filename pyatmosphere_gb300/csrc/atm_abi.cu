@@ -152,6 +152,9 @@ struct AtmPlan {
       intensity, tracked_r, fbase;
   std::vector<float> f_base;
   double cheb_cut = 0.0;
+  bool use_tc = false;  // screen GEMM on tensor cores
+  int Kp = 0, kc0 = 0;  // tensor-core layout
+  DevBuf ta_hi, ta_lo, tb_hi, tb_lo;
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
     int64_t s = 0;
@@ -409,6 +412,12 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
     delete pl;
     return fail(ATM_ERR_UNSUPPORTED, "too many low-frequency annuli (%d) for the prep kernel", pl->P_L);
   }
+  pl->use_tc = pl->n > 0 && pl->N >= 256 && (d->flags & ATM_FLAG_TC_GEMM) && !(d->flags & ATM_FLAG_SIMT_GEMM);
+  if (pl->use_tc) {
+    pl->kc0 = 2 * pl->P_H;
+    const int kraw = pl->kc0 + (pl->P_L > 0 ? pl->D - 1 : 0);
+    pl->Kp = std::max(64, (kraw + 63) / 64 * 64);
+  }
   pl->rows = atm::row_pass_rows(pl->N);
   pl->n_parts = pl->N / pl->rows;
   pl->n_meas = 6 + pl->n_pupils;
@@ -431,10 +440,25 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
     delete pl;
     return rc;
   }
+  if (pl->use_tc) {
+    const size_t th = B * N * (size_t)pl->Kp * sizeof(__half);
+    if ((rc = dev_alloc(pl->ta_hi, th, v)) || (rc = dev_alloc(pl->ta_lo, th, v)) ||
+        (rc = dev_alloc(pl->tb_hi, th, v)) || (rc = dev_alloc(pl->tb_lo, th, v))) {
+      delete pl;
+      return rc;
+    }
+    for (DevBuf* b : {&pl->ta_hi, &pl->ta_lo, &pl->tb_hi, &pl->tb_lo}) {
+      if (cudaMemset(b->p, 0, b->bytes) != cudaSuccess) {
+        delete pl;
+        return fail(ATM_ERR_CUDA, "cudaMemset of the tensor-core tables failed");
+      }
+    }
+  }
   if (pl->n > 0) {
+    const size_t simt_rows = pl->use_tc ? 0 : 1;  // FP32 SIMT tables only without tensor cores
     if ((rc = dev_alloc(pl->phi, B * plane * sizeof(float), v)) ||
-        (rc = dev_alloc(pl->At, B * pl->KH * N * sizeof(float), v)) ||
-        (rc = dev_alloc(pl->Bt, B * K * N * sizeof(float), v)) ||
+        (rc = dev_alloc(pl->At, simt_rows * B * pl->KH * N * sizeof(float), v)) ||
+        (rc = dev_alloc(pl->Bt, simt_rows * B * K * N * sizeof(float), v)) ||
         (rc = dev_alloc(pl->Ach, (size_t)pl->KC * N * sizeof(float), v)) ||
         (rc = dev_alloc(pl->ht, B * (pl->KH / 2) * sizeof(atm::HighTerm), v)) ||
         (rc = dev_alloc(pl->Py, B * N * sizeof(float2), v)) || (rc = dev_alloc(pl->Px, B * N * sizeof(float2), v)) ||
@@ -458,6 +482,16 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   if ((rc = plan_tables(pl, d))) {
     delete pl;
     return rc;
+  }
+  if (pl->use_tc && pl->P_L > 0) {
+    // Chebyshev columns of A are the same for every screen: written once
+    cudaError_t e = atm::launch_cheb_cols_tc(pl->B, pl->N, pl->Kp, pl->kc0, pl->D, (const float*)pl->Ach.p,
+                                             (__half*)pl->ta_hi.p, (__half*)pl->ta_lo.p, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+      delete pl;
+      return fail(ATM_ERR_CUDA, "Chebyshev columns: %s", cudaGetErrorString(e));
+    }
   }
   *out = pl;
   return ATM_OK;
@@ -492,7 +526,7 @@ int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
   info->n_out = pl->n_out;
   info->low_annuli = pl->P_L;
   info->cheb_terms = pl->D;
-  info->gemm_k = pl->KH + pl->KC;
+  info->gemm_k = pl->use_tc ? pl->Kp : pl->KH + pl->KC;
   info->workspace_bytes = pl->bytes();
   int launches = 0;
   for (int i = 0; i < pl->n; ++i) launches += 4 + (pl->dz[i + 1] > 0 ? 1 : 0);
@@ -549,6 +583,14 @@ atm::ScreenArgs screen_args(AtmPlan* pl, const float* rho, const float* theta, c
   s.Bt = (float*)pl->Bt.p;
   s.Gy = nullptr;
   s.Hx = nullptr;
+  if (pl->use_tc) {
+    s.ta_hi = (__half*)pl->ta_hi.p;
+    s.ta_lo = (__half*)pl->ta_lo.p;
+    s.tb_hi = (__half*)pl->tb_hi.p;
+    s.tb_lo = (__half*)pl->tb_lo.p;
+    s.Kp = pl->Kp;
+    s.kc0 = pl->kc0;
+  }
   return s;
 }
 
@@ -556,6 +598,17 @@ int run_screen(AtmPlan* pl, const atm::ScreenArgs& s, int B, cudaStream_t st) {
   {
     Prof p(pl, ATM_KIND_SCREEN_PREP, st);
     ATM_CUDA(atm::launch_screen_prep(B, s, st));
+  }
+  if (pl->use_tc) {
+    {
+      Prof p(pl, ATM_KIND_SCREEN_TABLE, st);
+      ATM_CUDA(atm::launch_screen_table_tc(B, s, st));
+    }
+    Prof p(pl, ATM_KIND_SCREEN_GEMM, st);
+    ATM_CUDA(atm::launch_tc_gemm(B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p, (const __half*)pl->ta_lo.p,
+                                 (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p, (float*)pl->phi.p,
+                                 0.15915494309189533577f, st));
+    return ATM_OK;
   }
   if (pl->P_H > 0) {
     Prof p(pl, ATM_KIND_SCREEN_TABLE, st);

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace atm {
@@ -99,6 +100,13 @@ struct ScreenArgs {
   float* Bt;                // [B][KH+KC][N]
   double* Gy;               // [B][N] FP64 phase of the y-only part (nullable)
   double* Hx;               // [B][N] FP64 phase of the x-only part (nullable)
+  // tensor-core layout (K-major FP16 hi/lo slices, [B][N][Kp]); null: FP32 SIMT layout
+  __half* ta_hi;
+  __half* ta_lo;
+  __half* tb_hi;
+  __half* tb_lo;
+  int Kp;                   // padded K of the tensor-core layout
+  int kc0;                  // first Chebyshev column (2 P_H)
 };
 
 // GEMM: phi[s][y][x] = sum_k At[s][k][y] B[s][k][x], k < KH from At, then the
@@ -147,6 +155,13 @@ int row_pass_rows(int N);          // rows per CTA of the row pass
 int col_tile_default(int N);
 bool supported_n(int N);
 size_t prep_smem_bytes(int P_L, int D);
+size_t tc_smem_bytes();
+cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
+                           const __half* b_lo, float* out, float scale, cudaStream_t st);
+cudaError_t launch_screen_table_tc(int B, const ScreenArgs& a, cudaStream_t st);
+cudaError_t launch_cheb_cols_tc(int B, int N, int Kp, int kc0, int D, const float* Ach, __half* hi, __half* lo,
+                                cudaStream_t st);
+cudaError_t tc_error_flag(int* host_flag, bool reset);
 // records the message returned by atm_last_error() on this host thread; returns code
 int set_error(int code, const char* fmt, ...);
 

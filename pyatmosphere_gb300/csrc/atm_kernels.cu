@@ -294,21 +294,46 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
+// Per-device cache of (attribute set, resident CTAs per SM, SM count) for one
+// kernel: after the first launch on a device, launching makes no other CUDA
+// API call (so a stream can be captured into a CUDA graph around it).
+struct LaunchCache {
+  static constexpr int kDev = 64;
+  int per_sm[kDev] = {};
+  int sms[kDev] = {};
+  template <class K>
+  cudaError_t get(K kernel, int threads, size_t smem, int* grid_max) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kDev) return cudaErrorInvalidDevice;
+    if (per_sm[dev] == 0) {
+      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      int nb = 0, n_sm = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem);
+      if (e != cudaSuccess) return e;
+      e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      sms[dev] = n_sm;
+      per_sm[dev] = std::max(nb, 1);
+    }
+    *grid_max = sms[dev] * per_sm[dev];
+    return cudaSuccess;
+  }
+};
+
 template <int N>
 static cudaError_t row_pipe_launch(int B, const RowArgs& a, cudaStream_t st) {
   constexpr int ROWS = RowRows<N>::value;
+  static LaunchCache cache;
   const int threads = ROWS * (N / 16);
   const size_t smem = RowPipe<N>::SMEM;
-  cudaError_t e = cudaFuncSetAttribute(row_pass_pipe_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_pass_pipe_kernel<N>, threads, smem);
+  int grid_max = 0;
+  cudaError_t e = cache.get(row_pass_pipe_kernel<N>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / ROWS);
-  const int grid = std::max(1, std::min(n_items, sms * std::max(per_sm, 1)));
+  const int grid = std::max(1, std::min(n_items, grid_max));
   row_pass_pipe_kernel<N><<<grid, threads, smem, st>>>(a, n_items);
   return cudaGetLastError();
 }
@@ -318,9 +343,13 @@ static cudaError_t row_plain_launch(int B, const RowArgs& a, cudaStream_t st) {
   constexpr int ROWS = RowRows<N>::value;
   const int threads = ROWS * (N / 16);
   const size_t smem = (size_t)ROWS * Padded<N>::value * sizeof(float2);
-  if (smem > 48 * 1024) {
+  static bool attr_done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (smem > 48 * 1024 && dev >= 0 && dev < 64 && !attr_done[dev]) {
     cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    attr_done[dev] = true;
   }
   dim3 grid(N / ROWS, B);
   row_pass_kernel<N><<<grid, threads, smem, st>>>(a);
@@ -454,18 +483,14 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
 
 template <int N, int C>
 static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
+  static LaunchCache cache;
   const int threads = C * (N / 16);
   const size_t smem = ColPipe<N, C>::SMEM;
-  cudaError_t e = cudaFuncSetAttribute(col_pass_pipe_kernel<N, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_pass_pipe_kernel<N, C>, threads, smem);
+  int grid_max = 0;
+  cudaError_t e = cache.get(col_pass_pipe_kernel<N, C>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / C);
-  const int grid = std::max(1, std::min(n_items, sms * std::max(per_sm, 1)));
+  const int grid = std::max(1, std::min(n_items, grid_max));
   col_pass_pipe_kernel<N, C><<<grid, threads, smem, st>>>(a, n_items);
   return cudaGetLastError();
 }
@@ -474,9 +499,13 @@ template <int N, int C>
 static cudaError_t col_plain_launch(int B, const ColArgs& a, cudaStream_t st) {
   const int threads = C * (N / 16);
   const size_t smem = (size_t)C * ColStride<N, C>::value * sizeof(float2);
-  if (smem > 48 * 1024) {
+  static bool attr_done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (smem > 48 * 1024 && dev >= 0 && dev < 64 && !attr_done[dev]) {
     cudaError_t e = cudaFuncSetAttribute(col_pass_kernel<N, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    attr_done[dev] = true;
   }
   dim3 grid(N / C, B);
   col_pass_kernel<N, C><<<grid, threads, smem, st>>>(a);
@@ -706,17 +735,33 @@ __global__ void __launch_bounds__(kPrepThreads) screen_prep_kernel(ScreenArgs a)
         T0 = T1;
         T1 = Tn;
       }
-      Bt[(size_t)(a.KH + e - 1) * N + j] = acc;
+      if (a.tb_hi) {
+        // tensor-core layout: B[x][kc0 + e - 1] as FP16 hi / scaled lo
+        const size_t o = ((size_t)r * N + j) * a.Kp + a.kc0 + e - 1;
+        const __half h = __float2half_rn(acc);
+        a.tb_hi[o] = h;
+        a.tb_lo[o] = __float2half_rn((acc - __half2float(h)) * 2048.f);
+      } else {
+        Bt[(size_t)(a.KH + e - 1) * N + j] = acc;
+      }
     }
-    for (int e = D - 1; e < a.KC; ++e) Bt[(size_t)(a.KH + e) * N + j] = 0.f;
+    if (!a.tb_hi)
+      for (int e = D - 1; e < a.KC; ++e) Bt[(size_t)(a.KH + e) * N + j] = 0.f;
   }
 }
 
 cudaError_t launch_screen_prep(int B, const ScreenArgs& a, cudaStream_t st) {
   if (a.D > kMaxD || a.D < 2) return cudaErrorInvalidValue;
   const size_t smem = prep_smem_bytes(a.P_L, a.D);
-  cudaError_t e = cudaFuncSetAttribute(screen_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  static int attr_set[64] = {};  // largest dynamic shared memory already granted, per device
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+  if ((int)smem > attr_set[dev]) {
+    e = cudaFuncSetAttribute(screen_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_set[dev] = 220 * 1024;
+  }
   screen_prep_kernel<<<B, kPrepThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
@@ -742,6 +787,58 @@ __global__ void __launch_bounds__(256) screen_table_kernel(ScreenArgs a) {
   float* Bt = a.Bt + ((size_t)r * K + 2 * q) * N;
   Bt[j] = cx;
   Bt[N + j] = sx;
+}
+
+// tensor-core layout of the high-frequency tables: thread (term q, row j)
+// writes A[j][2q..2q+1] and B[j][2q..2q+1] as FP16 hi / scaled lo pairs
+__device__ __forceinline__ void split_pair(float u, float w, __half2* hi, __half2* lo) {
+  const __half uh = __float2half_rn(u), wh = __float2half_rn(w);
+  *hi = __halves2half2(uh, wh);
+  *lo = __halves2half2(__float2half_rn((u - __half2float(uh)) * 2048.f),
+                       __float2half_rn((w - __half2float(wh)) * 2048.f));
+}
+
+__global__ void __launch_bounds__(128) screen_table_tc_kernel(ScreenArgs a) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, r = blockIdx.z, N = a.N;
+  if (q >= a.P_H) return;
+  const HighTerm h = a.hterms[(size_t)r * (a.KH / 2) + q];
+  const uint64_t ju = (uint64_t)j;
+  float sy, cy, sx, cx;
+  sincospif(fixed_to_halfturns(h.sy * ju + h.oy), &sy, &cy);
+  sincospif(fixed_to_halfturns(h.sx * ju + h.ox), &sx, &cx);
+  const size_t o = ((size_t)r * N + j) * a.Kp + 2 * q;
+  split_pair(h.v.x * cy - h.v.y * sy, -(h.v.x * sy + h.v.y * cy), reinterpret_cast<__half2*>(a.ta_hi + o),
+             reinterpret_cast<__half2*>(a.ta_lo + o));
+  split_pair(cx, sx, reinterpret_cast<__half2*>(a.tb_hi + o), reinterpret_cast<__half2*>(a.tb_lo + o));
+}
+
+cudaError_t launch_screen_table_tc(int B, const ScreenArgs& a, cudaStream_t st) {
+  if (a.P_H == 0) return cudaSuccess;
+  dim3 grid((a.P_H + 127) / 128, a.N, B);
+  screen_table_tc_kernel<<<grid, 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+// Chebyshev columns of A (T_e(t_y), the same for every screen), written once
+__global__ void cheb_cols_tc_kernel(int N, int Kp, int kc0, int D, const float* __restrict__ Ach,
+                                    __half* __restrict__ hi, __half* __restrict__ lo) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+  if (j >= N) return;
+  for (int e = 1; e < D; ++e) {
+    const float v = Ach[(size_t)(e - 1) * N + j];
+    const __half h = __float2half_rn(v);
+    const size_t o = ((size_t)r * N + j) * Kp + kc0 + e - 1;
+    hi[o] = h;
+    lo[o] = __float2half_rn((v - __half2float(h)) * 2048.f);
+  }
+}
+
+cudaError_t launch_cheb_cols_tc(int B, int N, int Kp, int kc0, int D, const float* Ach, __half* hi, __half* lo,
+                                cudaStream_t st) {
+  dim3 grid((N + 255) / 256, B);
+  cheb_cols_tc_kernel<<<grid, 256, 0, st>>>(N, Kp, kc0, D, Ach, hi, lo);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_screen_table(int B, const ScreenArgs& a, cudaStream_t st) {

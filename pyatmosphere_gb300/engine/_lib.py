@@ -17,6 +17,8 @@ SELFTEST_PATH = os.path.join(LIB_DIR, "libatm_selftest.so")
 
 ABI_VERSION = 1
 MAX_PUPILS = 8
+FLAG_SIMT_GEMM = 1
+FLAG_TC_GEMM = 2
 SOURCE_GAUSSIAN = 0
 SOURCE_PLANE = 1
 
@@ -123,6 +125,9 @@ SIGNATURES = {
     "atm_mlp_infer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p]),
+    "atm_tc_gemm_test": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
     "atm_vacuum_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
 }

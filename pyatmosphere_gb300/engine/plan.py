@@ -38,7 +38,7 @@ class EnginePlan:
                  losses_db: float = 0.0, path_output_loss: bool = False,
                  shift: Sequence[float] = (0.0, 0.0), pupils: Sequence[tuple] = (),
                  tracked: Sequence[float] = (), batch: int = 1, source: str = "gaussian",
-                 cheb_cut: float = 0.0, col_tile: int = 0, device=None):
+                 cheb_cut: float = 0.0, col_tile: int = 0, device=None, flags: int = 0):
         if not torch.cuda.is_available():
             raise _lib.EngineError("the GB300 engine needs a CUDA device; none is available")
         self.lib = load()
@@ -52,7 +52,7 @@ class EnginePlan:
         self._kw = dict(N=self.N, delta=float(delta), source=source, cheb_cut=float(cheb_cut),
                         col_tile=int(col_tile), batch=self.batch, shift=(float(shift[0]), float(shift[1])),
                         losses_db=float(losses_db or 0.0), path_output_loss=bool(path_output_loss),
-                        tracked=list(tracked))
+                        tracked=list(tracked), flags=int(flags))
         self.n_pupils = len(list(pupils))
         self.n_tracked = len(tracked)
         d = self._desc(wvl, w0, F0, positions, length, pupils)
@@ -98,7 +98,7 @@ class EnginePlan:
         d.batch = k["batch"]
         d.cheb_cut = k["cheb_cut"]
         d.col_tile = k["col_tile"]
-        d.flags = 0
+        d.flags = k["flags"]
         return d
 
     def update(self, wvl, w0, F0, positions, length, pupils=()):
@@ -177,6 +177,26 @@ class EnginePlan:
         with torch.cuda.device(self.device):
             check(self.lib.atm_measures(self._handle, _tptr(field), batch, _tptr(out), _stream(self.device)))
         return out
+
+    def capture(self, rho, theta, value, out=None):
+        """Captures one atm_run on these (fixed) tensors into a CUDA graph and
+        returns (graph, out): graph.replay() re-runs the whole launch
+        sequence with one launch call.  Refill rho / theta / value in place
+        between replays.  A warm-up run outside the capture comes first so
+        that the engine's per-device launch settings are already cached."""
+        batch = int(rho.shape[0]) if rho is not None else self.batch
+        if out is None:
+            out = torch.empty((batch, self.n_out), dtype=torch.float64, device=self.device)
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            self.run(rho, theta, value, out=out)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            self.run(rho, theta, value, out=out)
+        return g, out
 
     # ------------------------------------------------------------------
     def profile_begin(self, max_launches: int):

@@ -185,3 +185,26 @@ def test_config2_geometry_matches_oracle(torch_cuda):
     res, u = o.simulate(spec, rho, theta, value, return_field=True)
     assert o.rel_l2(field[0], u) < FIELD_TOL
     assert meas[0, 8] == pytest.approx(res[0]["eta_0"], rel=1e-5)
+
+
+def test_graph_capture_replays_run(torch_cuda):
+    """atm_run captured into a CUDA graph gives the direct run's results, also
+    after the inputs are refilled in place."""
+    torch = torch_cuda
+    spec = o.ChannelSpec(N=256, delta=4e-3, w0=0.08, length=8e3, count=3, points=256, Cn2=2e-15, pupil_radius=0.1)
+    plan, base = make_plan(spec, batch=2)
+    sp1 = spectra(spec, base, seed=1, R=2)
+    sp2 = spectra(spec, base, seed=2, R=2)
+    r, t, v = to_dev(torch, *sp1)
+    g, out = plan.capture(r, t, v)
+    g.replay()
+    torch.cuda.synchronize()
+    direct = plan.run(*to_dev(torch, *sp1)).cpu().numpy()
+    np.testing.assert_array_equal(out.cpu().numpy(), direct)
+    for dst, src in zip((r, t, v), to_dev(torch, *sp2)):
+        dst.copy_(src)
+    g.replay()
+    torch.cuda.synchronize()
+    direct2 = plan.run(*to_dev(torch, *sp2)).cpu().numpy()
+    np.testing.assert_array_equal(out.cpu().numpy(), direct2)
+    assert not np.array_equal(direct, direct2)

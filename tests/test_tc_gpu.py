@@ -1,0 +1,65 @@
+"""The tensor-core screen GEMM (tcgen05, FP16 hi/lo slices, FP32 TMEM
+accumulation) against an FP64 numpy product."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("S,M,N,K", [(1, 128, 256, 64), (2, 256, 512, 200), (1, 512, 512, 768)])
+def test_tc_gemm_matches_fp64(S, M, N, K):
+    import torch
+    from pyatmosphere_gb300.engine import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((S, M, K)).astype(np.float32)
+    B = rng.standard_normal((S, N, K)).astype(np.float32)
+    Ad, Bd = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    out = torch.empty((S, M, N), dtype=torch.float32, device="cuda")
+    rc = lib.atm_tc_gemm_test(ctypes.c_void_p(Ad.data_ptr()), ctypes.c_void_p(Bd.data_ptr()), S, M, N, K, 0.5,
+                              ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, lib.atm_last_error()
+    ref = 0.5 * np.einsum("smk,snk->smn", A.astype(np.float64), B.astype(np.float64))
+    got = out.cpu().numpy().astype(np.float64)
+    err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert err < 2e-6, err
+
+
+@pytest.mark.parametrize("N,P,Cn2,delta", [(256, 512, 1e-14, 4e-3), (2048, 1024, 5e-16, 1.5e-3)])
+def test_tc_screen_matches_oracle(N, P, Cn2, delta):
+    """Screens through the tensor-core GEMM against the FP64 oracle."""
+    import torch
+    from oracle import atm_oracle as o
+    from pyatmosphere_gb300.engine import EnginePlan, _lib
+    spec = o.ChannelSpec(N=N, delta=delta, points=P, Cn2=Cn2, count=2, length=10e3)
+    base = o.logpolar_base(P, spec.f_min, spec.f_max)
+    plan = EnginePlan(N, delta, spec.wvl, spec.w0, spec.F0, o.screen_positions(spec.length, 2), spec.length,
+                      f_base=base, batch=2, flags=_lib.FLAG_TC_GEMM)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, Cn2, spec.l0, spec.L0, use_scipy=False)
+    rho, theta, value = o.draw_spectra(N, range(2), 2, base, psd)
+    r, t, v = [torch.from_numpy(a).cuda() for a in (rho, theta, value)]
+    ph = torch.empty((2, N, N), dtype=torch.complex64, device="cuda")
+    plan.screen(r, t, v, 1, phasor_out=ph)
+    ph = ph.cpu().numpy()
+    for b in range(2):
+        ref = o.ss_screen(rho[b, 1], theta[b, 1], value[b, 1], N, delta)
+        assert o.rel_l2(ph[b], np.exp(-1j * ref)) < 1e-5
+
+
+def test_tc_channel_config2_matches_oracle():
+    import torch
+    from oracle import atm_oracle as o
+    from pyatmosphere_gb300.engine import EnginePlan, _lib
+    spec = o.ChannelSpec(N=2048, delta=1.5e-3, w0=0.12, length=50e3, Cn2=5e-16, pupil_radius=0.2)
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    rho, theta, value = o.draw_spectra(99, range(1), spec.count, base, psd)
+    plan = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, o.screen_positions(spec.length, spec.count),
+                      spec.length, f_base=base, pupils=[(0.2,)], batch=1, flags=_lib.FLAG_TC_GEMM)
+    field = torch.empty((1, 2048, 2048), dtype=torch.complex64, device="cuda")
+    meas = plan.run(*[torch.from_numpy(a).cuda() for a in (rho, theta, value)], field_out=field).cpu().numpy()
+    res, u = o.simulate(spec, rho, theta, value, return_field=True)
+    assert o.rel_l2(field.cpu().numpy()[0], u) < 1e-4
+    assert meas[0, 8] == pytest.approx(res[0]["eta_0"], rel=1e-5)
