@@ -176,8 +176,10 @@ def run_gb300(args, rank, world, local_rank):
     B = args.batch
     base, psd = base_and_psd()
     pos = positions(w["length"], w["count"])
+    from pyatmosphere_gb300.engine import _lib
+    flags = {"tc": _lib.FLAG_TC_GEMM, "simt": _lib.FLAG_SIMT_GEMM, "auto": 0}[args.gemm]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
-                      pupils=[(w["pupil_radius"],)], batch=B, device=dev)
+                      pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags)
     n_steps = args.warmup + args.steps
     # distinct seeded inputs per step (weak scaling: each rank its own realisations)
     host = []
@@ -246,7 +248,7 @@ def run_gb300(args, rank, world, local_rank):
     plain = None
     if args.plain > 0 and rank == 0:
         p1 = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
-                        pupils=[(w["pupil_radius"],)], batch=1, device=dev)
+                        pupils=[(w["pupil_radius"],)], batch=1, device=dev, flags=flags)
         one = [t[:1].contiguous() for t in devin[0]]
         for _ in range(2):
             p1.run(*one)
@@ -263,8 +265,10 @@ def run_gb300(args, rank, world, local_rank):
     # ---- roofline of the dominant kernel, measured in the timed region ----
     N, n = w["N"], w["count"]
     K = plan.info["gemm_k"]
+    tc = plan.info.get("gemm_k", 0) and (flags == _lib.FLAG_TC_GEMM)
     work = {  # algorithmic work per launch of a B-realisation batch
-        "screen_gemm": ("fp32", 2.0 * N * N * K * B, "TFLOP/s"),
+        # tensor cores: three FP16 MMAs (hi.hi, hi.lo, lo.hi) per FP32 product, against the dense 16-bit peak
+        "screen_gemm": ("tensor", 3 * 2.0 * N * N * K * B, "TFLOP/s") if tc else ("fp32", 2.0 * N * N * K * B, "TFLOP/s"),
         "col_pass": ("hbm", 16.0 * N * N * B, "GB/s"),
         # n+1 row launches move 8 (write) + 4 (phi) + (n-1)(16 + 4) + 8 (read) bytes per pixel
         "row_pass": ("hbm", (12.0 + 20.0 * (n - 1) + 8.0) / (n + 1) * N * N * B, "GB/s"),
@@ -278,6 +282,10 @@ def run_gb300(args, rank, world, local_rank):
     except (OSError, KeyError, ValueError):
         peaks["hbm"] = (6800.0, "fallback")
     peaks["fp32"] = (fma_peak_tflops(dev), "measured (FMA probe)")
+    try:
+        peaks["tensor"] = (float(mp["bf16_tflops"]), "measured (cuBLAS bf16 burst; FP16 dense rate is the same)")
+    except (NameError, KeyError, ValueError):
+        peaks["tensor"] = (1900.0, "fallback")
     kernels = {}
     for kname, st in prof.items():
         if st["launches"] == 0:
@@ -314,7 +322,7 @@ def run_gb300(args, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 (complex64 field, FP64 phase arguments and accumulators)",
             "data": "synthetic (seeded spectra, reference formulas)",
-            "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B,
+            "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B, "gemm": args.gemm,
                        "l2": "inputs larger than L2 (field batch 8.6 GB per step)", "gemm_k": K,
                        "low_annuli": plan.info["low_annuli"], "cheb_terms": plan.info["cheb_terms"]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -343,6 +351,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-realisations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gemm", choices=["auto", "tc", "simt"], default="auto",
+                    help="screen GEMM on tensor cores (tc) or FP32 SIMT cores")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
