@@ -265,7 +265,7 @@ def run_gb300(args, rank, world, local_rank):
     # ---- roofline of the dominant kernel, measured in the timed region ----
     N, n = w["N"], w["count"]
     K = plan.info["gemm_k"]
-    tc = plan.info.get("gemm_k", 0) and (flags == _lib.FLAG_TC_GEMM)
+    tc = flags != _lib.FLAG_SIMT_GEMM and w["N"] >= 256
     work = {  # algorithmic work per launch of a B-realisation batch
         # tensor cores: three FP16 MMAs (hi.hi, hi.lo, lo.hi) per FP32 product, against the dense 16-bit peak
         "screen_gemm": ("tensor", 3 * 2.0 * N * N * K * B, "TFLOP/s") if tc else ("fp32", 2.0 * N * N * K * B, "TFLOP/s"),
@@ -352,7 +352,7 @@ def main():
     ap.add_argument("--cpu-realisations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gemm", choices=["auto", "tc", "simt"], default="auto",
-                    help="screen GEMM on tensor cores (tc) or FP32 SIMT cores")
+                    help="screen GEMM on tensor cores (tc, the default at 2048^2) or FP32 SIMT cores")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

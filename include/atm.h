@@ -48,8 +48,8 @@ extern "C" {
 #define ATM_MAX_PUPILS 8
 
 /* AtmChannelDesc.flags */
-#define ATM_FLAG_SIMT_GEMM 1     /* screen GEMM on FP32 SIMT cores (no tensor cores) */
-#define ATM_FLAG_TC_GEMM 2       /* screen GEMM on tcgen05 tensor cores (N >= 256) */
+#define ATM_FLAG_SIMT_GEMM 1     /* screen GEMM on FP32 SIMT cores (default below N = 256) */
+#define ATM_FLAG_TC_GEMM 2       /* screen GEMM on tcgen05 tensor cores (the default for N >= 256) */
 
 /* per-realisation doubles in measures_out (slot index) */
 #define ATM_OUT_ETA_TOTAL 0      /* measures.eta(pupil=False)      measures.py:7-8   */

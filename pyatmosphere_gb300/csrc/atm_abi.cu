@@ -412,7 +412,8 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
     delete pl;
     return fail(ATM_ERR_UNSUPPORTED, "too many low-frequency annuli (%d) for the prep kernel", pl->P_L);
   }
-  pl->use_tc = pl->n > 0 && pl->N >= 256 && (d->flags & ATM_FLAG_TC_GEMM) && !(d->flags & ATM_FLAG_SIMT_GEMM);
+  // tensor cores by default for N >= 256 (the GEMM tile is 128 x 256); ATM_FLAG_SIMT_GEMM opts out
+  pl->use_tc = pl->n > 0 && pl->N >= 256 && !(d->flags & ATM_FLAG_SIMT_GEMM);
   if (pl->use_tc) {
     pl->kc0 = 2 * pl->P_H;
     const int kraw = pl->kc0 + (pl->P_L > 0 ? pl->D - 1 : 0);
