@@ -50,6 +50,15 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory");
 }
 
+// exp(-2 pi i t) for a phase t in turns: exact reduction to [-1/2, 1/2] turn,
+// then the SFU sine / cosine (absolute error <= 2^-21.4 on [-pi, pi])
+__device__ __forceinline__ float2 phasor_turns(float t) {
+  const float r = t - rintf(t);
+  float s, c;
+  __sincosf(r * 6.28318530717958647692f, &s, &c);
+  return make_float2(c, -s);
+}
+
 // rows per CTA of the row pass: about 256 threads per CTA
 template <int N>
 struct RowRows {
@@ -171,9 +180,7 @@ row_pass_kernel(RowArgs a) {
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
       const int x = t + m * T;
-      float s, c;
-      sincospif(2.f * ph[x], &s, &c);  // phi_G is stored in turns
-      v[m] = cmul(v[m], cmul(cmul(py, px[x]), make_float2(c, -s)));
+      v[m] = cmul(v[m], cmul(cmul(py, px[x]), phasor_turns(ph[x])));  // phi_G is stored in turns
     }
   } else if (a.loss != 1.0f) {
 #pragma unroll
@@ -272,9 +279,7 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
         const int x = t + m * T;
-        float sn, cs;
-        sincospif(2.f * ph[m], &sn, &cs);
-        v[m] = cmul(v[m], cmul(cmul(py, px[x]), make_float2(cs, -sn)));
+        v[m] = cmul(v[m], cmul(cmul(py, px[x]), phasor_turns(ph[m])));
       }
     } else if (a.loss != 1.0f) {
 #pragma unroll
@@ -425,7 +430,8 @@ struct ColPipe {
   static constexpr size_t EXCH = (size_t)C * ColStride<N, C>::value * sizeof(float2);
   static constexpr size_t STAGE = ((TILE > EXCH ? TILE : EXCH) + 127) / 128 * 128;
   static constexpr size_t TW = (size_t)Padded<N>::value * sizeof(float2);
-  static constexpr size_t SMEM = 2 * STAGE + TW;
+  static constexpr size_t HY = (size_t)N * sizeof(float2);
+  static constexpr size_t SMEM = 2 * STAGE + TW + HY;
 };
 
 template <int N, int C>
@@ -441,6 +447,9 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
   auto buf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * ColPipe<N, C>::STAGE); };
   float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * ColPipe<N, C>::STAGE);
   load_twiddles<N>(tws, a.tw);
+  float2* hys = reinterpret_cast<float2*>(smem_raw + 2 * ColPipe<N, C>::STAGE + ColPipe<N, C>::TW);
+  if (!a.inv_only)
+    for (int i = threadIdx.x; i < N; i += blockDim.x) hys[i] = a.hy[i];
   auto prefetch = [&](int item, int s) {
     const int r = item / NCT, x0 = (item - r * NCT) * C;
     const float2* src = a.field + (size_t)r * N * N + x0;
@@ -470,7 +479,7 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
       fft_dev<N, -1, 0, 1>(v, sm, t, tws);
       const float2 hx = a.hx[x];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(a.hy[t + m * T], hx));
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(hys[t + m * T], hx));
     }
     fft_dev<N, 1, 0, 1>(v, sm, t, tws);
     float2* f = a.field + (size_t)r * N * N + x;
@@ -943,11 +952,7 @@ __global__ void compose_screen_kernel(const double* Gy, const double* Hx, const 
   const size_t o = ((size_t)r * N + y) * N + x;
   if (phi_out)
     phi_out[o] = (float)(Gy[(size_t)r * N + y] + Hx[(size_t)r * N + x] + 6.283185307179586477 * (double)phiG[o]);
-  if (phasor_out) {
-    float s, c;
-    sincospif(2.f * phiG[o], &s, &c);
-    phasor_out[o] = cmul(cmul(Py[(size_t)r * N + y], Px[(size_t)r * N + x]), make_float2(c, -s));
-  }
+  if (phasor_out) phasor_out[o] = cmul(cmul(Py[(size_t)r * N + y], Px[(size_t)r * N + x]), phasor_turns(phiG[o]));
 }
 
 cudaError_t launch_compose_screen(int B, int N, const double* Gy, const double* Hx, const float* phiG,

@@ -63,3 +63,21 @@ def test_tc_channel_config2_matches_oracle():
     res, u = o.simulate(spec, rho, theta, value, return_field=True)
     assert o.rel_l2(field.cpu().numpy()[0], u) < 1e-4
     assert meas[0, 8] == pytest.approx(res[0]["eta_0"], rel=1e-5)
+
+
+def test_simt_gemm_path_still_matches_oracle():
+    """The FP32 SIMT screen GEMM (ATM_FLAG_SIMT_GEMM) stays covered."""
+    import torch
+    from oracle import atm_oracle as o
+    from pyatmosphere_gb300.engine import EnginePlan, _lib
+    N, P, d = 512, 1024, 1.0 / 512
+    spec = o.ChannelSpec(N=N, delta=d, points=P, Cn2=1e-15, count=2, length=10e3)
+    base = o.logpolar_base(P, spec.f_min, spec.f_max)
+    plan = EnginePlan(N, d, spec.wvl, spec.w0, spec.F0, o.screen_positions(spec.length, 2), spec.length,
+                      f_base=base, batch=1, flags=_lib.FLAG_SIMT_GEMM)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    rho, theta, value = o.draw_spectra(3, range(1), 2, base, psd)
+    ph = torch.empty((1, N, N), dtype=torch.complex64, device="cuda")
+    plan.screen(*[torch.from_numpy(a).cuda() for a in (rho, theta, value)], 0, phasor_out=ph)
+    ref = o.ss_screen(rho[0, 0], theta[0, 0], value[0, 0], N, d)
+    assert o.rel_l2(ph.cpu().numpy()[0], np.exp(-1j * ref)) < 1e-5
