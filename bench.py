@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -37,6 +38,13 @@ WORKLOAD = dict(N=2048, delta=1.5e-3, wvl=808e-9, w0=0.12, F0=float("inf"), leng
                 pupil_radius=0.2)
 WORKLOAD_NAME = ("config-2 advanced channel: 2048^2 grid, delta 1.5 mm, 808 nm, w0 0.12 m, 50 km, "
                  "5 SS screens x 1024 annuli, MVK Cn2 5e-16, pupil 0.2 m")
+
+
+# DRAM bytes (read + write) per launch and realisation, from one ncu capture
+# of a 16-realisation run of this workload (profiles/traffic_2048_b16.md),
+# averaged over the launches of one run; traffic grows with the realisations.
+TRAFFIC_PER_REALISATION = {"row_pass": 66.98e6, "col_pass": 63.49e6, "screen_gemm": 25.98e6,
+                           "screen_table": 8.24e6}
 
 
 def positions(length, count):
@@ -163,6 +171,91 @@ def run_reference(args, rank, world):
 # ---------------------------------------------------------------------------
 # GB300 engine
 # ---------------------------------------------------------------------------
+def surrogate_leg(args, dev):
+    """PDT surrogate: queries/s of the shipped network (device-resident and
+    end to end from host parameters), and its bin-edge KS against fresh
+    simulations of held-out points (4096 realisations each at 512^2)."""
+    import torch
+    from pyatmosphere_gb300.surrogate.experiment import load
+    from pyatmosphere_gb300.surrogate.model import (N_HIST, Box, PointSimulator, SimConfig, features, ks_binned,
+                                                    targets_from_measures)
+    s = load(os.path.join(ROOT, "pyatmosphere_gb300", "surrogate", "pdt_mlp.npz"), device=dev)
+    box = Box()
+    rng = np.random.default_rng(args.seed + 7)
+    n_q = 100_000
+    params = box.sample(n_q, rng)
+    X_host = torch.from_numpy(features(params, box)).pin_memory()
+    X = X_host.to(dev)
+    for _ in range(3):
+        s.predict(X)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        s.predict(X)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    q_dev = n_q * reps / (e0.elapsed_time(e1) * 1e-3)
+    # end to end: host parameter vectors in, host histograms out
+    out_host = torch.empty((n_q, N_HIST), dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        probs, _, _ = s.predict(X_host.to(dev, non_blocking=True))
+        out_host.copy_(probs, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    q_e2e = n_q * reps / (e0.elapsed_time(e1) * 1e-3)
+    # quality on held-out points against fresh simulations
+    n_pts, n_real = args.surrogate_points, 4096
+    pts = box.sample(n_pts, np.random.default_rng(args.seed + 8))
+    pts["l0"] = np.round(pts["l0"] * 1e3) / 1e3
+    probs = s.predict(torch.from_numpy(features(pts, box)).to(dev))[0].cpu().numpy()
+    sim = PointSimulator(SimConfig(N=512, realisations=2048, seed=args.seed + 9), device=dev)
+    ks, t_sim = [], 0.0
+    for i in range(n_pts):
+        q = {k: v[i] for k, v in pts.items()}
+        sim.run(q, 0)  # plan for this point's spectral grid, outside the timing
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        etas = [targets_from_measures(sim.run(q, 1 + 2 * i + c), q["aperture"])[1] for c in range(2)]
+        torch.cuda.synchronize()
+        t_sim += time.perf_counter() - t0
+        ks.append(ks_binned(probs[i], np.concatenate(etas)))
+    sim.plan.close()
+    ks = np.array(ks)
+    return {"queries_per_s": q_dev, "e2e_queries_per_s": q_e2e, "query_batch": n_q,
+            "h2d_bytes_per_batch": int(X_host.numel() * 4), "d2h_bytes_per_batch": int(out_host.numel() * 4),
+            "heldout_points": n_pts, "realisations_per_point": n_real,
+            "ks_binned_median": float(np.median(ks)), "ks_binned_max": float(ks.max()),
+            "frac_ks_le_0.02": float((ks <= 0.02).mean()),
+            "ks_noise_floor": 0.87 / math.sqrt(n_real),
+            "simulated_pdt_per_s": n_pts / t_sim,
+            "speedup_vs_simulation": q_dev / (n_pts / t_sim),
+            "weights": "pyatmosphere_gb300/surrogate/pdt_mlp.npz (8000 points x 256 realisations, 512^2)"}
+
+
+def mixed_leg(args, dev):
+    """Uneven workload: channels of mixed grid size (512..4096), screen count
+    (3..20) and geometry, 64 realisations and one 64-bin PDT each, through
+    one re-targeted plan per grid size."""
+    from pyatmosphere_gb300.engine.uneven import run_uneven, sample_mixed
+    chans = sample_mixed(args.mixed_channels, np.random.default_rng(args.seed + 11))
+    run_uneven(chans[:2], realisations=64, seed=args.seed, device=dev)  # first-use costs outside the timing
+    res = run_uneven(chans, realisations=64, seed=args.seed, device=dev, autotune=bool(args.autotune))
+    pix = sum(c.N * c.N * c.n_screens for c in chans) * 64
+    return {"channels": len(chans), "realisations_per_channel": 64, "seconds": res.seconds,
+            "channels_per_s": res.channels_per_s, "realisations_per_s": res.realisations_per_s,
+            "screen_pixel_steps_per_s": pix / res.seconds,
+            "by_N": {str(k): {"channels": v["channels"], "max_screens": v["max_screens"],
+                              "seconds": v["seconds"]} for k, v in sorted(res.groups.items())},
+            "distribution": "N in {512,1024,2048,4096}, N delta = 3 m, n ~ U{3..20}, L log-U[1,100] km, "
+                            "Cn2 log-U[1e-16,1e-14], w0 U[0.02,0.2], wvl in {808,1550} nm, F0 in {inf, L}; "
+                            "l0 6 mm, L0 1 km, pupil 0.1 m; plan creation inside the timing"}
+
+
 def run_gb300(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -180,6 +273,7 @@ def run_gb300(args, rank, world, local_rank):
     flags = {"tc": _lib.FLAG_TC_GEMM, "simt": _lib.FLAG_SIMT_GEMM, "auto": 0}[args.gemm]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
                       pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags)
+    tuned = plan.autotune(repeats=2) if args.autotune else None
     n_steps = args.warmup + args.steps
     # distinct seeded inputs per step (weak scaling: each rank its own realisations)
     host = []
@@ -305,8 +399,22 @@ def run_gb300(args, rank, world, local_rank):
 
     def roof(k):
         e = kernels[k]
+        t = TRAFFIC_PER_REALISATION.get(k)
         return {"kernel": k, "bound": e["bound"], "achieved": e["achieved"], "peak": e["peak"], "unit": e["unit"],
-                "frac": e["frac"], "traffic": None, "peak_source": e["peak_source"]}
+                "frac": e["frac"], "traffic": t * B if t else None, "traffic_unit": "bytes per launch",
+                "peak_source": e["peak_source"]}
+
+    info = dict(plan.info)
+    sur = mixed = None
+    if rank == 0 and (args.surrogate_points > 0 or args.mixed_channels > 0):
+        plan.close()
+        plan = None
+        del devin, out, scratch
+        torch.cuda.empty_cache()
+        if args.surrogate_points > 0:
+            sur = surrogate_leg(args, dev)
+        if args.mixed_channels > 0:
+            mixed = mixed_leg(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -324,7 +432,7 @@ def run_gb300(args, rank, world, local_rank):
             "data": "synthetic (seeded spectra, reference formulas)",
             "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B, "gemm": args.gemm,
                        "l2": "inputs larger than L2 (field batch 8.6 GB per step)", "gemm_k": K,
-                       "low_annuli": plan.info["low_annuli"], "cheb_terms": plan.info["cheb_terms"]},
+                       "low_annuli": info["low_annuli"], "cheb_terms": info["cheb_terms"], "autotune": tuned},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "plain": {"value": plain, "unit": UNIT, "realisations": args.plain,
                       "batched_over_plain": (value / world / plain) if plain else None},
@@ -334,9 +442,12 @@ def run_gb300(args, rank, world, local_rank):
             "kernels": kernels,
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
+            "surrogate": sur,
+            "mixed": mixed,
         }
         print(json.dumps(line), flush=True)
-    plan.close()
+    if plan is not None:
+        plan.close()
     return 0
 
 
@@ -351,6 +462,11 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-realisations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", type=int, default=1, help="time the FFT-pass launch variants first (atm_autotune)")
+    ap.add_argument("--mixed-channels", type=int, default=16,
+                    help="channels of the mixed-size workload leg (0: skip)")
+    ap.add_argument("--surrogate-points", type=int, default=8,
+                    help="held-out points of the surrogate check (0: skip the surrogate leg)")
     ap.add_argument("--gemm", choices=["auto", "tc", "simt"], default="auto",
                     help="screen GEMM on tensor cores (tc, the default at 2048^2) or FP32 SIMT cores")
     args = ap.parse_args()

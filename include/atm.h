@@ -99,6 +99,10 @@ typedef struct AtmPlanInfo {
   int64_t workspace_bytes;    /* device memory held by the plan */
   int32_t launches_per_run;   /* kernel launches of one atm_run (without tracked/field extras) */
   int32_t row_parts;          /* row-pass CTAs per realisation */
+  int32_t col_tile;           /* columns per CTA of the column pass */
+  int32_t row_variant;        /* 0: persistent pipelined row pass, 1: one CTA per row block */
+  int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile */
+  int32_t tuned;              /* 1 after a successful atm_autotune */
 } AtmPlanInfo;
 
 /* ABI version of the loaded library (ATM_ABI_VERSION). */
@@ -169,11 +173,13 @@ int atm_measures(AtmPlan* plan, const void* field, int32_t batch, double* measur
 int atm_fft_screen(AtmPlan* plan, const float* normals, const float* amp, const void* sub_x, const void* sub_y,
                    const double* sub_mean, int32_t n_sub, int32_t batch, void* screen_out, void* stream);
 
-/* Re-targets a plan to another channel of the same grid, screen count,
- * spectral grid, pupil counts and batch (source, positions, length, losses,
- * shift and pupil radii may change) without reallocating; waits for the
- * device first.  Replaces building a new Channel for each parameter point
- * of a sweep (channels.py:17-29). */
+/* Re-targets a plan to another channel of the same grid, spectral grid,
+ * pupil counts and batch (source, positions, length, losses, shift and
+ * pupil radii may change; the screen count may be any 1..n_screens of the
+ * creating descriptor, and the spectra of later runs are then laid out
+ * [batch][new count][P]) without reallocating; waits for the device first.
+ * Replaces building a new Channel for each parameter point of a sweep
+ * (channels.py:17-29). */
 int atm_plan_update(AtmPlan* plan, const AtmChannelDesc* desc);
 
 /* Seeded spectra on the device: rho, theta [batch][n][P] float32 and value
@@ -217,6 +223,16 @@ int atm_mlp_infer(AtmMlp* mlp, const float* x, int32_t batch, const float* lo, c
 int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32_t N, int32_t K, float scale,
                      float* out, void* stream);
 
+/* Times the launch variants of the FFT passes on this plan's own workspace
+ * (`batch` realisations, `repeats` timed launches each after one warm-up)
+ * and keeps the fastest: row-pass variant, column tile (2..16 columns,
+ * at most 512 threads per CTA) and column-pass variant.  Overwrites the
+ * plan's field / screen workspace (zeroes) and blocks until the timing
+ * launches finish, so it is called outside CUDA-graph capture, before the
+ * runs it tunes.  The reference has no tuner: cupy picks cuFFT plans inside
+ * the FFT calls of utils.py:42-50 (the boundary item atm_autotune). */
+int atm_autotune(AtmPlan* plan, int32_t batch, int32_t repeats, void* stream);
+
 /* Launch categories reported by atm_profile_end. */
 #define ATM_KIND_SCREEN_PREP 0
 #define ATM_KIND_SCREEN_TABLE 1
@@ -225,7 +241,8 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
 #define ATM_KIND_COL_PASS 4
 #define ATM_KIND_FINALIZE 5
 #define ATM_KIND_TRACKED 6
-#define ATM_KIND_COUNT 7
+#define ATM_KIND_SCREEN_EVAL 7
+#define ATM_KIND_COUNT 8
 
 /* Starts recording a CUDA event pair around each kernel launch of this plan
  * (at most max_launches launches), on the stream the kernel runs on.  No

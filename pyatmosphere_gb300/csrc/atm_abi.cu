@@ -100,6 +100,7 @@ int dev_alloc(DevBuf& b, size_t bytes, std::vector<DevBuf*>& all) {
 
 template <class T>
 int upload(DevBuf& b, const std::vector<T>& v) {
+  if (v.size() * sizeof(T) > b.bytes) return fail(ATM_ERR_INVALID, "table larger than its device buffer");
   ATM_CUDA(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
   return ATM_OK;
 }
@@ -133,8 +134,10 @@ int check_device(const AtmPlan* pl);
 struct AtmPlan {
   int device = 0;
   int N = 0, n = 0, P = 0, B = 0, n_pupils = 0, n_tracked = 0;
+  int n_alloc = 0;  // screen count the workspace was sized for (atm_plan_update may lower n)
   double delta = 0, wvl = 0, w0 = 0, F0 = 0, length = 0, losses_db = 0, kw = 0, sx = 0, sy = 0;
   int path_output_loss = 0, source_kind = 0, col_tile = 0;
+  int row_variant = 0, col_variant = 0, tuned = 0;  // launch choices (atm_autotune)
   int P_L = 0, D = 2, P_H = 0, KH = 0, KC = 0;
   int rows = 1, n_parts = 0, n_meas = 0, n_out = 0;
   std::vector<double> positions, dz;      // dz[0..n]
@@ -155,6 +158,7 @@ struct AtmPlan {
   bool use_tc = false;  // screen GEMM on tensor cores
   int Kp = 0, kc0 = 0;  // tensor-core layout
   DevBuf ta_hi, ta_lo, tb_hi, tb_lo;
+  DevBuf s_int, s_edge;  // chunk sums of the low-frequency block
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
     int64_t s = 0;
@@ -380,6 +384,7 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   cudaGetDevice(&pl->device);
   pl->N = d->resolution;
   pl->n = d->n_screens;
+  pl->n_alloc = d->n_screens;
   pl->P = d->n_screens > 0 ? d->points : 0;
   pl->B = d->batch;
   pl->delta = d->delta;
@@ -408,10 +413,6 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   pl->KH = ((2 * pl->P_H + 7) / 8) * 8;
   pl->KC = pl->P_L > 0 ? ((pl->D - 1 + 7) / 8) * 8 : 0;
   if (pl->n > 0 && pl->KH + pl->KC == 0) pl->KH = 8;  // keep the GEMM well-formed
-  if (pl->n > 0 && atm::prep_smem_bytes(pl->P_L, pl->D) > 220 * 1024) {
-    delete pl;
-    return fail(ATM_ERR_UNSUPPORTED, "too many low-frequency annuli (%d) for the prep kernel", pl->P_L);
-  }
   // tensor cores by default for N >= 256 (the GEMM tile is 128 x 256); ATM_FLAG_SIMT_GEMM opts out
   pl->use_tc = pl->n > 0 && pl->N >= 256 && !(d->flags & ATM_FLAG_SIMT_GEMM);
   if (pl->use_tc) {
@@ -463,7 +464,9 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
         (rc = dev_alloc(pl->Ach, (size_t)pl->KC * N * sizeof(float), v)) ||
         (rc = dev_alloc(pl->ht, B * (pl->KH / 2) * sizeof(atm::HighTerm), v)) ||
         (rc = dev_alloc(pl->Py, B * N * sizeof(float2), v)) || (rc = dev_alloc(pl->Px, B * N * sizeof(float2), v)) ||
-        (rc = dev_alloc(pl->Gy, B * N * sizeof(double), v)) || (rc = dev_alloc(pl->Hx, B * N * sizeof(double), v))) {
+        (rc = dev_alloc(pl->Gy, B * N * sizeof(double), v)) || (rc = dev_alloc(pl->Hx, B * N * sizeof(double), v)) ||
+        (rc = dev_alloc(pl->s_int, B * atm::prep_chunks(pl->P_L) * (pl->D - 1) * (pl->D - 1) * sizeof(float2), v)) ||
+        (rc = dev_alloc(pl->s_edge, B * atm::prep_chunks(pl->P_L) * (2 * pl->D - 1) * sizeof(double2), v))) {
       delete pl;
       return rc;
     }
@@ -502,15 +505,18 @@ int atm_plan_update(AtmPlan* pl, const AtmChannelDesc* d) {
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
   if (int rc = validate(d)) return rc;
   if (int rc = check_device(pl)) return rc;
-  if (d->resolution != pl->N || d->delta != pl->delta || d->n_screens != pl->n || d->n_pupils != pl->n_pupils ||
+  if (d->resolution != pl->N || d->delta != pl->delta || d->n_pupils != pl->n_pupils ||
       d->n_tracked != pl->n_tracked || d->batch > pl->B || d->cheb_cut != pl->cheb_cut)
-    return fail(ATM_ERR_INVALID, "atm_plan_update keeps grid, screen count, pupil counts, batch and cheb_cut");
+    return fail(ATM_ERR_INVALID, "atm_plan_update keeps grid, pupil counts, batch and cheb_cut");
+  if (d->n_screens > pl->n_alloc || (pl->n_alloc > 0) != (d->n_screens > 0))
+    return fail(ATM_ERR_INVALID, "atm_plan_update takes 1..%d screens (the creating descriptor's count)", pl->n_alloc);
   if (pl->n > 0) {
     if (d->points != pl->P) return fail(ATM_ERR_INVALID, "atm_plan_update keeps the spectral grid");
     for (int p = 0; p < pl->P; ++p)
       if (d->f_base[p] != pl->f_base[p]) return fail(ATM_ERR_INVALID, "atm_plan_update keeps the spectral grid");
   }
   ATM_CUDA(cudaDeviceSynchronize());  // tables may still be read by enqueued work
+  pl->n = d->n_screens;
   set_geometry(pl, d);
   return plan_tables(pl, d);
 }
@@ -530,11 +536,16 @@ int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
   info->gemm_k = pl->use_tc ? pl->Kp : pl->KH + pl->KC;
   info->workspace_bytes = pl->bytes();
   int launches = 0;
-  for (int i = 0; i < pl->n; ++i) launches += 4 + (pl->dz[i + 1] > 0 ? 1 : 0);
+  // per screen: terms, eval, table, GEMM, row pass (+ column pass)
+  for (int i = 0; i < pl->n; ++i) launches += 5 + (pl->dz[i + 1] > 0 ? 1 : 0);
   launches += (pl->n == 0 || pl->dz[pl->n] > 0) ? 1 : 0;
   launches += 1;  // finalize
   info->launches_per_run = launches;
   info->row_parts = pl->n_parts;
+  info->col_tile = pl->col_tile;
+  info->row_variant = pl->row_variant;
+  info->col_variant = pl->col_variant;
+  info->tuned = pl->tuned;
   return ATM_OK;
 }
 
@@ -578,6 +589,8 @@ atm::ScreenArgs screen_args(AtmPlan* pl, const float* rho, const float* theta, c
   s.KH = pl->KH;
   s.KC = pl->KC;
   s.hterms = (atm::HighTerm*)pl->ht.p;
+  s.s_int = (float2*)pl->s_int.p;
+  s.s_edge = (double2*)pl->s_edge.p;
   s.Py = (float2*)pl->Py.p;
   s.Px = (float2*)pl->Px.p;
   s.At = (float*)pl->At.p;
@@ -598,7 +611,11 @@ atm::ScreenArgs screen_args(AtmPlan* pl, const float* rho, const float* theta, c
 int run_screen(AtmPlan* pl, const atm::ScreenArgs& s, int B, cudaStream_t st) {
   {
     Prof p(pl, ATM_KIND_SCREEN_PREP, st);
-    ATM_CUDA(atm::launch_screen_prep(B, s, st));
+    ATM_CUDA(atm::launch_screen_terms(B, s, st));
+  }
+  {
+    Prof p(pl, ATM_KIND_SCREEN_EVAL, st);
+    ATM_CUDA(atm::launch_screen_eval(B, s, st));
   }
   if (pl->use_tc) {
     {
@@ -647,6 +664,7 @@ atm::RowArgs row_args(AtmPlan* pl, float* mean_intensity, void* field_out) {
   ra.delta = (float)pl->delta;
   ra.delta64 = pl->delta;
   ra.out = (float2*)field_out;
+  ra.variant = pl->row_variant;
   return ra;
 }
 
@@ -706,6 +724,7 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
   atm::ColArgs ca{};
   ca.field = (float2*)pl->field.p;
   ca.tw = (const float2*)pl->tw.p;
+  ca.variant = pl->col_variant;
 
   bool measured = false;
   for (int i = 0; i < n; ++i) {
@@ -782,6 +801,89 @@ int atm_screen(AtmPlan* pl, const float* rho, const float* theta, const void* va
   return ATM_OK;
 }
 
+int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
+  if (repeats < 1 || repeats > 100) return fail(ATM_ERR_INVALID, "repeats %d out of range [1, 100]", repeats);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = pl->N;
+  const size_t plane = (size_t)N * N;
+  // the candidates read the field, the screen phase and the phasors: zeroes
+  ATM_CUDA(cudaMemsetAsync(pl->field.p, 0, (size_t)batch * plane * sizeof(float2), st));
+  if (pl->n > 0) {
+    ATM_CUDA(cudaMemsetAsync(pl->phi.p, 0, (size_t)batch * plane * sizeof(float), st));
+    ATM_CUDA(cudaMemsetAsync(pl->Py.p, 0, (size_t)batch * N * sizeof(float2), st));
+    ATM_CUDA(cudaMemsetAsync(pl->Px.p, 0, (size_t)batch * N * sizeof(float2), st));
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return fail(ATM_ERR_CUDA, "cudaEventCreate failed");
+  }
+  // mean device ms of `repeats` launches after one warm-up; < 0 if the candidate does not launch
+  auto time_it = [&](auto&& launch) -> double {
+    if (launch() != cudaSuccess) {
+      cudaGetLastError();
+      return -1.0;
+    }
+    cudaEventRecord(e0, st);
+    for (int k = 0; k < repeats; ++k)
+      if (launch() != cudaSuccess) {
+        cudaGetLastError();
+        cudaEventSynchronize(e0);
+        return -1.0;
+      }
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.0;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return (double)ms / repeats;
+  };
+  // row pass: a middle screen step (inverse FFT, phasor, forward FFT, store)
+  atm::RowArgs ra = row_args(pl, nullptr, nullptr);
+  ra.flags = atm::ROW_INV | atm::ROW_FWD | atm::ROW_STORE | (pl->n > 0 ? atm::ROW_PHASOR : 0);
+  ra.loss = 1.f;
+  double best_row = -1.0;
+  int row_variant = 0;
+  for (int v = 0; v < 2; ++v) {
+    ra.variant = v;
+    const double ms = time_it([&] { return atm::launch_row_pass(N, batch, ra, st); });
+    if (ms >= 0 && (best_row < 0 || ms < best_row)) {
+      best_row = ms;
+      row_variant = v;
+    }
+  }
+  // column pass: every tile of at most 512 threads, both variants
+  atm::ColArgs ca{};
+  ca.field = (float2*)pl->field.p;
+  ca.tw = (const float2*)pl->tw.p;
+  ca.hy = (const float2*)pl->hy.p;
+  ca.hx = (const float2*)pl->hx.p;
+  double best_col = -1.0;
+  int col_tile = pl->col_tile, col_variant = 0;
+  for (int C : {2, 4, 8, 16}) {
+    if (C * (N / 16) > 512 || C > N) continue;
+    for (int v = 0; v < 2; ++v) {
+      ca.variant = v;
+      const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
+      if (ms >= 0 && (best_col < 0 || ms < best_col)) {
+        best_col = ms;
+        col_tile = C;
+        col_variant = v;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best_row < 0 || best_col < 0) return fail(ATM_ERR_CUDA, "autotune: no candidate launched");
+  pl->row_variant = row_variant;
+  pl->col_tile = col_tile;
+  pl->col_variant = col_variant;
+  pl->tuned = 1;
+  return ATM_OK;
+}
+
 int atm_vacuum(AtmPlan* pl, void* field, int32_t batch, double dz, void* stream) {
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
   if (int rc = check_device(pl)) return rc;
@@ -811,6 +913,7 @@ int atm_vacuum(AtmPlan* pl, void* field, int32_t batch, double dz, void* stream)
   atm::ColArgs ca{};
   ca.field = (float2*)field;
   ca.tw = (const float2*)pl->tw.p;
+  ca.variant = pl->col_variant;
   ca.hy = (const float2*)pl->vac_h.p;
   ca.hx = (const float2*)pl->vac_h.p + N;
   ATM_CUDA(atm::launch_col_pass(N, batch, pl->col_tile, ca, st));
@@ -853,6 +956,7 @@ int atm_fft_screen(AtmPlan* pl, const float* normals, const float* amp, const vo
   atm::ColArgs ca{};
   ca.field = (float2*)pl->field.p;
   ca.tw = (const float2*)pl->tw.p;
+  ca.variant = pl->col_variant;
   ca.inv_only = 1;
   {
     Prof p(pl, ATM_KIND_COL_PASS, st);

@@ -50,6 +50,7 @@ struct RowArgs {
   int flags;
   float delta;
   double delta64;
+  int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per row block
 };
 
 struct ColArgs {
@@ -58,6 +59,7 @@ struct ColArgs {
   const float2* hy;         // [N] transfer function along y incl. exp(i k dz) / N^2
   const float2* hx;         // [N] transfer function along x
   int inv_only;             // 1: inverse column FFT only (no forward FFT, no H)
+  int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per column tile
 };
 
 // FFT screen (phase_screens.py:42-67) without shifts: screen[y][x] =
@@ -107,6 +109,8 @@ struct ScreenArgs {
   __half* tb_lo;
   int Kp;                   // padded K of the tensor-core layout
   int kc0;                  // first Chebyshev column (2 P_H)
+  float2* s_int;            // [B][chunks][(D-1)^2] FP32 chunk sums of the Chebyshev interior
+  double2* s_edge;          // [B][chunks][2D-1] FP64 chunk sums of its edge row / column
 };
 
 // GEMM: phi[s][y][x] = sum_k At[s][k][y] B[s][k][x], k < KH from At, then the
@@ -138,7 +142,8 @@ struct TrackedArgs {
 // kernel launchers (atm_kernels.cu); return cudaGetLastError()
 cudaError_t launch_row_pass(int N, int B, const RowArgs& a, cudaStream_t st);
 cudaError_t launch_col_pass(int N, int B, int col_tile, const ColArgs& a, cudaStream_t st);
-cudaError_t launch_screen_prep(int B, const ScreenArgs& a, cudaStream_t st);
+cudaError_t launch_screen_terms(int B, const ScreenArgs& a, cudaStream_t st);
+cudaError_t launch_screen_eval(int B, const ScreenArgs& a, cudaStream_t st);
 cudaError_t launch_screen_table(int B, const ScreenArgs& a, cudaStream_t st);
 cudaError_t launch_screen_gemm(int B, const GemmArgs& a, cudaStream_t st);
 cudaError_t launch_compose_screen(int B, int N, const double* Gy, const double* Hx, const float* phiG,
@@ -154,7 +159,7 @@ cudaError_t launch_draw_spectra(uint64_t seed, uint64_t first, int n, int P, con
 int row_pass_rows(int N);          // rows per CTA of the row pass
 int col_tile_default(int N);
 bool supported_n(int N);
-size_t prep_smem_bytes(int P_L, int D);
+__host__ __device__ int prep_chunks(int P_L);
 size_t tc_smem_bytes();
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                            const __half* b_lo, float* out, float scale, cudaStream_t st);

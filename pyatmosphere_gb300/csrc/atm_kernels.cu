@@ -1,9 +1,12 @@
 // GB300 (sm_103a) kernels of the split-step propagation engine.
 //
 // Per realisation and screen i the engine runs
-//   screen_prep   (FP64: low-frequency annuli -> Chebyshev block, 1-D phasors)
-//   screen_table  (high-frequency annuli -> A^T / B tables, exact phase wrap)
-//   screen_gemm   (FP32 SIMT GEMM: phi_G = A B, K ~ 600-900)
+//   screen_terms  (annuli -> high-frequency terms, chunk sums of the
+//                  low-frequency Chebyshev block; FP64 edge, FP32 interior)
+//   screen_eval   (Chebyshev block -> 1-D phasors and GEMM columns)
+//   screen_table  (high-frequency annuli -> GEMM tables, exact phase wrap)
+//   screen_gemm   (phi_G = A B, K ~ 600-900: tcgen05 tensor cores with an
+//                  FP16 hi/lo split in atm_tc.cu, or the FP32 SIMT GEMM here)
 //   row_pass      (inverse row FFT, exp(-i phi) multiply, forward row FFT)
 //   col_pass      (forward column FFT, H(fy,fx,dz), inverse column FFT)
 // and one last row_pass with the pupil / moment reductions, then finalize.
@@ -365,7 +368,7 @@ template <int N>
 static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
-  if (field_ok && phi_ok) return row_pipe_launch<N>(B, a, st);
+  if (field_ok && phi_ok && a.variant == 0) return row_pipe_launch<N>(B, a, st);
   return row_plain_launch<N>(B, a, st);
 }
 
@@ -523,7 +526,8 @@ static cudaError_t col_plain_launch(int B, const ColArgs& a, cudaStream_t st) {
 
 template <int N, int C>
 static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
-  if (C >= 2 && aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024) return col_pipe_launch<N, C>(B, a, st);
+  if (C >= 2 && aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024 && a.variant == 0)
+    return col_pipe_launch<N, C>(B, a, st);
   return col_plain_launch<N, C>(B, a, st);
 }
 
@@ -562,143 +566,187 @@ cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t 
 }
 
 // ---------------------------------------------------------------------------
-// screen preparation: one CTA per realisation.
-//   high annuli  -> HighTerm (fixed-point phase increments, amplitude)
-//   low annuli   -> M[e][d] = eps_e eps_d i^(e+d) sum_p v'_p J_e(a_y,p) J_d(a_x,p)
-//   outputs      Py[y] = exp(-i (Re M00 + sum_e Re M_e0 T_e(t_y)))
-//                Px[x] = exp(-i sum_d Re M_0d T_d(t_x))
-//                Bt[KH + e - 1][x] = sum_{d>=1} Re M_ed T_d(t_x)   (e >= 1)
-// The edge row / column of M (which carries the piston and the large tilts)
-// is accumulated in FP64, the interior in FP32 per chunk of 32 annuli.
+// screen preparation, spread over many CTAs per realisation.
+//
+// screen_terms_kernel, grid (n_low_chunks + n_high_blocks, B):
+//   a high block turns 256 high annuli into HighTerm records (fixed-point
+//   phase increments, amplitude); a low chunk takes 64 low annuli and writes
+//   its share of S[e][d] = sum_p v'_p J_e(a_y,p) J_d(a_x,p):
+//   the interior (e, d >= 1) summed in FP32, the edge row / column (which
+//   carries the piston and the large tilts) in FP64.
+// screen_eval_kernel, grid (ceil(N / 256), B):
+//   sums the chunks in chunk order in FP64, forms M[e][d] =
+//   eps_e eps_d i^(e+d) S[e][d] and writes, for its 256 indices j,
+//     Py[j] = exp(-i (Re M00 + sum_e Re M_e0 T_e(t_j)))
+//     Px[j] = exp(-i sum_d Re M_0d T_d(t_j))
+//     B[kc0 + e - 1][j] = sum_{d>=1} Re M_ed T_d(t_j)   (e >= 1)
 // ---------------------------------------------------------------------------
 constexpr int kPrepThreads = 256;
 constexpr int kPrepChunk = 64;
 constexpr int kMaxD = 64;
+constexpr int kEvalCols = 256;
 
 struct LowTerm {
   double vr, vi, ax, ay;
 };
 
-size_t prep_smem_bytes(int P_L, int D) {
-  size_t b = (size_t)P_L * sizeof(LowTerm);
-  b += 2 * (size_t)kPrepChunk * D * sizeof(double);     // Jy, Jx
-  b += 2 * (size_t)kPrepChunk * D * sizeof(float);      // Jyf, Jxf
-  b += (size_t)kPrepChunk * sizeof(float2);             // vf
-  b = (b + 15) & ~(size_t)15;
-  b += (size_t)D * D * sizeof(double2);                 // S / M
-  b += (size_t)D * D * sizeof(float);                   // Re M (float)
+__host__ __device__ int prep_chunks(int P_L) { return (P_L + kPrepChunk - 1) / kPrepChunk; }
+
+size_t prep_smem_bytes(int D) {
+  size_t b = (size_t)kPrepChunk * sizeof(LowTerm);
+  b += 2 * (size_t)kPrepChunk * D * sizeof(double);  // Jy, Jx
+  b += 2 * (size_t)kPrepChunk * D * sizeof(float);   // Jyf, Jxf
+  b += (size_t)kPrepChunk * sizeof(float2);          // vf
   return b;
 }
 
-__global__ void __launch_bounds__(kPrepThreads) screen_prep_kernel(ScreenArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int r = blockIdx.x, tid = threadIdx.x;
-  const int P = a.P, N = a.N, D = a.D, P_L = a.P_L;
-  LowTerm* low = reinterpret_cast<LowTerm*>(smem_raw);
-  double* Jy = reinterpret_cast<double*>(low + P_L);
-  double* Jx = Jy + kPrepChunk * D;
-  float* Jyf = reinterpret_cast<float*>(Jx + kPrepChunk * D);
-  float* Jxf = Jyf + kPrepChunk * D;
-  float2* vf = reinterpret_cast<float2*>(Jxf + kPrepChunk * D);
-  size_t off = (size_t)P_L * sizeof(LowTerm) + 2 * (size_t)kPrepChunk * D * sizeof(double) +
-               2 * (size_t)kPrepChunk * D * sizeof(float) + (size_t)kPrepChunk * sizeof(float2);
-  off = (off + 15) & ~(size_t)15;
-  double2* S = reinterpret_cast<double2*>(smem_raw + off);
-  float* Mf = reinterpret_cast<float*>(S + D * D);
+size_t eval_smem_bytes(int D) { return (size_t)D * D * (sizeof(double2) + sizeof(float)); }
 
+__global__ void __launch_bounds__(kPrepThreads) screen_terms_kernel(ScreenArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int r = blockIdx.y, tid = threadIdx.x;
+  const int P = a.P, N = a.N, D = a.D, P_L = a.P_L;
+  const int nlc = prep_chunks(P_L);
   const size_t in_off = ((size_t)r * a.n_screens + a.screen) * P;
   const float* rho = a.rho + in_off;
   const float* theta = a.theta + in_off;
   const float2* value = a.value + in_off;
   const double delta = a.delta;
-  const double xh = 0.5 * (N - 1) * delta;
-  const double xc = -0.5 * delta + a.sx, yc = -0.5 * delta + a.sy;
-  const double x0 = a.sx - 0.5 * N * delta, y0 = a.sy - 0.5 * N * delta;
-  const int nh = a.KH / 2;
-  HighTerm* ht = a.hterms + (size_t)r * nh;
   const double two_pi = 6.283185307179586476925;
 
-  for (int p = tid; p < P; p += blockDim.x) {
-    double s, c;
-    sincos((double)theta[p], &s, &c);
-    const double rh = (double)rho[p];
-    const double fx = rh * c, fy = rh * s;
-    const float2 v = value[p];
-    if (p >= P_L) {
-      HighTerm h;
+  if ((int)blockIdx.x >= nlc) {
+    // high annuli P_L + q, q in this block's range; q >= P_H pads with zeros
+    const int nh = a.KH / 2;
+    const int q = ((int)blockIdx.x - nlc) * kPrepThreads + tid;
+    if (q >= nh) return;
+    HighTerm h;
+    h.pad_ = make_float2(0.f, 0.f);
+    if (q < a.P_H) {
+      const int p = P_L + q;
+      double s, c;
+      sincos((double)theta[p], &s, &c);
+      const double rh = (double)rho[p];
+      const double fx = rh * c, fy = rh * s;
+      const double x0 = a.sx - 0.5 * N * delta, y0 = a.sy - 0.5 * N * delta;
       h.sx = turns_to_fixed(fx * delta);
       h.ox = turns_to_fixed(fx * x0);
       h.sy = turns_to_fixed(fy * delta);
       h.oy = turns_to_fixed(fy * y0);
-      h.v = v;
-      h.pad_ = make_float2(0.f, 0.f);
-      ht[p - P_L] = h;
+      h.v = value[p];
     } else {
-      double ps, pc;
-      sincospi(2.0 * (fx * xc + fy * yc), &ps, &pc);
-      LowTerm lt;
-      lt.vr = (double)v.x * pc - (double)v.y * ps;
-      lt.vi = (double)v.x * ps + (double)v.y * pc;
-      lt.ax = two_pi * fx * xh;
-      lt.ay = two_pi * fy * xh;
-      low[p] = lt;
+      h.sx = h.ox = h.sy = h.oy = 0;
+      h.v = make_float2(0.f, 0.f);
     }
+    a.hterms[(size_t)r * nh + q] = h;
+    return;
   }
-  for (int q = a.P_H + tid; q < nh; q += blockDim.x) {
-    HighTerm h;
-    h.sx = h.ox = h.sy = h.oy = 0;
-    h.v = make_float2(0.f, 0.f);
-    h.pad_ = make_float2(0.f, 0.f);
-    ht[q] = h;
-  }
-  for (int e = tid; e < D * D; e += blockDim.x) S[e] = make_double2(0.0, 0.0);
-  __syncthreads();
 
-  for (int p0 = 0; p0 < P_L; p0 += kPrepChunk) {
-    const int np = min(kPrepChunk, P_L - p0);
-    if (tid < np) {
-      bessel_j(low[p0 + tid].ay, D, Jy + tid * D);
-      for (int n = 0; n < D; ++n) Jyf[tid * D + n] = (float)Jy[tid * D + n];
-      vf[tid] = make_float2((float)low[p0 + tid].vr, (float)low[p0 + tid].vi);
-    } else if (tid >= kPrepChunk && tid - kPrepChunk < np) {
-      const int q = tid - kPrepChunk;
-      bessel_j(low[p0 + q].ax, D, Jx + q * D);
-      for (int n = 0; n < D; ++n) Jxf[q * D + n] = (float)Jx[q * D + n];
-    }
-    __syncthreads();
-    // interior (e, d >= 1) in FP32 per chunk; one FP64 add per chunk
-    const int Di = D - 1;
-    for (int idx = tid; idx < Di * Di; idx += blockDim.x) {
-      const int e = 1 + idx / Di, d = 1 + idx % Di;
-      float ar = 0.f, ai = 0.f;
-      for (int q = 0; q < np; ++q) {
-        const float w = Jyf[q * D + e] * Jxf[q * D + d];
-        ar = fmaf(vf[q].x, w, ar);
-        ai = fmaf(vf[q].y, w, ai);
-      }
-      S[e * D + d].x += (double)ar;
-      S[e * D + d].y += (double)ai;
-    }
-    // edge row e = 0 and column d = 0 (piston and tilts) in FP64, by
-    // dedicated threads so no warp carries both paths
-    for (int idx = tid; idx < 2 * D - 1; idx += blockDim.x) {
-      const int e = idx < D ? 0 : idx - D + 1, d = idx < D ? idx : 0;
-      double ar = 0.0, ai = 0.0;
-      for (int q = 0; q < np; ++q) {
-        const double w = Jy[q * D + e] * Jx[q * D + d];
-        ar = fma(low[p0 + q].vr, w, ar);
-        ai = fma(low[p0 + q].vi, w, ai);
-      }
-      S[e * D + d].x += ar;
-      S[e * D + d].y += ai;
-    }
-    __syncthreads();
+  const int c = blockIdx.x, p0 = c * kPrepChunk;
+  const int np = min(kPrepChunk, P_L - p0);
+  LowTerm* low = reinterpret_cast<LowTerm*>(smem_raw);
+  double* Jy = reinterpret_cast<double*>(low + kPrepChunk);
+  double* Jx = Jy + kPrepChunk * D;
+  float* Jyf = reinterpret_cast<float*>(Jx + kPrepChunk * D);
+  float* Jxf = Jyf + kPrepChunk * D;
+  float2* vf = reinterpret_cast<float2*>(Jxf + kPrepChunk * D);
+  if (tid < np) {
+    const int p = p0 + tid;
+    double s, cs;
+    sincos((double)theta[p], &s, &cs);
+    const double rh = (double)rho[p];
+    const double fx = rh * cs, fy = rh * s;
+    const float2 v = value[p];
+    const double xh = 0.5 * (N - 1) * delta;
+    const double xc = -0.5 * delta + a.sx, yc = -0.5 * delta + a.sy;
+    double ps, pc;
+    sincospi(2.0 * (fx * xc + fy * yc), &ps, &pc);
+    LowTerm lt;
+    lt.vr = (double)v.x * pc - (double)v.y * ps;
+    lt.vi = (double)v.x * ps + (double)v.y * pc;
+    lt.ax = two_pi * fx * xh;
+    lt.ay = two_pi * fy * xh;
+    low[tid] = lt;
   }
-  // M = eps_e eps_d i^(e+d) S
+  __syncthreads();
+  if (tid < np) {
+    bessel_j(low[tid].ay, D, Jy + tid * D);
+    for (int n = 0; n < D; ++n) Jyf[tid * D + n] = (float)Jy[tid * D + n];
+    vf[tid] = make_float2((float)low[tid].vr, (float)low[tid].vi);
+  } else if (tid >= kPrepChunk && tid - kPrepChunk < np) {
+    const int q = tid - kPrepChunk;
+    bessel_j(low[q].ax, D, Jx + q * D);
+    for (int n = 0; n < D; ++n) Jxf[q * D + n] = (float)Jx[q * D + n];
+  }
+  __syncthreads();
+  const int Di = D - 1;
+  float2* s_int = a.s_int + ((size_t)r * nlc + c) * Di * Di;
+  for (int idx = tid; idx < Di * Di; idx += blockDim.x) {
+    const int e = 1 + idx / Di, d = 1 + idx % Di;
+    float ar = 0.f, ai = 0.f;
+    for (int q = 0; q < np; ++q) {
+      const float w = Jyf[q * D + e] * Jxf[q * D + d];
+      ar = fmaf(vf[q].x, w, ar);
+      ai = fmaf(vf[q].y, w, ai);
+    }
+    s_int[idx] = make_float2(ar, ai);
+  }
+  // edge row e = 0 and column d = 0 in FP64, by dedicated threads
+  double2* s_edge = a.s_edge + ((size_t)r * nlc + c) * (2 * D - 1);
+  for (int idx = tid; idx < 2 * D - 1; idx += blockDim.x) {
+    const int e = idx < D ? 0 : idx - D + 1, d = idx < D ? idx : 0;
+    double ar = 0.0, ai = 0.0;
+    for (int q = 0; q < np; ++q) {
+      const double w = Jy[q * D + e] * Jx[q * D + d];
+      ar = fma(low[q].vr, w, ar);
+      ai = fma(low[q].vi, w, ai);
+    }
+    s_edge[idx] = make_double2(ar, ai);
+  }
+}
+
+// exp(-i g) for an FP64 phase g: reduction to [-1/2, 1/2] turn in FP64, FP32
+// sincospi of the rounded half-turns, first-order correction for the
+// rounding residual (second-order term below 1e-15)
+__device__ __forceinline__ float2 phasor_fp64(double g) {
+  double t = g * 0.15915494309189533577;  // turns
+  t -= rint(t);
+  const double h = 2.0 * t;               // half-turns in [-1, 1]
+  const float hf = (float)h;
+  const float dh = (float)(h - (double)hf) * 3.14159265358979323846f;
+  float s, c;
+  sincospif(hf, &s, &c);
+  return make_float2(fmaf(-dh, s, c), -fmaf(dh, c, s));
+}
+
+__global__ void __launch_bounds__(kEvalCols) screen_eval_kernel(ScreenArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int r = blockIdx.y, tid = threadIdx.x;
+  const int N = a.N, D = a.D, Di = D - 1;
+  const int nlc = prep_chunks(a.P_L);
+  double2* S = reinterpret_cast<double2*>(smem_raw);
+  float* Mf = reinterpret_cast<float*>(S + D * D);
+  const float2* s_int = a.s_int + (size_t)r * nlc * Di * Di;
+  const double2* s_edge = a.s_edge + (size_t)r * nlc * (2 * D - 1);
+  // chunk sums in chunk order, then M = eps_e eps_d i^(e+d) S
   for (int ed = tid; ed < D * D; ed += blockDim.x) {
     const int e = ed / D, d = ed - e * D;
+    double2 s = make_double2(0.0, 0.0);
+    if (e >= 1 && d >= 1) {
+      const int idx = (e - 1) * Di + (d - 1);
+      for (int c = 0; c < nlc; ++c) {
+        const float2 v = s_int[(size_t)c * Di * Di + idx];
+        s.x += (double)v.x;
+        s.y += (double)v.y;
+      }
+    } else {
+      const int idx = e == 0 ? d : D - 1 + e;
+      for (int c = 0; c < nlc; ++c) {
+        const double2 v = s_edge[(size_t)c * (2 * D - 1) + idx];
+        s.x += v.x;
+        s.y += v.y;
+      }
+    }
     const double f = (e ? 2.0 : 1.0) * (d ? 2.0 : 1.0);
-    const double2 s = S[ed];
     double2 m;
     switch ((e + d) & 3) {
       case 0: m = make_double2(s.x, s.y); break;
@@ -713,68 +761,86 @@ __global__ void __launch_bounds__(kPrepThreads) screen_prep_kernel(ScreenArgs a)
   }
   __syncthreads();
 
+  const int j = blockIdx.x * kEvalCols + tid;
+  if (j >= N) return;
   const double half = 0.5 * (N - 1);
   const int K = a.KH + a.KC;
   float* Bt = a.Bt + (size_t)r * K * N;
-  for (int j = tid; j < N; j += blockDim.x) {
-    const double tj = ((double)j - half) / half;
-    double Tm1 = 1.0, Tc = tj, G = S[0].x, H = 0.0;
-    for (int n = 1; n < D; ++n) {
-      G = fma(S[n * D].x, Tc, G);
-      H = fma(S[n].x, Tc, H);
-      const double Tn = 2.0 * tj * Tc - Tm1;
-      Tm1 = Tc;
-      Tc = Tn;
-    }
-    double sg, cg, sh, ch;
-    sincos(G, &sg, &cg);
-    sincos(H, &sh, &ch);
-    a.Py[(size_t)r * N + j] = make_float2((float)cg, (float)-sg);
-    a.Px[(size_t)r * N + j] = make_float2((float)ch, (float)-sh);
-    if (a.Gy) a.Gy[(size_t)r * N + j] = G;
-    if (a.Hx) a.Hx[(size_t)r * N + j] = H;
-    if (a.KC == 0) continue;  // no low-frequency block: no Chebyshev rows
-    const float tf = (float)tj;
-    for (int e = 1; e < D; ++e) {
-      float T0 = 1.f, T1 = tf, acc = 0.f;
-      const float* Me = Mf + e * D;
-      for (int d = 1; d < D; ++d) {
-        acc = fmaf(Me[d], T1, acc);
-        const float Tn = 2.f * tf * T1 - T0;
-        T0 = T1;
-        T1 = Tn;
-      }
-      if (a.tb_hi) {
-        // tensor-core layout: B[x][kc0 + e - 1] as FP16 hi / scaled lo
-        const size_t o = ((size_t)r * N + j) * a.Kp + a.kc0 + e - 1;
-        const __half h = __float2half_rn(acc);
-        a.tb_hi[o] = h;
-        a.tb_lo[o] = __float2half_rn((acc - __half2float(h)) * 2048.f);
-      } else {
-        Bt[(size_t)(a.KH + e - 1) * N + j] = acc;
-      }
-    }
-    if (!a.tb_hi)
-      for (int e = D - 1; e < a.KC; ++e) Bt[(size_t)(a.KH + e) * N + j] = 0.f;
+  const double tj = ((double)j - half) / half;
+  double Tm1 = 1.0, Tc = tj, G = S[0].x, H = 0.0;
+  for (int n = 1; n < D; ++n) {
+    G = fma(S[n * D].x, Tc, G);
+    H = fma(S[n].x, Tc, H);
+    const double Tn = 2.0 * tj * Tc - Tm1;
+    Tm1 = Tc;
+    Tc = Tn;
   }
+  a.Py[(size_t)r * N + j] = phasor_fp64(G);
+  a.Px[(size_t)r * N + j] = phasor_fp64(H);
+  if (a.Gy) a.Gy[(size_t)r * N + j] = G;
+  if (a.Hx) a.Hx[(size_t)r * N + j] = H;
+  if (a.KC == 0) return;  // no low-frequency block: no Chebyshev rows
+  const float tf = (float)tj;
+  for (int e = 1; e < D; ++e) {
+    float T0 = 1.f, T1 = tf, acc = 0.f;
+    const float* Me = Mf + e * D;
+    for (int d = 1; d < D; ++d) {
+      acc = fmaf(Me[d], T1, acc);
+      const float Tn = 2.f * tf * T1 - T0;
+      T0 = T1;
+      T1 = Tn;
+    }
+    if (a.tb_hi) {
+      // tensor-core layout: B[x][kc0 + e - 1] as FP16 hi / scaled lo
+      const size_t o = ((size_t)r * N + j) * a.Kp + a.kc0 + e - 1;
+      const __half h = __float2half_rn(acc);
+      a.tb_hi[o] = h;
+      a.tb_lo[o] = __float2half_rn((acc - __half2float(h)) * 2048.f);
+    } else {
+      Bt[(size_t)(a.KH + e - 1) * N + j] = acc;
+    }
+  }
+  if (!a.tb_hi)
+    for (int e = D - 1; e < a.KC; ++e) Bt[(size_t)(a.KH + e) * N + j] = 0.f;
 }
 
-cudaError_t launch_screen_prep(int B, const ScreenArgs& a, cudaStream_t st) {
-  if (a.D > kMaxD || a.D < 2) return cudaErrorInvalidValue;
-  const size_t smem = prep_smem_bytes(a.P_L, a.D);
-  static int attr_set[64] = {};  // largest dynamic shared memory already granted, per device
+// largest dynamic shared memory granted so far, per device and kernel
+template <typename F>
+static cudaError_t grant_smem(F* kernel, size_t bytes, int (&granted)[64]) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 64) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
-  if ((int)smem > attr_set[dev]) {
-    e = cudaFuncSetAttribute(screen_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if ((int)bytes > 48 * 1024 && (int)bytes > granted[dev]) {
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
-    attr_set[dev] = 220 * 1024;
+    granted[dev] = (int)bytes;
   }
-  screen_prep_kernel<<<B, kPrepThreads, smem, st>>>(a);
+  return cudaSuccess;
+}
+
+cudaError_t launch_screen_terms(int B, const ScreenArgs& a, cudaStream_t st) {
+  if (a.D > kMaxD || a.D < 2) return cudaErrorInvalidValue;
+  static int granted[64] = {};
+  const size_t smem = prep_smem_bytes(a.D);
+  cudaError_t e = grant_smem(screen_terms_kernel, smem, granted);
+  if (e != cudaSuccess) return e;
+  const int nhb = (a.KH / 2 + kPrepThreads - 1) / kPrepThreads;
+  const int blocks = prep_chunks(a.P_L) + nhb;
+  if (blocks == 0) return cudaSuccess;
+  screen_terms_kernel<<<dim3(blocks, B), kPrepThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
+cudaError_t launch_screen_eval(int B, const ScreenArgs& a, cudaStream_t st) {
+  if (a.D > kMaxD || a.D < 2) return cudaErrorInvalidValue;
+  static int granted[64] = {};
+  const size_t smem = eval_smem_bytes(a.D);
+  cudaError_t e = grant_smem(screen_eval_kernel, smem, granted);
+  if (e != cudaSuccess) return e;
+  screen_eval_kernel<<<dim3((a.N + kEvalCols - 1) / kEvalCols, B), kEvalCols, smem, st>>>(a);
+  return cudaGetLastError();
+}
 // ---------------------------------------------------------------------------
 // high-frequency tables: A^T[2q][y] = Re(v e^{i th_y}), A^T[2q+1][y] = -Im(...),
 // B[2q][x] = cos th_x, B[2q+1][x] = sin th_x; phases from exact 64-bit turns

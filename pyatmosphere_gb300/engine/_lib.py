@@ -77,6 +77,10 @@ class AtmPlanInfo(ctypes.Structure):
         ("workspace_bytes", ctypes.c_int64),
         ("launches_per_run", ctypes.c_int32),
         ("row_parts", ctypes.c_int32),
+        ("col_tile", ctypes.c_int32),
+        ("row_variant", ctypes.c_int32),
+        ("col_variant", ctypes.c_int32),
+        ("tuned", ctypes.c_int32),
     ]
 
 
@@ -97,6 +101,7 @@ SIGNATURES = {
                                   ctypes.c_void_p]),
     "atm_measures": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                     ctypes.c_void_p]),
+    "atm_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
     "atm_profile_begin": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "atm_profile_end": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "atm_fma_probe": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
@@ -132,7 +137,8 @@ SIGNATURES = {
                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
 }
 
-KIND_NAMES = ["screen_prep", "screen_table", "screen_gemm", "row_pass", "col_pass", "finalize", "tracked"]
+KIND_NAMES = ["screen_prep", "screen_table", "screen_gemm", "row_pass", "col_pass", "finalize", "tracked",
+              "screen_eval"]
 
 _lock = threading.Lock()
 _lib = None

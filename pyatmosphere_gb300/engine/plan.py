@@ -59,10 +59,13 @@ class EnginePlan:
         self._handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             check(self.lib.atm_plan_create(ctypes.byref(d), ctypes.byref(self._handle)))
+        self._refresh_info()
+        self.n_out = self.info["n_out"]
+
+    def _refresh_info(self):
         info = _lib.AtmPlanInfo()
         check(self.lib.atm_plan_info(self._handle, ctypes.byref(info)))
         self.info = {f: getattr(info, f) for f, _ in _lib.AtmPlanInfo._fields_}
-        self.n_out = info.n_out
 
     def _desc(self, wvl, w0, F0, positions, length, pupils):
         k = self._kw
@@ -102,11 +105,21 @@ class EnginePlan:
         return d
 
     def update(self, wvl, w0, F0, positions, length, pupils=()):
-        """Re-targets the plan (atm_plan_update): same grid, screen count,
-        spectral grid, pupil count and batch; new source / path / pupil radii."""
+        """Re-targets the plan (atm_plan_update): same grid, spectral grid,
+        pupil count and batch, at most the creating screen count; new source /
+        path / pupil radii."""
         d = self._desc(wvl, w0, F0, positions, length, pupils)
         with torch.cuda.device(self.device):
             check(self.lib.atm_plan_update(self._handle, ctypes.byref(d)))
+        self.n_screens = len(positions)
+
+    def autotune(self, batch: Optional[int] = None, repeats: int = 3) -> dict:
+        """Times the FFT-pass launch variants on the plan's workspace
+        (atm_autotune) and keeps the fastest; returns the choice."""
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_autotune(self._handle, int(batch or self.batch), int(repeats), _stream(self.device)))
+        self._refresh_info()
+        return {k: self.info[k] for k in ("col_tile", "row_variant", "col_variant", "tuned")}
 
     def draw_spectra(self, seed, first, sqrt_psd, rho, theta, value):
         """Seeded spectra on the device (atm_draw_spectra) into the given tensors."""

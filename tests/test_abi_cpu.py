@@ -46,6 +46,8 @@ def test_plan_create_rejects_bad_descriptors_without_gpu(built):
     assert b"resolution" in lib.atm_last_error()
     d.resolution, d.abi_version = 256, 7
     assert lib.atm_plan_create(ctypes.byref(d), ctypes.byref(h)) == -1
+    assert lib.atm_autotune(None, 1, 1, None) == -1
+    assert b"NULL" in lib.atm_last_error()
 
 
 @pytest.mark.parametrize("N", [64, 128, 256, 512, 1024, 2048, 4096])

@@ -208,3 +208,24 @@ def test_graph_capture_replays_run(torch_cuda):
     direct2 = plan.run(*to_dev(torch, *sp2)).cpu().numpy()
     np.testing.assert_array_equal(out.cpu().numpy(), direct2)
     assert not np.array_equal(direct, direct2)
+
+
+@pytest.mark.parametrize("N", [512, 2048])
+def test_autotune_keeps_results(torch_cuda, N):
+    """atm_autotune only changes launch shapes: the tuned plan gives the same
+    bits as the untuned one, and its choice is reported in the plan info."""
+    torch = torch_cuda
+    d = 3.0 / N
+    spec = o.ChannelSpec(N=N, delta=d, w0=0.08, length=8e3, count=3, points=256, Cn2=2e-15, pupil_radius=0.1)
+    plan, base = make_plan(spec, batch=3)
+    sp = to_dev(torch, *spectra(spec, base, seed=5, R=3))
+    before = plan.run(*sp).cpu().numpy()
+    choice = plan.autotune(repeats=2)
+    assert choice["tuned"] == 1
+    assert choice["col_tile"] in (2, 4, 8, 16) and choice["col_tile"] * N // 16 <= 512
+    assert choice["row_variant"] in (0, 1) and choice["col_variant"] in (0, 1)
+    after = plan.run(*sp).cpu().numpy()
+    np.testing.assert_array_equal(after, before)
+    # every column tile computes the same arithmetic
+    plan2, _ = make_plan(spec, batch=3, col_tile=2)
+    np.testing.assert_array_equal(plan2.run(*sp).cpu().numpy(), before)

@@ -27,7 +27,8 @@ def test_tc_gemm_matches_fp64(S, M, N, K):
     assert err < 2e-6, err
 
 
-@pytest.mark.parametrize("N,P,Cn2,delta", [(256, 512, 1e-14, 4e-3), (2048, 1024, 5e-16, 1.5e-3)])
+@pytest.mark.parametrize("N,P,Cn2,delta", [(256, 512, 1e-14, 4e-3), (2048, 1024, 5e-16, 1.5e-3),
+                                           (4096, 256, 1e-15, 3.0 / 4096)])
 def test_tc_screen_matches_oracle(N, P, Cn2, delta):
     """Screens through the tensor-core GEMM against the FP64 oracle."""
     import torch
@@ -59,6 +60,26 @@ def test_tc_channel_config2_matches_oracle():
     plan = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, o.screen_positions(spec.length, spec.count),
                       spec.length, f_base=base, pupils=[(0.2,)], batch=1, flags=_lib.FLAG_TC_GEMM)
     field = torch.empty((1, 2048, 2048), dtype=torch.complex64, device="cuda")
+    meas = plan.run(*[torch.from_numpy(a).cuda() for a in (rho, theta, value)], field_out=field).cpu().numpy()
+    res, u = o.simulate(spec, rho, theta, value, return_field=True)
+    assert o.rel_l2(field.cpu().numpy()[0], u) < 1e-4
+    assert meas[0, 8] == pytest.approx(res[0]["eta_0"], rel=1e-5)
+
+
+def test_tc_channel_4096_matches_oracle():
+    """The largest grid: 4096^2, two screens, through the whole run."""
+    import torch
+    from oracle import atm_oracle as o
+    from pyatmosphere_gb300.engine import EnginePlan
+    spec = o.ChannelSpec(N=4096, delta=3.0 / 4096, w0=0.1, length=20e3, count=2, points=256, Cn2=2e-15,
+                         pupil_radius=0.15)
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    rho, theta, value = o.draw_spectra(41, range(1), spec.count, base, psd)
+    plan = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, o.screen_positions(spec.length, spec.count),
+                      spec.length, f_base=base, pupils=[(0.15,)], batch=1)
+    assert plan.info["gemm_k"] % 64 == 0  # the tensor-core layout is in use
+    field = torch.empty((1, 4096, 4096), dtype=torch.complex64, device="cuda")
     meas = plan.run(*[torch.from_numpy(a).cuda() for a in (rho, theta, value)], field_out=field).cpu().numpy()
     res, u = o.simulate(spec, rho, theta, value, return_field=True)
     assert o.rel_l2(field.cpu().numpy()[0], u) < 1e-4
