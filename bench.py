@@ -366,7 +366,8 @@ def run_gb300(args, rank, world, local_rank):
         "col_pass": ("hbm", 16.0 * N * N * B, "GB/s"),
         # n+1 row launches move 8 (write) + 4 (phi) + (n-1)(16 + 4) + 8 (read) bytes per pixel
         "row_pass": ("hbm", (12.0 + 20.0 * (n - 1) + 8.0) / (n + 1) * N * N * B, "GB/s"),
-        "screen_table": ("hbm", 2.0 * (plan.info["gemm_k"]) * N * 4.0 * B, "GB/s"),
+        # high-frequency columns of A and B: FP16 hi + lo (tensor cores) or FP32 (SIMT)
+        "screen_table": ("hbm", (4 * 2.0 if tc else 2 * 4.0) * 2 * (w["points"] - plan.info["low_annuli"]) * N * B, "GB/s"),
     }
     peaks = {}
     try:
