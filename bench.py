@@ -270,7 +270,8 @@ def run_gb300(args, rank, world, local_rank):
     base, psd = base_and_psd()
     pos = positions(w["length"], w["count"])
     from pyatmosphere_gb300.engine import _lib
-    flags = {"tc": _lib.FLAG_TC_GEMM, "simt": _lib.FLAG_SIMT_GEMM, "auto": 0}[args.gemm]
+    flags = {"tc": _lib.FLAG_TC_GEMM, "simt": _lib.FLAG_SIMT_GEMM, "auto": 0,
+             "tc-cpasync": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_CPASYNC}[args.gemm]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
                       pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags)
     tuned = plan.autotune(repeats=2) if args.autotune else None
@@ -359,7 +360,7 @@ def run_gb300(args, rank, world, local_rank):
     # ---- roofline of the dominant kernel, measured in the timed region ----
     N, n = w["N"], w["count"]
     K = plan.info["gemm_k"]
-    tc = flags != _lib.FLAG_SIMT_GEMM and w["N"] >= 256
+    tc = not (flags & _lib.FLAG_SIMT_GEMM) and w["N"] >= 256
     work = {  # algorithmic work per launch of a B-realisation batch
         # tensor cores: three FP16 MMAs (hi.hi, hi.lo, lo.hi) per FP32 product, against the dense 16-bit peak
         "screen_gemm": ("tensor", 3 * 2.0 * N * N * K * B, "TFLOP/s") if tc else ("fp32", 2.0 * N * N * K * B, "TFLOP/s"),
@@ -433,7 +434,8 @@ def run_gb300(args, rank, world, local_rank):
             "data": "synthetic (seeded spectra, reference formulas)",
             "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B, "gemm": args.gemm,
                        "l2": "inputs larger than L2 (field batch 8.6 GB per step)", "gemm_k": K,
-                       "low_annuli": info["low_annuli"], "cheb_terms": info["cheb_terms"], "autotune": tuned},
+                       "low_annuli": info["low_annuli"], "cheb_terms": info["cheb_terms"], "autotune": tuned,
+                       "gemm_form": ["fp32 simt", "tcgen05 cp.async", "tcgen05 persistent tma"][info["gemm_form"]]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "plain": {"value": plain, "unit": UNIT, "realisations": args.plain,
                       "batched_over_plain": (value / world / plain) if plain else None},
@@ -468,8 +470,9 @@ def main():
                     help="channels of the mixed-size workload leg (0: skip)")
     ap.add_argument("--surrogate-points", type=int, default=8,
                     help="held-out points of the surrogate check (0: skip the surrogate leg)")
-    ap.add_argument("--gemm", choices=["auto", "tc", "simt"], default="auto",
-                    help="screen GEMM on tensor cores (tc, the default at 2048^2) or FP32 SIMT cores")
+    ap.add_argument("--gemm", choices=["auto", "tc", "tc-cpasync", "simt"], default="auto",
+                    help="screen GEMM on tensor cores (tc: persistent TMA form, the default at 2048^2; "
+                         "tc-cpasync: one CTA per tile) or FP32 SIMT cores")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

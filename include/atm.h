@@ -50,6 +50,8 @@ extern "C" {
 /* AtmChannelDesc.flags */
 #define ATM_FLAG_SIMT_GEMM 1     /* screen GEMM on FP32 SIMT cores (default below N = 256) */
 #define ATM_FLAG_TC_GEMM 2       /* screen GEMM on tcgen05 tensor cores (the default for N >= 256) */
+#define ATM_FLAG_TC_CPASYNC 4    /* tensor-core GEMM in its one-CTA-per-tile cp.async form instead of the
+                                    persistent TMA form */
 
 /* per-realisation doubles in measures_out (slot index) */
 #define ATM_OUT_ETA_TOTAL 0      /* measures.eta(pupil=False)      measures.py:7-8   */
@@ -103,6 +105,7 @@ typedef struct AtmPlanInfo {
   int32_t row_variant;        /* 0: persistent pipelined row pass, 1: one CTA per row block */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile */
   int32_t tuned;              /* 1 after a successful atm_autotune */
+  int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA form */
 } AtmPlanInfo;
 
 /* ABI version of the loaded library (ATM_ABI_VERSION). */
@@ -217,11 +220,12 @@ int atm_mlp_infer(AtmMlp* mlp, const float* x, int32_t batch, const float* lo, c
 /* Unit-test entry point of the tensor-core screen GEMM: out[s][m][n] =
  * scale * sum_k A[s][m][k] B[s][n][k] for FP32 device arrays (row stride K),
  * computed with tcgen05 MMAs on FP16 hi/lo slices; M % 128 == 0,
- * N % 256 == 0.  Allocates its slice scratch; synchronises the stream.  No
- * reference counterpart (the reference's screen product is a cupy/numpy
- * complex GEMM, phase_screens.py:125-126). */
+ * N % 256 == 0.  variant 0: persistent TMA form, 1: cp.async form.
+ * Allocates its slice scratch; synchronises the stream.  No reference
+ * counterpart (the reference's screen product is a cupy/numpy complex GEMM,
+ * phase_screens.py:125-126). */
 int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32_t N, int32_t K, float scale,
-                     float* out, void* stream);
+                     float* out, int32_t variant, void* stream);
 
 /* Times the launch variants of the FFT passes on this plan's own workspace
  * (`batch` realisations, `repeats` timed launches each after one warm-up)

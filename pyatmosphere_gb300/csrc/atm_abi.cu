@@ -159,6 +159,7 @@ struct AtmPlan {
   int Kp = 0, kc0 = 0;  // tensor-core layout
   DevBuf ta_hi, ta_lo, tb_hi, tb_lo;
   DevBuf s_int, s_edge;  // chunk sums of the low-frequency block
+  atm::TcPlan* tcp = nullptr;  // TMA descriptors of the screen GEMM (null: cp.async form)
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
     int64_t s = 0;
@@ -166,6 +167,7 @@ struct AtmPlan {
     return s;
   }
   ~AtmPlan() {
+    atm::tc_plan_destroy(tcp);
     for (auto* b : bufs)
       if (b->p) cudaFree(b->p);
     for (auto e : ev) cudaEventDestroy(e);
@@ -455,6 +457,9 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
         return fail(ATM_ERR_CUDA, "cudaMemset of the tensor-core tables failed");
       }
     }
+    if (!(d->flags & ATM_FLAG_TC_CPASYNC))
+      pl->tcp = atm::tc_plan_create(pl->B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p,
+                                    (const __half*)pl->ta_lo.p, (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p);
   }
   if (pl->n > 0) {
     const size_t simt_rows = pl->use_tc ? 0 : 1;  // FP32 SIMT tables only without tensor cores
@@ -546,6 +551,7 @@ int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
   info->row_variant = pl->row_variant;
   info->col_variant = pl->col_variant;
   info->tuned = pl->tuned;
+  info->gemm_form = pl->n == 0 ? 0 : (!pl->use_tc ? 0 : (pl->tcp ? 2 : 1));
   return ATM_OK;
 }
 
@@ -623,9 +629,13 @@ int run_screen(AtmPlan* pl, const atm::ScreenArgs& s, int B, cudaStream_t st) {
       ATM_CUDA(atm::launch_screen_table_tc(B, s, st));
     }
     Prof p(pl, ATM_KIND_SCREEN_GEMM, st);
-    ATM_CUDA(atm::launch_tc_gemm(B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p, (const __half*)pl->ta_lo.p,
-                                 (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p, (float*)pl->phi.p,
-                                 0.15915494309189533577f, st));
+    constexpr float kInv2Pi = 0.15915494309189533577f;  // phi_G in turns
+    if (pl->tcp)
+      ATM_CUDA(atm::launch_tc_gemm_tma(pl->tcp, B, (float*)pl->phi.p, kInv2Pi, st));
+    else
+      ATM_CUDA(atm::launch_tc_gemm(B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p, (const __half*)pl->ta_lo.p,
+                                   (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p, (float*)pl->phi.p, kInv2Pi,
+                                   st));
     return ATM_OK;
   }
   if (pl->P_H > 0) {

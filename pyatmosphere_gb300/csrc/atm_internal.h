@@ -160,7 +160,18 @@ int row_pass_rows(int N);          // rows per CTA of the row pass
 int col_tile_default(int N);
 bool supported_n(int N);
 __host__ __device__ int prep_chunks(int P_L);
+// FP16 slices of the tensor-core operands: a = hi + lo / kTcLoScale with
+// hi = fp16(a), lo = fp16((a - hi) * kTcLoScale); the scale keeps the
+// residual in FP16's normal range
+constexpr float kTcLoScale = 2048.0f;
 size_t tc_smem_bytes();
+// TMA descriptors of one GEMM's operands ([S][M][Kp] and [S][Nn][Kp] FP16
+// slices), encoded once on the host; null when the driver offers no encoder
+struct TcPlan;
+TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
+                       const __half* b_lo);
+void tc_plan_destroy(TcPlan* p);
+cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, cudaStream_t st);
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                            const __half* b_lo, float* out, float scale, cudaStream_t st);
 cudaError_t launch_screen_table_tc(int B, const ScreenArgs& a, cudaStream_t st);

@@ -791,11 +791,11 @@ __global__ void __launch_bounds__(kEvalCols) screen_eval_kernel(ScreenArgs a) {
       T1 = Tn;
     }
     if (a.tb_hi) {
-      // tensor-core layout: B[x][kc0 + e - 1] as FP16 hi / scaled lo
+      // tensor-core layout: B[x][kc0 + e - 1] as FP16 hi / lo
       const size_t o = ((size_t)r * N + j) * a.Kp + a.kc0 + e - 1;
       const __half h = __float2half_rn(acc);
       a.tb_hi[o] = h;
-      a.tb_lo[o] = __float2half_rn((acc - __half2float(h)) * 2048.f);
+      a.tb_lo[o] = __float2half_rn((acc - __half2float(h)) * kTcLoScale);
     } else {
       Bt[(size_t)(a.KH + e - 1) * N + j] = acc;
     }
@@ -865,12 +865,12 @@ __global__ void __launch_bounds__(256) screen_table_kernel(ScreenArgs a) {
 }
 
 // tensor-core layout of the high-frequency tables: thread (term q, row j)
-// writes A[j][2q..2q+1] and B[j][2q..2q+1] as FP16 hi / scaled lo pairs
+// writes A[j][2q..2q+1] and B[j][2q..2q+1] as FP16 hi / lo pairs
 __device__ __forceinline__ void split_pair(float u, float w, __half2* hi, __half2* lo) {
   const __half uh = __float2half_rn(u), wh = __float2half_rn(w);
   *hi = __halves2half2(uh, wh);
-  *lo = __halves2half2(__float2half_rn((u - __half2float(uh)) * 2048.f),
-                       __float2half_rn((w - __half2float(wh)) * 2048.f));
+  *lo = __halves2half2(__float2half_rn((u - __half2float(uh)) * kTcLoScale),
+                       __float2half_rn((w - __half2float(wh)) * kTcLoScale));
 }
 
 __global__ void __launch_bounds__(128) screen_table_tc_kernel(ScreenArgs a) {
@@ -905,7 +905,7 @@ __global__ void cheb_cols_tc_kernel(int N, int Kp, int kc0, int D, const float* 
     const __half h = __float2half_rn(v);
     const size_t o = ((size_t)r * N + j) * Kp + kc0 + e - 1;
     hi[o] = h;
-    lo[o] = __float2half_rn((v - __half2float(h)) * 2048.f);
+    lo[o] = __float2half_rn((v - __half2float(h)) * kTcLoScale);
   }
 }
 

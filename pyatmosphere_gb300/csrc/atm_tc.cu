@@ -1,22 +1,35 @@
 // 5th-generation tensor-core GEMM for the screen synthesis (sm_103a).
 //
-//   phi_G[s][y][x] = (1/2pi) sum_k A[s][y][k] B[s][x][k]
+//   phi_G[s][y][x] = scale * sum_k A[s][y][k] B[s][x][k]
 //
 // Operands are FP32 values split into two scaled FP16 slices,
 //   a = a_hi + a_lo / 2^11,  a_hi = fp16(a),  a_lo = fp16((a - a_hi) 2^11),
 // so that a_hi b_hi + (a_hi b_lo + a_lo b_hi) / 2^11 carries ~22 bits: three
-// tcgen05.mma (kind::f16, FP32 accumulation) per K step into two TMEM
-// accumulators (D0 = sum hi.hi, D1 = sum of the cross terms), combined in the
-// epilogue.  Tiles: M = 128 rows (y) x N = 256 columns (x) per CTA, K tile 64
-// (one 128-byte swizzle atom of FP16), two shared-memory stages filled with
-// cp.async into the K-major SWIZZLE_128B layout the MMA descriptors describe.
-// One elected thread issues the MMAs; tcgen05.commit arrives on an mbarrier
-// per stage.  Every mbarrier wait is bounded by %globaltimer: on timeout the
-// CTA records an error, drains its copies, frees its TMEM and returns.
+// tcgen05.mma (kind::f16, FP32 accumulation) per K step of 16 into two TMEM
+// accumulators (D0 = sum hi.hi, D1 = sum of the cross terms, 2 x 256
+// columns), combined in the epilogue.  Accumulating the cross terms apart
+// matters: added into D0 they lose their low bits to the tensor core's
+// alignment of small addends (2.8e-6 instead of < 2e-6 relative at K = 768).
+//
+// tc_gemm_tma_kernel (default): persistent, warp-specialised.  Warp 0 loads
+// the four 128-byte-swizzled operand boxes of a K tile with TMA
+// (cp.async.bulk.tensor) into a two-stage ring, running ahead into the next
+// tile while warps 2-5 drain the accumulators (tcgen05.ld, combine, scale,
+// store); warp 1 issues the MMAs of each 128 x 256 output tile.  mbarriers:
+// full / empty per stage, full / empty for the accumulator pair.
+// tc_gemm_kernel: the first form, one CTA per tile, operands through cp.async
+// by all threads (kept for comparison and as the fallback when the driver
+// offers no tensor-map encoder).
+//
+// Every mbarrier wait is bounded by %globaltimer: on timeout a CTA records an
+// error, waits (bounded) for its copies and MMAs in flight, frees its TMEM
+// and returns.
+#include <cuda.h>  // CUtensorMap and the driver enums (the encoder is fetched at run time)
 #include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "../../include/atm.h"
 #include "atm_internal.h"
@@ -228,7 +241,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_gemm_kernel(TcArgs a) {
             "=r"(l[24]), "=r"(l[25]), "=r"(l[26]), "=r"(l[27]), "=r"(l[28]), "=r"(l[29]), "=r"(l[30]), "=r"(l[31])
           : "r"(d1 + lane_addr + c0));
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      const float lo_scale = 1.f / 2048.f;
+      constexpr float lo_scale = 1.f / kTcLoScale;
 #pragma unroll
       for (int j = 0; j < 32; j += 4) {
         float4 o;
@@ -247,7 +260,240 @@ __global__ void __launch_bounds__(THREADS, 1) tc_gemm_kernel(TcArgs a) {
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem) : "memory");
 }
 
-// split FP32 [rows][K] (row stride lds) into scaled FP16 slices [rows][Kp] (zero padded)
+// ---------------------------------------------------------------------------
+// persistent, warp-specialised form: TMA producer, MMA issuer, epilogue warps
+// ---------------------------------------------------------------------------
+constexpr int P_STAGES = 2;
+constexpr int P_THREADS = 192;  // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
+constexpr int P_SMEM = P_STAGES * STAGE + 1024;
+constexpr int EPI_THREADS = 128;
+
+struct TmaOperands {
+  CUtensorMap ah, al, bh, bl;  // [S][rows][Kp] FP16, boxes of 64 (K) x 128 or 256 rows
+};
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+// bounded wait that also gives up once another role has set the abort flag;
+// a timeout sets the flag itself
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+  const uint64_t t0 = globaltimer();
+  for (uint32_t spin = 1;; ++spin) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if ((spin & 15) == 0) {
+      if (*abort_flag) return false;
+      if (globaltimer() - t0 > kTimeoutNs) {
+        *abort_flag = 1;
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int* s, int* m0, int* n0) {
+  const int per = tiles_m * tiles_n;
+  *s = t / per;
+  const int r = t - *s * per;
+  *m0 = (r / tiles_n) * TM;
+  *n0 = (r - (r / tiles_n) * tiles_n) * TN;
+}
+
+__global__ void __launch_bounds__(P_THREADS, 1)
+    tc_gemm_tma_kernel(const __grid_constant__ TmaOperands ops, float* __restrict__ out, int S, int M, int Nn, int Kp,
+                       float scale) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[P_STAGES], empty_bar[P_STAGES], accf_bar, acce_bar, drain_bar;
+  __shared__ uint32_t tmem_holder;
+  __shared__ int abort_word;
+  volatile int* abort_flag = &abort_word;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t base = (smem_u32(smem_raw) + 1023) & ~1023u;
+  const int KT = Kp / TK;
+  const int tiles_m = M / TM, tiles_n = Nn / TN;
+  const int n_tiles = S * tiles_m * tiles_n;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < P_STAGES; ++i) {
+      mbar_init(smem_u32(&full_bar[i]), 1);
+      mbar_init(smem_u32(&empty_bar[i]), 1);
+    }
+    mbar_init(smem_u32(&accf_bar), 1);
+    mbar_init(smem_u32(&acce_bar), EPI_THREADS);
+    mbar_init(smem_u32(&drain_bar), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(smem_u32(&tmem_holder))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_holder;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer ----
+      int stage = 0;
+      uint32_t phase = 0;
+      bool issued[P_STAGES] = {};
+      uint32_t issued_phase[P_STAGES] = {};
+      bool stop = false;
+      for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
+        int s, m0, n0;
+        tile_coords(t, tiles_m, tiles_n, &s, &m0, &n0);
+        for (int kt = 0; kt < KT; ++kt) {
+          if (!mbar_wait_or_abort(smem_u32(&empty_bar[stage]), phase ^ 1u, abort_flag)) {
+            stop = true;
+            break;
+          }
+          const uint32_t fb = smem_u32(&full_bar[stage]);
+          mbar_arrive_expect_tx(fb, (uint32_t)STAGE);
+          const uint32_t st = base + stage * STAGE;
+          const int x = kt * TK;
+          tma_load_3d(st, &ops.ah, x, m0, s, fb);
+          tma_load_3d(st + A_SLICE, &ops.al, x, m0, s, fb);
+          tma_load_3d(st + 2 * A_SLICE, &ops.bh, x, n0, s, fb);
+          tma_load_3d(st + 2 * A_SLICE + B_SLICE, &ops.bl, x, n0, s, fb);
+          issued[stage] = true;
+          issued_phase[stage] = phase;
+          if (++stage == P_STAGES) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+      }
+      // before teardown: every issued copy has landed, and (normal path) the
+      // MMAs have released every stage
+      const bool aborted = *abort_flag != 0;
+      for (int i = 0; i < P_STAGES; ++i)
+        if (issued[i])
+          mbar_wait(smem_u32(aborted ? &full_bar[i] : &empty_bar[i]), issued_phase[i]);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      int stage = 0;
+      uint32_t phase = 0, aphase = 0;
+      bool stop = false;
+      const uint32_t d0 = tmem, d1 = tmem + TN;  // columns [0, 256) and [256, 512)
+      for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
+        // the epilogue has drained the previous tile's accumulators
+        if (!mbar_wait_or_abort(smem_u32(&acce_bar), aphase ^ 1u, abort_flag)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        for (int kt = 0; kt < KT; ++kt) {
+          if (!mbar_wait_or_abort(smem_u32(&full_bar[stage]), phase, abort_flag)) {
+            stop = true;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t sa = base + stage * STAGE, sal = sa + A_SLICE, sb = sa + 2 * A_SLICE, sbl = sb + B_SLICE;
+#pragma unroll
+          for (int k4 = 0; k4 < TK / 16; ++k4) {
+            const uint32_t off = k4 * 32;  // 16 FP16 of K = 32 bytes inside the swizzle atom
+            const uint32_t acc = (kt > 0 || k4 > 0) ? 1u : 0u;
+            mma_f16(d0, smem_desc(sa + off), smem_desc(sb + off), acc);
+            mma_f16(d1, smem_desc(sa + off), smem_desc(sbl + off), acc);
+            mma_f16(d1, smem_desc(sal + off), smem_desc(sb + off), 1u);
+          }
+          mma_commit(smem_u32(&empty_bar[stage]));
+          if (++stage == P_STAGES) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+        if (stop) break;
+        mma_commit(smem_u32(&accf_bar));
+        aphase ^= 1u;
+      }
+      // every MMA of this thread has finished before TMEM is freed
+      mma_commit(smem_u32(&drain_bar));
+      mbar_wait(smem_u32(&drain_bar), 0);
+    }
+  } else {
+    // ---- epilogue: warps 2-5, TMEM lane quarter (warp % 4) ----
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    uint32_t aphase = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+      int s, m0, n0;
+      tile_coords(t, tiles_m, tiles_n, &s, &m0, &n0);
+      int ok = 0;
+      if (lane == 0) ok = mbar_wait_or_abort(smem_u32(&accf_bar), aphase, abort_flag) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+      float* o = out + ((size_t)s * M + m0 + row) * Nn + n0;
+#pragma unroll 1
+      for (int c0 = 0; c0 < TN; c0 += 32) {
+        uint32_t h[32], l[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(h[0]), "=r"(h[1]), "=r"(h[2]), "=r"(h[3]), "=r"(h[4]), "=r"(h[5]), "=r"(h[6]), "=r"(h[7]),
+              "=r"(h[8]), "=r"(h[9]), "=r"(h[10]), "=r"(h[11]), "=r"(h[12]), "=r"(h[13]), "=r"(h[14]), "=r"(h[15]),
+              "=r"(h[16]), "=r"(h[17]), "=r"(h[18]), "=r"(h[19]), "=r"(h[20]), "=r"(h[21]), "=r"(h[22]), "=r"(h[23]),
+              "=r"(h[24]), "=r"(h[25]), "=r"(h[26]), "=r"(h[27]), "=r"(h[28]), "=r"(h[29]), "=r"(h[30]), "=r"(h[31])
+            : "r"(tmem + lane_addr + c0));
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(l[0]), "=r"(l[1]), "=r"(l[2]), "=r"(l[3]), "=r"(l[4]), "=r"(l[5]), "=r"(l[6]), "=r"(l[7]),
+              "=r"(l[8]), "=r"(l[9]), "=r"(l[10]), "=r"(l[11]), "=r"(l[12]), "=r"(l[13]), "=r"(l[14]), "=r"(l[15]),
+              "=r"(l[16]), "=r"(l[17]), "=r"(l[18]), "=r"(l[19]), "=r"(l[20]), "=r"(l[21]), "=r"(l[22]), "=r"(l[23]),
+              "=r"(l[24]), "=r"(l[25]), "=r"(l[26]), "=r"(l[27]), "=r"(l[28]), "=r"(l[29]), "=r"(l[30]), "=r"(l[31])
+            : "r"(tmem + TN + lane_addr + c0));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        constexpr float lo_scale = 1.f / kTcLoScale;
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+          float4 v;
+          v.x = (__uint_as_float(h[j + 0]) + __uint_as_float(l[j + 0]) * lo_scale) * scale;
+          v.y = (__uint_as_float(h[j + 1]) + __uint_as_float(l[j + 1]) * lo_scale) * scale;
+          v.z = (__uint_as_float(h[j + 2]) + __uint_as_float(l[j + 2]) * lo_scale) * scale;
+          v.w = (__uint_as_float(h[j + 3]) + __uint_as_float(l[j + 3]) * lo_scale) * scale;
+          *reinterpret_cast<float4*>(o + c0 + j) = v;
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      mbar_arrive(smem_u32(&acce_bar));
+      aphase ^= 1u;
+    }
+  }
+
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_error, 1);
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem) : "memory");
+  }
+}
+
+// split FP32 [rows][K] (row stride lds) into FP16 hi / lo slices [rows][Kp] (zero padded)
 __global__ void split_fp16_kernel(const float* __restrict__ src, int rows, int K, int lds, int Kp,
                                   __half* __restrict__ hi, __half* __restrict__ lo) {
   const size_t total = (size_t)rows * Kp;
@@ -256,13 +502,94 @@ __global__ void split_fp16_kernel(const float* __restrict__ src, int rows, int K
     const float v = k < K ? src[(size_t)r * lds + k] : 0.f;
     const __half h = __float2half_rn(v);
     hi[i] = h;
-    lo[i] = __float2half_rn((v - __half2float(h)) * 2048.f);
+    lo[i] = __float2half_rn((v - __half2float(h)) * kTcLoScale);
   }
 }
 
 }  // namespace
 
 size_t tc_smem_bytes() { return SMEM; }
+
+// ---------------------------------------------------------------------------
+// host side of the TMA form
+// ---------------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// [S][rows][Kp] FP16 operand, boxes of TK x box_rows, 128-byte swizzle
+static bool encode_operand(EncodeTiledFn fn, CUtensorMap* map, const __half* base, int S, int rows, int Kp,
+                           int box_rows) {
+  if (((uintptr_t)base & 15) != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)S};
+  const cuuint64_t strides[2] = {(cuuint64_t)Kp * sizeof(__half), (cuuint64_t)rows * Kp * sizeof(__half)};
+  const cuuint32_t box[3] = {(cuuint32_t)TK, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct TcPlan {
+  TmaOperands ops;
+  int S, M, Nn, Kp;
+};
+
+TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
+                       const __half* b_lo) {
+  if (S < 1 || M % TM || Nn % TN || Kp % TK || Kp < TK) return nullptr;
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return nullptr;
+  TcPlan* p = new TcPlan{};
+  p->S = S;
+  p->M = M;
+  p->Nn = Nn;
+  p->Kp = Kp;
+  if (!encode_operand(fn, &p->ops.ah, a_hi, S, M, Kp, TM) || !encode_operand(fn, &p->ops.al, a_lo, S, M, Kp, TM) ||
+      !encode_operand(fn, &p->ops.bh, b_hi, S, Nn, Kp, TN) || !encode_operand(fn, &p->ops.bl, b_lo, S, Nn, Kp, TN)) {
+    delete p;
+    return nullptr;
+  }
+  return p;
+}
+
+void tc_plan_destroy(TcPlan* p) { delete p; }
+
+cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, cudaStream_t st) {
+  if (!p || S < 1 || S > p->S || !out) return cudaErrorInvalidValue;
+  static int sms[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (sms[dev] == 0) {
+    e = cudaFuncSetAttribute(tc_gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM);
+    if (e != cudaSuccess) return e;
+    int n = 0;
+    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    sms[dev] = std::max(n, 1);
+  }
+  const int n_tiles = S * (p->M / TM) * (p->Nn / TN);
+  const int grid = std::min(n_tiles, sms[dev]);
+  tc_gemm_tma_kernel<<<grid, P_THREADS, P_SMEM, st>>>(p->ops, out, S, p->M, p->Nn, p->Kp, scale);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                            const __half* b_lo, float* out, float scale, cudaStream_t st) {
@@ -306,13 +633,15 @@ cudaError_t tc_error_flag(int* host_flag, bool reset) {
 // unit-test entry point of the tensor-core GEMM (device pointers):
 //   out[s][m][n] = scale * sum_k A[s][m][k] B[s][n][k]  for FP32 A, B with K
 //   columns (row strides K), via the FP16 hi/lo split; M % 128 == 0,
-//   N % 256 == 0.  Scratch for the slices is allocated here (test path).
+//   N % 256 == 0; variant 0 = TMA form, 1 = cp.async form.  Scratch for the
+//   slices is allocated here (test path).
 // ---------------------------------------------------------------------------
 extern "C" int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32_t N, int32_t K,
-                                float scale, float* out, void* stream) {
+                                float scale, float* out, int32_t variant, void* stream) {
   if (!A || !B || !out || S < 1 || M < 1 || N < 1 || K < 1)
     return atm::set_error(ATM_ERR_INVALID, "bad tc gemm arguments");
   if (M % 128 || N % 256) return atm::set_error(ATM_ERR_UNSUPPORTED, "M %% 128 and N %% 256 must be 0");
+  if (variant != 0 && variant != 1) return atm::set_error(ATM_ERR_INVALID, "variant %d is not 0 or 1", variant);
   cudaStream_t st = (cudaStream_t)stream;
   const int Kp = (K + 63) / 64 * 64;
   __half *ah = nullptr, *al = nullptr, *bh = nullptr, *bl = nullptr;
@@ -328,10 +657,18 @@ extern "C" int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32
   }
   cudaError_t e = atm::launch_split_fp16(A, S * M, K, K, Kp, ah, al, st);
   if (e == cudaSuccess) e = atm::launch_split_fp16(B, S * N, K, K, Kp, bh, bl, st);
-  if (e == cudaSuccess) e = atm::launch_tc_gemm(S, M, N, Kp, ah, al, bh, bl, out, scale, st);
+  atm::TcPlan* tp = nullptr;
+  if (e == cudaSuccess && variant == 0) {
+    tp = atm::tc_plan_create(S, M, N, Kp, ah, al, bh, bl);
+    if (!tp) e = cudaErrorNotSupported;
+  }
+  if (e == cudaSuccess)
+    e = variant == 0 ? atm::launch_tc_gemm_tma(tp, S, out, scale, st)
+                     : atm::launch_tc_gemm(S, M, N, Kp, ah, al, bh, bl, out, scale, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   int flag = 0;
   if (e == cudaSuccess) e = atm::tc_error_flag(&flag, true);
+  atm::tc_plan_destroy(tp);
   cudaFree(ah);
   cudaFree(al);
   cudaFree(bh);

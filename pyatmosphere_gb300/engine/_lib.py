@@ -19,6 +19,7 @@ ABI_VERSION = 1
 MAX_PUPILS = 8
 FLAG_SIMT_GEMM = 1
 FLAG_TC_GEMM = 2
+FLAG_TC_CPASYNC = 4
 SOURCE_GAUSSIAN = 0
 SOURCE_PLANE = 1
 
@@ -81,6 +82,7 @@ class AtmPlanInfo(ctypes.Structure):
         ("row_variant", ctypes.c_int32),
         ("col_variant", ctypes.c_int32),
         ("tuned", ctypes.c_int32),
+        ("gemm_form", ctypes.c_int32),
     ]
 
 
@@ -132,7 +134,7 @@ SIGNATURES = {
                                      ctypes.c_void_p]),
     "atm_tc_gemm_test": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_void_p,
-                                        ctypes.c_void_p]),
+                                        ctypes.c_int32, ctypes.c_void_p]),
     "atm_vacuum_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
 }

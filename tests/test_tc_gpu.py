@@ -8,8 +8,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("S,M,N,K", [(1, 128, 256, 64), (2, 256, 512, 200), (1, 512, 512, 768)])
-def test_tc_gemm_matches_fp64(S, M, N, K):
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("S,M,N,K", [(1, 128, 256, 64), (2, 256, 512, 200), (1, 512, 512, 768), (3, 2048, 2048, 768)])
+def test_tc_gemm_matches_fp64(S, M, N, K, variant):
+    """Both forms (0: persistent TMA, 1: cp.async per tile), including more
+    tiles than SMs so the persistent loop wraps."""
     import torch
     from pyatmosphere_gb300.engine import _lib
     lib = _lib.load()
@@ -19,7 +22,8 @@ def test_tc_gemm_matches_fp64(S, M, N, K):
     Ad, Bd = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
     out = torch.empty((S, M, N), dtype=torch.float32, device="cuda")
     rc = lib.atm_tc_gemm_test(ctypes.c_void_p(Ad.data_ptr()), ctypes.c_void_p(Bd.data_ptr()), S, M, N, K, 0.5,
-                              ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+                              ctypes.c_void_p(out.data_ptr()), variant,
+                              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == 0, lib.atm_last_error()
     ref = 0.5 * np.einsum("smk,snk->smn", A.astype(np.float64), B.astype(np.float64))
     got = out.cpu().numpy().astype(np.float64)
@@ -84,6 +88,27 @@ def test_tc_channel_4096_matches_oracle():
     res, u = o.simulate(spec, rho, theta, value, return_field=True)
     assert o.rel_l2(field.cpu().numpy()[0], u) < 1e-4
     assert meas[0, 8] == pytest.approx(res[0]["eta_0"], rel=1e-5)
+
+
+def test_tc_forms_agree_on_a_channel():
+    """The persistent TMA form is the default; the cp.async form (flag) gives
+    the same measures to FP32 round-off."""
+    import torch
+    from oracle import atm_oracle as o
+    from pyatmosphere_gb300.engine import EnginePlan, _lib
+    spec = o.ChannelSpec(N=512, delta=3.0 / 512, w0=0.08, length=10e3, count=3, points=512, Cn2=3e-15,
+                         pupil_radius=0.1)
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    sp = [torch.from_numpy(a).cuda() for a in o.draw_spectra(17, range(4), spec.count, base, psd)]
+    pos = o.screen_positions(spec.length, spec.count)
+    tma = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, f_base=base,
+                     pupils=[(0.1,)], batch=4)
+    cpa = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, f_base=base,
+                     pupils=[(0.1,)], batch=4, flags=_lib.FLAG_TC_CPASYNC)
+    assert tma.info["gemm_form"] == 2 and cpa.info["gemm_form"] == 1
+    a, b = tma.run(*sp).cpu().numpy(), cpa.run(*sp).cpu().numpy()
+    np.testing.assert_allclose(a, b, rtol=2e-5, atol=1e-9)
 
 
 def test_simt_gemm_path_still_matches_oracle():
