@@ -102,7 +102,8 @@ typedef struct AtmPlanInfo {
   int32_t launches_per_run;   /* kernel launches of one atm_run (without tracked/field extras) */
   int32_t row_parts;          /* row-pass CTAs per realisation */
   int32_t col_tile;           /* columns per CTA of the column pass */
-  int32_t row_variant;        /* 0: persistent pipelined row pass, 1: one CTA per row block */
+  int32_t row_variant;        /* 0: persistent pipelined row pass, 1: one CTA per row block,
+                                 2: persistent pipelined with one row per CTA */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA form */
@@ -229,13 +230,19 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
 
 /* Times the launch variants of the FFT passes on this plan's own workspace
  * (`batch` realisations, `repeats` timed launches each after one warm-up)
- * and keeps the fastest: row-pass variant, column tile (2..16 columns,
- * at most 512 threads per CTA) and column-pass variant.  Overwrites the
+ * and keeps the fastest: row-pass variant (three forms), column tile
+ * (2..16 columns, at most 512 threads per CTA) and column-pass variant.  Overwrites the
  * plan's field / screen workspace (zeroes) and blocks until the timing
  * launches finish, so it is called outside CUDA-graph capture, before the
  * runs it tunes.  The reference has no tuner: cupy picks cuFFT plans inside
  * the FFT calls of utils.py:42-50 (the boundary item atm_autotune). */
 int atm_autotune(AtmPlan* plan, int32_t batch, int32_t repeats, void* stream);
+
+/* Sets the launch choices atm_autotune makes (row-pass variant 0..2, column
+ * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..1)
+ * by hand.  Launch shapes only: results do not change.  No reference
+ * counterpart. */
+int atm_plan_set_variants(AtmPlan* plan, int32_t row_variant, int32_t col_tile, int32_t col_variant);
 
 /* Launch categories reported by atm_profile_end. */
 #define ATM_KIND_SCREEN_PREP 0

@@ -159,6 +159,7 @@ struct AtmPlan {
   int Kp = 0, kc0 = 0;  // tensor-core layout
   DevBuf ta_hi, ta_lo, tb_hi, tb_lo;
   DevBuf s_int, s_edge;  // chunk sums of the low-frequency block
+  DevBuf gy_t, hx_t;     // 1-D phases in turns, folded into the GEMM output (TMA form)
   atm::TcPlan* tcp = nullptr;  // TMA descriptors of the screen GEMM (null: cp.async form)
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
@@ -470,6 +471,7 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
         (rc = dev_alloc(pl->ht, B * (pl->KH / 2) * sizeof(atm::HighTerm), v)) ||
         (rc = dev_alloc(pl->Py, B * N * sizeof(float2), v)) || (rc = dev_alloc(pl->Px, B * N * sizeof(float2), v)) ||
         (rc = dev_alloc(pl->Gy, B * N * sizeof(double), v)) || (rc = dev_alloc(pl->Hx, B * N * sizeof(double), v)) ||
+        (rc = dev_alloc(pl->gy_t, B * N * sizeof(float), v)) || (rc = dev_alloc(pl->hx_t, B * N * sizeof(float), v)) ||
         (rc = dev_alloc(pl->s_int, B * atm::prep_chunks(pl->P_L) * (pl->D - 1) * (pl->D - 1) * sizeof(float2), v)) ||
         (rc = dev_alloc(pl->s_edge, B * atm::prep_chunks(pl->P_L) * (2 * pl->D - 1) * sizeof(double2), v))) {
       delete pl;
@@ -614,7 +616,14 @@ atm::ScreenArgs screen_args(AtmPlan* pl, const float* rho, const float* theta, c
   return s;
 }
 
-int run_screen(AtmPlan* pl, const atm::ScreenArgs& s, int B, cudaStream_t st) {
+// fold: the GEMM output carries the 1-D phases too (persistent TMA form only);
+// the row pass then multiplies by exp(-2 pi i phi) alone
+bool folds(const AtmPlan* pl) { return pl->tcp != nullptr; }
+
+int run_screen(AtmPlan* pl, atm::ScreenArgs s, int B, bool fold, cudaStream_t st) {
+  fold = fold && folds(pl);
+  s.gy_t = fold ? (float*)pl->gy_t.p : nullptr;
+  s.hx_t = fold ? (float*)pl->hx_t.p : nullptr;
   {
     Prof p(pl, ATM_KIND_SCREEN_PREP, st);
     ATM_CUDA(atm::launch_screen_terms(B, s, st));
@@ -631,7 +640,7 @@ int run_screen(AtmPlan* pl, const atm::ScreenArgs& s, int B, cudaStream_t st) {
     Prof p(pl, ATM_KIND_SCREEN_GEMM, st);
     constexpr float kInv2Pi = 0.15915494309189533577f;  // phi_G in turns
     if (pl->tcp)
-      ATM_CUDA(atm::launch_tc_gemm_tma(pl->tcp, B, (float*)pl->phi.p, kInv2Pi, st));
+      ATM_CUDA(atm::launch_tc_gemm_tma(pl->tcp, B, (float*)pl->phi.p, kInv2Pi, s.gy_t, s.hx_t, st));
     else
       ATM_CUDA(atm::launch_tc_gemm(B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p, (const __half*)pl->ta_lo.p,
                                    (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p, (float*)pl->phi.p, kInv2Pi,
@@ -739,8 +748,9 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
   bool measured = false;
   for (int i = 0; i < n; ++i) {
     atm::ScreenArgs s = screen_args(pl, rho, theta, value, i);
-    if (int rc = run_screen(pl, s, batch, st)) return rc;
-    int flags = (i == 0 ? atm::ROW_GEN : (pl->dz[i] > 0 ? atm::ROW_INV : 0)) | atm::ROW_PHASOR;
+    if (int rc = run_screen(pl, s, batch, true, st)) return rc;
+    int flags = (i == 0 ? atm::ROW_GEN : (pl->dz[i] > 0 ? atm::ROW_INV : 0)) | atm::ROW_PHASOR |
+                (folds(pl) ? atm::ROW_FOLDED : 0);
     const bool next_vac = pl->dz[i + 1] > 0;
     if (next_vac) {
       flags |= atm::ROW_FWD | atm::ROW_STORE;
@@ -804,7 +814,7 @@ int atm_screen(AtmPlan* pl, const float* rho, const float* theta, const void* va
   atm::ScreenArgs s = screen_args(pl, rho, theta, value, screen);
   s.Gy = (double*)pl->Gy.p;
   s.Hx = (double*)pl->Hx.p;
-  if (int rc = run_screen(pl, s, batch, st)) return rc;
+  if (int rc = run_screen(pl, s, batch, false, st)) return rc;
   ATM_CUDA(atm::launch_compose_screen(batch, pl->N, (const double*)pl->Gy.p, (const double*)pl->Hx.p,
                                       (const float*)pl->phi.p, (const float2*)pl->Py.p, (const float2*)pl->Px.p,
                                       phi_out, (float2*)phasor_out, st));
@@ -852,11 +862,12 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   };
   // row pass: a middle screen step (inverse FFT, phasor, forward FFT, store)
   atm::RowArgs ra = row_args(pl, nullptr, nullptr);
-  ra.flags = atm::ROW_INV | atm::ROW_FWD | atm::ROW_STORE | (pl->n > 0 ? atm::ROW_PHASOR : 0);
+  ra.flags = atm::ROW_INV | atm::ROW_FWD | atm::ROW_STORE |
+             (pl->n > 0 ? atm::ROW_PHASOR | (folds(pl) ? atm::ROW_FOLDED : 0) : 0);
   ra.loss = 1.f;
   double best_row = -1.0;
   int row_variant = 0;
-  for (int v = 0; v < 2; ++v) {
+  for (int v = 0; v < 3; ++v) {
     ra.variant = v;
     const double ms = time_it([&] { return atm::launch_row_pass(N, batch, ra, st); });
     if (ms >= 0 && (best_row < 0 || ms < best_row)) {
@@ -891,6 +902,20 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   pl->col_tile = col_tile;
   pl->col_variant = col_variant;
   pl->tuned = 1;
+  return ATM_OK;
+}
+
+int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, int32_t col_variant) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (row_variant < 0 || row_variant > 2) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..2", row_variant);
+  if (col_variant < 0 || col_variant > 1) return fail(ATM_ERR_INVALID, "col_variant %d not in 0..1", col_variant);
+  if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
+    return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);
+  if (col_tile * (pl->N / 16) > 512 || col_tile > pl->N)
+    return fail(ATM_ERR_UNSUPPORTED, "col_tile %d exceeds 512 threads per CTA at N = %d", col_tile, pl->N);
+  pl->row_variant = row_variant;
+  pl->col_tile = col_tile;
+  pl->col_variant = col_variant;
   return ATM_OK;
 }
 

@@ -16,6 +16,7 @@ enum : int {
   ROW_FWD = 8,      // forward row FFT after the multiply
   ROW_STORE = 16,   // write the row back
   ROW_MEAS = 32,    // accumulate the measure partial sums (spatial domain)
+  ROW_FOLDED = 64,  // phi already holds the 1-D phases in turns: the phasor is exp(-2 pi i phi) * loss
 };
 
 constexpr int kMaxPupils = 8;
@@ -50,7 +51,8 @@ struct RowArgs {
   int flags;
   float delta;
   double delta64;
-  int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per row block
+  int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per row block,
+                            // 2: persistent pipeline with one row per CTA (row blocks of several rows otherwise)
 };
 
 struct ColArgs {
@@ -109,6 +111,8 @@ struct ScreenArgs {
   __half* tb_lo;
   int Kp;                   // padded K of the tensor-core layout
   int kc0;                  // first Chebyshev column (2 P_H)
+  float* gy_t;              // [B][N] y-only phase in turns reduced to [-1/2, 1/2] (nullable)
+  float* hx_t;              // [B][N] x-only phase in turns reduced to [-1/2, 1/2] (nullable)
   float2* s_int;            // [B][chunks][(D-1)^2] FP32 chunk sums of the Chebyshev interior
   double2* s_edge;          // [B][chunks][2D-1] FP64 chunk sums of its edge row / column
 };
@@ -171,7 +175,9 @@ struct TcPlan;
 TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                        const __half* b_lo);
 void tc_plan_destroy(TcPlan* p);
-cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, cudaStream_t st);
+// fold_y [S][M] / fold_x [S][Nn] (nullable, turns): added to every output
+cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
+                               const float* fold_x, cudaStream_t st);
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                            const __half* b_lo, float* out, float scale, cudaStream_t st);
 cudaError_t launch_screen_table_tc(int B, const ScreenArgs& a, cudaStream_t st);

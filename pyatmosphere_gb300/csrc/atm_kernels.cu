@@ -176,7 +176,11 @@ row_pass_kernel(RowArgs a) {
     for (int m = 0; m < 16; ++m) v[m] = a.field[rowoff + t + m * T];
   }
   if (flags & ROW_INV) fft_dev<N, 1>(v, sm, t, a.tw);
-  if (flags & ROW_PHASOR) {
+  if ((flags & ROW_PHASOR) && (flags & ROW_FOLDED)) {
+    const float* ph = a.phi + rowoff;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cscale(phasor_turns(ph[t + m * T]), a.loss));
+  } else if (flags & ROW_PHASOR) {
     const float2 py = cscale(a.Py[(size_t)r * N + y], a.loss);
     const float* ph = a.phi + rowoff;
     const float2* px = a.Px + (size_t)r * N;
@@ -205,19 +209,19 @@ row_pass_kernel(RowArgs a) {
 // stage buffer doubles as the FFT exchange area once its rows are in
 // registers.
 // ---------------------------------------------------------------------------
-template <int N>
+template <int N, int ROWS>
 struct RowPipe {
-  static constexpr int ROWS = RowRows<N>::value;
   static constexpr size_t STAGE = (size_t)ROWS * Padded<N>::value * sizeof(float2);
   static constexpr size_t TW = (size_t)Padded<N>::value * sizeof(float2);
   static constexpr size_t SMEM = 2 * STAGE + TW;
 };
 
-template <int N>
-__global__ void __launch_bounds__(RowRows<N>::value * (N / 16))
+// ROWS rows per CTA: RowRows<N> (about 256 threads) or 1 (N/16 threads, so
+// the exchange barriers of a row never wait for another row)
+template <int N, int ROWS>
+__global__ void __launch_bounds__(ROWS * (N / 16), (ROWS * (N / 16) <= 128) ? 4 : ((ROWS * (N / 16) <= 256) ? 2 : 1))
 row_pass_pipe_kernel(RowArgs a, int n_items) {
   constexpr int T = N / 16;
-  constexpr int ROWS = RowRows<N>::value;
   constexpr int P = Padded<N>::value;
   constexpr int NT = ROWS * T;
   constexpr int NRB = N / ROWS;  // row blocks per realisation
@@ -228,8 +232,8 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
   const bool load_field = !(flags & ROW_GEN);
   const bool load_phi = (flags & ROW_PHASOR) != 0;
 
-  auto fbuf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * RowPipe<N>::STAGE); };
-  float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * RowPipe<N>::STAGE);
+  auto fbuf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * RowPipe<N, ROWS>::STAGE); };
+  float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * RowPipe<N, ROWS>::STAGE);
   load_twiddles<N>(tws, a.tw);
   auto prefetch = [&](int item, int s) {
     const int r = item / NRB, y0 = (item - r * NRB) * ROWS;
@@ -276,7 +280,10 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
     }
     __syncthreads();  // the exchange below overwrites the staged rows
     if (flags & ROW_INV) fft_dev<N, 1, 0, 1>(v, sm, t, tws);
-    if (load_phi) {
+    if (load_phi && (flags & ROW_FOLDED)) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cscale(phasor_turns(ph[m]), a.loss));
+    } else if (load_phi) {
       const float2 py = cscale(a.Py[(size_t)r * N + y], a.loss);
       const float2* px = a.Px + (size_t)r * N;
 #pragma unroll
@@ -331,18 +338,17 @@ struct LaunchCache {
   }
 };
 
-template <int N>
+template <int N, int ROWS>
 static cudaError_t row_pipe_launch(int B, const RowArgs& a, cudaStream_t st) {
-  constexpr int ROWS = RowRows<N>::value;
   static LaunchCache cache;
   const int threads = ROWS * (N / 16);
-  const size_t smem = RowPipe<N>::SMEM;
+  const size_t smem = RowPipe<N, ROWS>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(row_pass_pipe_kernel<N>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(row_pass_pipe_kernel<N, ROWS>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / ROWS);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  row_pass_pipe_kernel<N><<<grid, threads, smem, st>>>(a, n_items);
+  row_pass_pipe_kernel<N, ROWS><<<grid, threads, smem, st>>>(a, n_items);
   return cudaGetLastError();
 }
 
@@ -368,7 +374,13 @@ template <int N>
 static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
-  if (field_ok && phi_ok && a.variant == 0) return row_pipe_launch<N>(B, a, st);
+  // the measure partials are laid out per block of RowRows<N> rows: variant 2 falls back to 0 there
+  const int variant = (a.flags & ROW_MEAS) && a.variant == 2 ? 0 : a.variant;
+  if (field_ok && phi_ok && variant == 2) {
+    // one row per CTA only where a row fills at least four warps
+    if constexpr (RowRows<N>::value > 1 && N / 16 >= 128) return row_pipe_launch<N, 1>(B, a, st);
+  }
+  if (field_ok && phi_ok && variant != 1) return row_pipe_launch<N, RowRows<N>::value>(B, a, st);
   return row_plain_launch<N>(B, a, st);
 }
 
@@ -718,6 +730,12 @@ __device__ __forceinline__ float2 phasor_fp64(double g) {
   return make_float2(fmaf(-dh, s, c), -fmaf(dh, c, s));
 }
 
+// FP64 phase -> turns reduced to [-1/2, 1/2], rounded to FP32 (error <= 2^-26 turn)
+__device__ __forceinline__ float reduced_turns(double g) {
+  double t = g * 0.15915494309189533577;
+  return (float)(t - rint(t));
+}
+
 __global__ void __launch_bounds__(kEvalCols) screen_eval_kernel(ScreenArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int r = blockIdx.y, tid = threadIdx.x;
@@ -777,6 +795,8 @@ __global__ void __launch_bounds__(kEvalCols) screen_eval_kernel(ScreenArgs a) {
   }
   a.Py[(size_t)r * N + j] = phasor_fp64(G);
   a.Px[(size_t)r * N + j] = phasor_fp64(H);
+  if (a.gy_t) a.gy_t[(size_t)r * N + j] = reduced_turns(G);
+  if (a.hx_t) a.hx_t[(size_t)r * N + j] = reduced_turns(H);
   if (a.Gy) a.Gy[(size_t)r * N + j] = G;
   if (a.Hx) a.Hx[(size_t)r * N + j] = H;
   if (a.KC == 0) return;  // no low-frequency block: no Chebyshev rows

@@ -14,9 +14,10 @@
 // tc_gemm_tma_kernel (default): persistent, warp-specialised.  Warp 0 loads
 // the four 128-byte-swizzled operand boxes of a K tile with TMA
 // (cp.async.bulk.tensor) into a two-stage ring, running ahead into the next
-// tile while warps 2-5 drain the accumulators (tcgen05.ld, combine, scale,
-// store); warp 1 issues the MMAs of each 128 x 256 output tile.  mbarriers:
-// full / empty per stage, full / empty for the accumulator pair.
+// tile while warps 2-9 drain the accumulators (tcgen05.ld, combine, scale,
+// store, optionally adding 1-D phases fold_y[y] + fold_x[x]); warp 1 issues
+// the MMAs of each 128 x 256 output tile.  mbarriers: full / empty per
+// stage, full / empty for the accumulator pair.
 // tc_gemm_kernel: the first form, one CTA per tile, operands through cp.async
 // by all threads (kept for comparison and as the fallback when the driver
 // offers no tensor-map encoder).
@@ -264,9 +265,9 @@ __global__ void __launch_bounds__(THREADS, 1) tc_gemm_kernel(TcArgs a) {
 // persistent, warp-specialised form: TMA producer, MMA issuer, epilogue warps
 // ---------------------------------------------------------------------------
 constexpr int P_STAGES = 2;
-constexpr int P_THREADS = 192;  // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
+constexpr int P_THREADS = 320;  // warp 0: TMA, warp 1: MMA, warps 2-9: epilogue
 constexpr int P_SMEM = P_STAGES * STAGE + 1024;
-constexpr int EPI_THREADS = 128;
+constexpr int EPI_THREADS = 256;  // two warps per TMEM lane quarter, each draining half of the columns
 
 struct TmaOperands {
   CUtensorMap ah, al, bh, bl;  // [S][rows][Kp] FP16, boxes of 64 (K) x 128 or 256 rows
@@ -320,7 +321,7 @@ __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int
 
 __global__ void __launch_bounds__(P_THREADS, 1)
     tc_gemm_tma_kernel(const __grid_constant__ TmaOperands ops, float* __restrict__ out, int S, int M, int Nn, int Kp,
-                       float scale) {
+                       float scale, const float* __restrict__ fold_y, const float* __restrict__ fold_x) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[P_STAGES], empty_bar[P_STAGES], accf_bar, acce_bar, drain_bar;
   __shared__ uint32_t tmem_holder;
@@ -433,9 +434,10 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       mbar_wait(smem_u32(&drain_bar), 0);
     }
   } else {
-    // ---- epilogue: warps 2-5, TMEM lane quarter (warp % 4) ----
+    // ---- epilogue: warps 2-9; TMEM lane quarter warp % 4, column half (warp - 2) / 4 ----
     const int q = warp & 3;
     const int row = q * 32 + lane;
+    const int cbeg = ((warp - 2) >> 2) * (TN / 2);
     uint32_t aphase = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
       int s, m0, n0;
@@ -447,8 +449,10 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
       float* o = out + ((size_t)s * M + m0 + row) * Nn + n0;
+      const float fy = fold_y ? fold_y[(size_t)s * M + m0 + row] : 0.f;
+      const float* fx = fold_x ? fold_x + (size_t)s * Nn + n0 : nullptr;
 #pragma unroll 1
-      for (int c0 = 0; c0 < TN; c0 += 32) {
+      for (int c0 = cbeg; c0 < cbeg + TN / 2; c0 += 32) {
         uint32_t h[32], l[32];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -467,14 +471,23 @@ __global__ void __launch_bounds__(P_THREADS, 1)
               "=r"(l[24]), "=r"(l[25]), "=r"(l[26]), "=r"(l[27]), "=r"(l[28]), "=r"(l[29]), "=r"(l[30]), "=r"(l[31])
             : "r"(tmem + TN + lane_addr + c0));
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        constexpr float lo_scale = 1.f / kTcLoScale;
+        const float lo_scale = scale / kTcLoScale;
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
+          // the 1-D phases (turns, each in [-1/2, 1/2]) join the product
+          float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (fx) {
+            f = *reinterpret_cast<const float4*>(fx + c0 + j);
+            f.x += fy;
+            f.y += fy;
+            f.z += fy;
+            f.w += fy;
+          }
           float4 v;
-          v.x = (__uint_as_float(h[j + 0]) + __uint_as_float(l[j + 0]) * lo_scale) * scale;
-          v.y = (__uint_as_float(h[j + 1]) + __uint_as_float(l[j + 1]) * lo_scale) * scale;
-          v.z = (__uint_as_float(h[j + 2]) + __uint_as_float(l[j + 2]) * lo_scale) * scale;
-          v.w = (__uint_as_float(h[j + 3]) + __uint_as_float(l[j + 3]) * lo_scale) * scale;
+          v.x = fmaf(__uint_as_float(l[j + 0]), lo_scale, fmaf(__uint_as_float(h[j + 0]), scale, f.x));
+          v.y = fmaf(__uint_as_float(l[j + 1]), lo_scale, fmaf(__uint_as_float(h[j + 1]), scale, f.y));
+          v.z = fmaf(__uint_as_float(l[j + 2]), lo_scale, fmaf(__uint_as_float(h[j + 2]), scale, f.z));
+          v.w = fmaf(__uint_as_float(l[j + 3]), lo_scale, fmaf(__uint_as_float(h[j + 3]), scale, f.w));
           *reinterpret_cast<float4*>(o + c0 + j) = v;
         }
       }
@@ -570,8 +583,10 @@ TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const _
 
 void tc_plan_destroy(TcPlan* p) { delete p; }
 
-cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, cudaStream_t st) {
-  if (!p || S < 1 || S > p->S || !out) return cudaErrorInvalidValue;
+cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
+                               const float* fold_x, cudaStream_t st) {
+  if (!p || S < 1 || S > p->S || !out || (!fold_y) != (!fold_x)) return cudaErrorInvalidValue;
+  if (((uintptr_t)fold_x & 15) != 0) return cudaErrorMisalignedAddress;
   static int sms[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -587,7 +602,7 @@ cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, 
   }
   const int n_tiles = S * (p->M / TM) * (p->Nn / TN);
   const int grid = std::min(n_tiles, sms[dev]);
-  tc_gemm_tma_kernel<<<grid, P_THREADS, P_SMEM, st>>>(p->ops, out, S, p->M, p->Nn, p->Kp, scale);
+  tc_gemm_tma_kernel<<<grid, P_THREADS, P_SMEM, st>>>(p->ops, out, S, p->M, p->Nn, p->Kp, scale, fold_y, fold_x);
   return cudaGetLastError();
 }
 
@@ -663,7 +678,7 @@ extern "C" int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32
     if (!tp) e = cudaErrorNotSupported;
   }
   if (e == cudaSuccess)
-    e = variant == 0 ? atm::launch_tc_gemm_tma(tp, S, out, scale, st)
+    e = variant == 0 ? atm::launch_tc_gemm_tma(tp, S, out, scale, nullptr, nullptr, st)
                      : atm::launch_tc_gemm(S, M, N, Kp, ah, al, bh, bl, out, scale, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   int flag = 0;

@@ -121,6 +121,11 @@ class EnginePlan:
         self._refresh_info()
         return {k: self.info[k] for k in ("col_tile", "row_variant", "col_variant", "tuned")}
 
+    def set_variants(self, row_variant: int, col_tile: int, col_variant: int):
+        """Launch choices by hand (atm_plan_set_variants); results do not change."""
+        check(self.lib.atm_plan_set_variants(self._handle, int(row_variant), int(col_tile), int(col_variant)))
+        self._refresh_info()
+
     def draw_spectra(self, seed, first, sqrt_psd, rho, theta, value):
         """Seeded spectra on the device (atm_draw_spectra) into the given tensors."""
         batch = int(rho.shape[0])

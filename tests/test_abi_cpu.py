@@ -47,6 +47,7 @@ def test_plan_create_rejects_bad_descriptors_without_gpu(built):
     d.resolution, d.abi_version = 256, 7
     assert lib.atm_plan_create(ctypes.byref(d), ctypes.byref(h)) == -1
     assert lib.atm_autotune(None, 1, 1, None) == -1
+    assert lib.atm_plan_set_variants(None, 0, 4, 0) == -1
     assert b"NULL" in lib.atm_last_error()
 
 

@@ -223,9 +223,14 @@ def test_autotune_keeps_results(torch_cuda, N):
     choice = plan.autotune(repeats=2)
     assert choice["tuned"] == 1
     assert choice["col_tile"] in (2, 4, 8, 16) and choice["col_tile"] * N // 16 <= 512
-    assert choice["row_variant"] in (0, 1) and choice["col_variant"] in (0, 1)
+    assert choice["row_variant"] in (0, 1, 2) and choice["col_variant"] in (0, 1)
     after = plan.run(*sp).cpu().numpy()
     np.testing.assert_array_equal(after, before)
-    # every column tile computes the same arithmetic
-    plan2, _ = make_plan(spec, batch=3, col_tile=2)
-    np.testing.assert_array_equal(plan2.run(*sp).cpu().numpy(), before)
+    # every launch form computes the same arithmetic
+    for rv in (0, 1, 2):
+        for ct in (2, 4, 8, 16):
+            if ct * N // 16 > 512:
+                continue
+            for cv in (0, 1):
+                plan.set_variants(rv, ct, cv)
+                np.testing.assert_array_equal(plan.run(*sp).cpu().numpy(), before, err_msg=f"{rv} {ct} {cv}")

@@ -108,7 +108,11 @@ def test_tc_forms_agree_on_a_channel():
                      pupils=[(0.1,)], batch=4, flags=_lib.FLAG_TC_CPASYNC)
     assert tma.info["gemm_form"] == 2 and cpa.info["gemm_form"] == 1
     a, b = tma.run(*sp).cpu().numpy(), cpa.run(*sp).cpu().numpy()
-    np.testing.assert_allclose(a, b, rtol=2e-5, atol=1e-9)
+    # the TMA form also folds the 1-D phases into the GEMM output (one FP32
+    # rounding more): integrated measures to 2e-5, the one-pixel intensity to 1e-4
+    cols = [c for c in range(a.shape[1]) if c != _lib.OUT_I_CENTER]
+    np.testing.assert_allclose(a[:, cols], b[:, cols], rtol=2e-5, atol=1e-9)
+    np.testing.assert_allclose(a[:, _lib.OUT_I_CENTER], b[:, _lib.OUT_I_CENTER], rtol=1e-4)
 
 
 def test_simt_gemm_path_still_matches_oracle():
