@@ -52,7 +52,16 @@ extern "C" {
 #define ATM_FLAG_TC_GEMM 2       /* screen GEMM on tcgen05 tensor cores (the default for N >= 256) */
 #define ATM_FLAG_TC_CPASYNC 4    /* tensor-core GEMM in its one-CTA-per-tile cp.async form instead of the
                                     persistent TMA form */
+#define ATM_FLAG_STEP_MEASURES 8 /* also measure the field just after every screen (per-step measures) */
 
+/* per-realisation doubles in measures_out (slot index).  With
+ * ATM_FLAG_STEP_MEASURES, ATM_STEP_SLOTS more doubles per screen i follow the
+ * pupil and tracked slots, at ATM_OUT_PUPIL0 + n_pupils + n_tracked +
+ * i * ATM_STEP_SLOTS: slots 0..7 below (eta_total .. I_center) of the field
+ * just after screen i, the value PhaseScreensPath.generator yields
+ * (pathes.py:61-75) and SIResult / BeamPropagationResult measure
+ * (simulations/si.py:11-48, simulations/beam.py:83-114). */
+#define ATM_STEP_SLOTS 8
 /* per-realisation doubles in measures_out (slot index) */
 #define ATM_OUT_ETA_TOTAL 0      /* measures.eta(pupil=False)      measures.py:7-8   */
 #define ATM_OUT_MEAN_X 1         /* measures.mean_x                measures.py:11-13 */

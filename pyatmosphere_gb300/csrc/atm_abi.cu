@@ -160,6 +160,9 @@ struct AtmPlan {
   DevBuf ta_hi, ta_lo, tb_hi, tb_lo;
   DevBuf s_int, s_edge;  // chunk sums of the low-frequency block
   DevBuf gy_t, hx_t;     // 1-D phases in turns, folded into the GEMM output (TMA form)
+  DevBuf step_partials, step_center;  // per-step measures (ATM_FLAG_STEP_MEASURES)
+  bool step_meas = false;
+  int step_slot0 = 0;
   atm::TcPlan* tcp = nullptr;  // TMA descriptors of the screen GEMM (null: cp.async form)
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
@@ -427,6 +430,9 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   pl->n_parts = pl->N / pl->rows;
   pl->n_meas = 6 + pl->n_pupils;
   pl->n_out = ATM_OUT_PUPIL0 + pl->n_pupils + pl->n_tracked;
+  pl->step_meas = pl->n > 0 && (d->flags & ATM_FLAG_STEP_MEASURES);
+  pl->step_slot0 = pl->n_out;
+  if (pl->step_meas) pl->n_out += ATM_STEP_SLOTS * pl->n;
 
   const size_t N = pl->N, B = pl->B, K = pl->KH + pl->KC;
   const size_t plane = N * N;
@@ -441,7 +447,9 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
       (rc = dev_alloc(pl->center, B * sizeof(float), v)) ||
       (rc = dev_alloc(pl->pupil_rows, (size_t)pl->n_pupils * N * sizeof(int2), v)) ||
       (rc = dev_alloc(pl->tracked_r, (size_t)pl->n_tracked * sizeof(double), v)) ||
-      (rc = dev_alloc(pl->intensity, pl->n_tracked > 0 ? B * plane * sizeof(float) : 0, v))) {
+      (rc = dev_alloc(pl->intensity, pl->n_tracked > 0 ? B * plane * sizeof(float) : 0, v)) ||
+      (rc = dev_alloc(pl->step_partials, pl->step_meas ? (size_t)pl->n * B * pl->n_parts * 6 * sizeof(double) : 0, v)) ||
+      (rc = dev_alloc(pl->step_center, pl->step_meas ? (size_t)pl->n * B * sizeof(float) : 0, v))) {
     delete pl;
     return rc;
   }
@@ -546,7 +554,7 @@ int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
   // per screen: terms, eval, table, GEMM, row pass (+ column pass)
   for (int i = 0; i < pl->n; ++i) launches += 5 + (pl->dz[i + 1] > 0 ? 1 : 0);
   launches += (pl->n == 0 || pl->dz[pl->n] > 0) ? 1 : 0;
-  launches += 1;  // finalize
+  launches += 1 + (pl->step_meas ? pl->n : 0);  // finalize (+ one per step)
   info->launches_per_run = launches;
   info->row_parts = pl->n_parts;
   info->col_tile = pl->col_tile;
@@ -760,6 +768,11 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
     } else {
       flags |= atm::ROW_STORE;
     }
+    if (pl->step_meas) {
+      flags |= atm::ROW_STEP;
+      ra.step_partials = (double*)pl->step_partials.p + (size_t)i * pl->B * pl->n_parts * 6;
+      ra.step_center = (float*)pl->step_center.p + (size_t)i * pl->B;
+    }
     ra.flags = flags;
     ra.loss = pl->loss[i] * ((i == n - 1 && !next_vac) ? pl->final_loss : 1.f);
     ra.store_out = (flags & atm::ROW_MEAS) ? 1 : 0;
@@ -782,7 +795,21 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
     Prof p(pl, ATM_KIND_ROW_PASS, st);
     ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
   }
-  return finish_measures(pl, batch, measures, st);
+  if (int rc = finish_measures(pl, batch, measures, st)) return rc;
+  for (int i = 0; pl->step_meas && i < n; ++i) {
+    atm::FinalArgs fa{};
+    fa.partials = (const double*)pl->step_partials.p + (size_t)i * pl->B * pl->n_parts * 6;
+    fa.center = (const float*)pl->step_center.p + (size_t)i * pl->B;
+    fa.out = measures + pl->step_slot0 + (size_t)i * ATM_STEP_SLOTS;
+    fa.n_parts = pl->n_parts;
+    fa.n_meas = 6;
+    fa.n_out = pl->n_out;
+    fa.n_pupils = 0;
+    fa.delta = pl->delta;
+    Prof p(pl, ATM_KIND_FINALIZE, st);
+    ATM_CUDA(atm::launch_finalize(batch, fa, st));
+  }
+  return ATM_OK;
 }
 
 int atm_measures(AtmPlan* pl, const void* field, int32_t batch, double* measures, void* stream) {

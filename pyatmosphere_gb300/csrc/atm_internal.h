@@ -17,6 +17,7 @@ enum : int {
   ROW_STORE = 16,   // write the row back
   ROW_MEAS = 32,    // accumulate the measure partial sums (spatial domain)
   ROW_FOLDED = 64,  // phi already holds the 1-D phases in turns: the phasor is exp(-2 pi i phi) * loss
+  ROW_STEP = 128,   // measure partial sums of the field just after the screen (per-step measures)
 };
 
 constexpr int kMaxPupils = 8;
@@ -51,6 +52,8 @@ struct RowArgs {
   int flags;
   float delta;
   double delta64;
+  double* step_partials;    // [B][gridDim.x][6] partials of the post-screen field (ROW_STEP)
+  float* step_center;       // [B] post-screen intensity at the grid origin (ROW_STEP)
   int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per row block,
                             // 2: persistent pipeline with one row per CTA (row blocks of several rows otherwise)
 };

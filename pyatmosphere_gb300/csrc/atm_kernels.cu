@@ -148,6 +148,21 @@ __device__ __forceinline__ void measure_row(const RowArgs& a, const float2 (&v)[
   __syncthreads();  // red[] is reused by the next row of a persistent CTA
 }
 
+// measures of the field just after a screen: the moments and the centre
+// intensity, into the per-step buffers
+template <int N, int ROWS>
+__device__ __forceinline__ void measure_step(const RowArgs& a, const float2 (&v)[16], int t, int y, int r, int part,
+                                             int n_parts) {
+  RowArgs b = a;
+  b.partials = a.step_partials;
+  b.center = a.step_center;
+  b.n_pupils = 0;
+  b.n_meas = 6;
+  b.mean_I = nullptr;
+  b.intensity = nullptr;
+  measure_row<N, ROWS>(b, v, t, y, r, part, n_parts);
+}
+
 // ---------------------------------------------------------------------------
 // row pass
 // ---------------------------------------------------------------------------
@@ -193,6 +208,7 @@ row_pass_kernel(RowArgs a) {
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = cscale(v[m], a.loss);
   }
+  if (flags & ROW_STEP) measure_step<N, ROWS>(a, v, t, y, r, blockIdx.x, gridDim.x);
   if (flags & ROW_FWD) fft_dev<N, -1>(v, sm, t, a.tw);
   if (flags & ROW_STORE) {
     float2* dst = (a.store_out && a.out) ? a.out : a.field;
@@ -295,6 +311,7 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cscale(v[m], a.loss);
     }
+    if (flags & ROW_STEP) measure_step<N, ROWS>(a, v, t, y, r, rb, NRB);
     if (flags & ROW_FWD) fft_dev<N, -1, 0, 1>(v, sm, t, tws);
     if (flags & ROW_STORE) {
       float2* dst = (a.store_out && a.out) ? a.out : a.field;
@@ -374,8 +391,8 @@ template <int N>
 static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
-  // the measure partials are laid out per block of RowRows<N> rows: variant 2 falls back to 0 there
-  const int variant = (a.flags & ROW_MEAS) && a.variant == 2 ? 0 : a.variant;
+  // measure partials are laid out per block of RowRows<N> rows: variant 2 falls back to 0 there
+  const int variant = (a.flags & (ROW_MEAS | ROW_STEP)) && a.variant == 2 ? 0 : a.variant;
   if (field_ok && phi_ok && variant == 2) {
     // one row per CTA only where a row fills at least four warps
     if constexpr (RowRows<N>::value > 1 && N / 16 >= 128) return row_pipe_launch<N, 1>(B, a, st);

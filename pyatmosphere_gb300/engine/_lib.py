@@ -20,6 +20,8 @@ MAX_PUPILS = 8
 FLAG_SIMT_GEMM = 1
 FLAG_TC_GEMM = 2
 FLAG_TC_CPASYNC = 4
+FLAG_STEP_MEASURES = 8
+STEP_SLOTS = 8
 SOURCE_GAUSSIAN = 0
 SOURCE_PLANE = 1
 

@@ -59,6 +59,7 @@ class EnginePlan:
         self._handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             check(self.lib.atm_plan_create(ctypes.byref(d), ctypes.byref(self._handle)))
+        self._geometry = (wvl, w0, F0, list(positions), length, list(pupils))
         self._refresh_info()
         self.n_out = self.info["n_out"]
 
@@ -112,6 +113,17 @@ class EnginePlan:
         with torch.cuda.device(self.device):
             check(self.lib.atm_plan_update(self._handle, ctypes.byref(d)))
         self.n_screens = len(positions)
+        self._geometry = (wvl, w0, F0, list(positions), length, list(pupils))
+
+    def set_shift(self, shift):
+        """Moves every screen by `shift` (x, y) metres (atm_plan_update with the
+        plan's geometry), as generate_phase_screen(shift=...) does."""
+        shift = (float(shift[0]), float(shift[1]))
+        if shift == self._kw["shift"]:
+            return
+        self._kw["shift"] = shift
+        wvl, w0, F0, positions, length, pupils = self._geometry
+        self.update(wvl, w0, F0, positions, length, pupils)
 
     def autotune(self, batch: Optional[int] = None, repeats: int = 3) -> dict:
         """Times the FFT-pass launch variants on the plan's workspace

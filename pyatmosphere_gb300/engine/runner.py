@@ -12,6 +12,7 @@ from typing import List, Sequence, Tuple
 import numpy as np
 
 from .. import gpu
+from . import _lib
 
 
 def _path_geometry(channel):
@@ -42,7 +43,7 @@ def _source(channel):
 
 
 def get_plan(channel, batch: int = 1, pupils: Sequence[tuple] = (), tracked: Sequence[float] = (),
-             shift=(0.0, 0.0), path_output_loss: bool = False, length=None):
+             shift=(0.0, 0.0), path_output_loss: bool = False, length=None, step_measures: bool = False):
     from .plan import EnginePlan
     gpu.require_engine()
     positions, L, losses, base = _path_geometry(channel)
@@ -53,7 +54,7 @@ def get_plan(channel, batch: int = 1, pupils: Sequence[tuple] = (), tracked: Seq
     key = (N, delta, kind, wvl, w0, F0, tuple(positions), L, losses,
            None if base is None else base.tobytes(), int(batch), tuple(map(tuple, pupils)), tuple(tracked),
            (float(shift[0]), float(shift[1])), bool(path_output_loss), gpu.config.get("cheb_cut", 0.0),
-           str(gpu.device()))
+           str(gpu.device()), bool(step_measures))
     cache = channel.__dict__.setdefault("_atm_plans", {})
     plan = cache.get(key)
     if plan is None:
@@ -64,7 +65,7 @@ def get_plan(channel, batch: int = 1, pupils: Sequence[tuple] = (), tracked: Seq
         plan = EnginePlan(N, delta, wvl, w0, F0, positions, L, f_base=base, losses_db=losses,
                           path_output_loss=path_output_loss, shift=shift, pupils=pupils, tracked=tracked,
                           batch=batch, source=kind, cheb_cut=gpu.config.get("cheb_cut", 0.0),
-                          device=gpu.device())
+                          device=gpu.device(), flags=_lib.FLAG_STEP_MEASURES if step_measures else 0)
         cache[key] = plan
     return plan
 

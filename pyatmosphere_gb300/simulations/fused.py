@@ -44,10 +44,42 @@ def classify(channel, mtype, ops):
         return None
     if mtype == "pupil" and len(ops) == 1 and ops[0] is M.eta and channel.pupil is not None:
         return ("pupil", (float(channel.pupil.radius), 0.0, 0.0))
+    if mtype == "propagation" and len(ops) == 1 and len(getattr(channel.path, "phase_screens", ())) > 0:
+        # after every screen and at the receiver (the engine's per-step measures)
+        from .si import intensity_at_center
+        op = ops[0]
+        if op is intensity_at_center:
+            return ("step", _lib.OUT_I_CENTER)
+        if op in _MOMENT:
+            return ("step", _MOMENT[op])
+        if op is M.eta:
+            return ("step", _lib.OUT_ETA_TOTAL)
+        if op is M.mean_r:
+            return ("step_mean_r",)
+        if op is M.mean_r2:
+            return ("step_mean_r2",)
     return None
 
 
-def resolve(kind, out, pupils, tracked):
+def _steps(out, base, n, slots):
+    """[R][n + 1] values of the given slots: after each screen, then at the receiver."""
+    import numpy as np
+    cols = [out[:, [base + i * _lib.STEP_SLOTS + s for s in slots]] for i in range(n)] + [out[:, slots]]
+    return np.stack(cols, axis=1)
+
+
+def resolve(kind, out, pupils, tracked, n_screens=0):
+    """Per-realisation values of one measure: [R] (or [R][n + 1] for the
+    per-step kinds) from atm_run's output rows."""
+    base = _lib.OUT_PUPIL0 + len(pupils) + len(tracked)
+    if kind[0] == "step":
+        return _steps(out, base, n_screens, [kind[1]])[:, :, 0]
+    if kind[0] == "step_mean_r":
+        v = _steps(out, base, n_screens, [_lib.OUT_MEAN_X, _lib.OUT_MEAN_Y])
+        return (v[:, :, 0] ** 2 + v[:, :, 1] ** 2) ** 0.5
+    if kind[0] == "step_mean_r2":
+        v = _steps(out, base, n_screens, [_lib.OUT_MEAN_X2, _lib.OUT_MEAN_Y2])
+        return v[:, :, 0] + v[:, :, 1]
     if kind[0] == "slot":
         return out[:, kind[1]]
     if kind[0] == "mean_r":

@@ -3,9 +3,11 @@
 ``Simulation.iter`` keeps the reference's per-realisation semantics
 (channel -> time -> measure type -> operation chain).  ``Simulation.run``
 first tries the batched engine path: when every measure of every channel is
-one the engine computes in its fused reduction (Beam moments, mean_x2_r,
-eta through fixed or centroid-tracked CirclePupils, total eta), it runs
-``gpu.config['batch']`` realisations per engine call and appends their
+one the engine computes in its fused reductions (Beam moments, mean_x2_r,
+eta through fixed or centroid-tracked CirclePupils, total eta, and the same
+quantities after every screen for "propagation" measures such as SIResult
+and BeamPropagationResult), it runs ``gpu.config['batch']`` realisations per
+engine call, once per time shift of the wind measures, and appends their
 scalars; otherwise it falls back to ``iter`` (engine propagation, one
 realisation at a time).  Spectra are drawn from numpy's global RNG in the
 same order as the reference (realisation by realisation, channel by
@@ -111,22 +113,21 @@ class Simulation:
     # batched engine path
     # ------------------------------------------------------------------
     def _batch_plan(self):
-        """Per channel: (measures, slot resolver, pupils, tracked) or None if
+        """Per channel: [(measure, fused kind, time tuple or None)], or None if
         some measure is outside what the engine fuses."""
         from .fused import classify
         plans = {}
         for channel, by_time in self.measures.items():
-            if list(by_time.keys()) != [None]:
-                return None
-            entries = []
-            for mtype, by_ops in by_time[None].items():
-                for ops, ms in by_ops.items():
-                    kind = classify(channel, mtype, ops)
-                    if kind is None:
-                        return None
-                    entries += [(m, kind) for m in ms]
             if not getattr(channel, "_fused_ok", lambda: False)():
                 return None
+            entries = []
+            for time, by_type in by_time.items():
+                for mtype, by_ops in by_type.items():
+                    for ops, ms in by_ops.items():
+                        kind = classify(channel, mtype, ops)
+                        if kind is None:
+                            return None
+                        entries += [(m, kind, time) for m in ms]
             plans[channel] = entries
         return plans
 
@@ -135,33 +136,49 @@ class Simulation:
         from ..engine.runner import draw_channel_spectra, get_plan, to_device
         from .fused import resolve
         batch = int(gpu.config.get("batch", 256))
-        remaining = max(m.max_size - len(m) for ms in plans.values() for m, _ in ms
-                        if m.max_size is not None and not m.is_done) if any(
-            m.max_size is not None for ms in plans.values() for m, _ in ms) else batch
-        R = max(1, min(batch, remaining))
-        spectra = {}
+        live = [m for ms in plans.values() for m, _, _ in ms if not m.is_done]
+        sized = [m.max_size - len(m) for m in live if m.max_size is not None]
+        R = max(1, min(batch, max(sized) if sized else batch))
         chans = list(plans)
         for c in chans:
             c.path.init_phase_screens()
-        # reference RNG order: realisation, then channel, then screen
+        # reference RNG order: realisation, then channel, then screen; one
+        # spectrum per realisation serves every time shift (wind cache)
         per = {c: [] for c in chans}
         for _ in range(R):
             for c in chans:
                 per[c].append(draw_channel_spectra(c, 1, wind=True, clear=True))
-        for c in chans:
-            spectra[c] = [np.concatenate([p[k] for p in per[c]]) for k in range(3)]
         for c, entries in plans.items():
-            pupils = sorted({k[1] for _, k in entries if k[0] == "pupil"})
-            tracked = sorted({k[1][0] for _, k in entries if k[0] == "tracked"})
-            plan = get_plan(c, batch=batch, pupils=pupils, tracked=tracked, path_output_loss=False)
-            out = plan.run(*to_device(*spectra[c])).cpu().numpy()
-            for m, kind in entries:
-                vals = resolve(kind, out, pupils, tracked)
+            spectra = [np.concatenate([p[k] for p in per[c]]) for k in range(3)]
+            pupils = sorted({k[1] for _, k, _ in entries if k[0] == "pupil"})
+            tracked = sorted({k[1][0] for _, k, _ in entries if k[0] == "tracked"})
+            steps = any(k[0].startswith("step") for _, k, _ in entries)
+            plan = get_plan(c, batch=batch, pupils=pupils, tracked=tracked, path_output_loss=False,
+                            step_measures=steps)
+            dev = to_device(*spectra)
+            # screens move by (0, t) for each time value (Simulation.iter's shift=(0, time))
+            shifts = sorted({float(t or 0) for _, _, T in entries for t in (T or (0,))})
+            outs = {}
+            try:
+                for t in shifts:
+                    plan.set_shift((0.0, t))
+                    outs[t] = plan.run(*dev).cpu().numpy()
+            finally:
+                plan.set_shift((0.0, 0.0))
+            n = plan.n_screens
+            for m, kind, T in entries:
+                if T is None:
+                    vals = resolve(kind, outs[0.0], pupils, tracked, n)
+                    rows = [vals[r] for r in range(R)]
+                else:
+                    vs = [resolve(kind, outs[float(t or 0)], pupils, tracked, n) for t in T]
+                    rows = [[v[r] for v in vs] for r in range(R)]
                 for r in range(R):
                     if m.is_done:
                         break
-                    m.data.append(float(vals[r]))
-                    m.iteration_data = float(vals[r])
+                    val = np.asarray(rows[r], dtype=float).tolist()
+                    m.data.append(val)
+                    m.iteration_data = val
         return R
 
     def run(self, *args, plot_step: int = None, save_step: int = None, **kwargs):

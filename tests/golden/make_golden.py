@@ -232,6 +232,23 @@ def main(ref_path):
     g["seeded_sim_eta"] = np.array(pdt.measures[0].data)
     g["seeded_sim_tracked_eta"] = np.array(tpdt.measures[2].data)
 
+    # 9. seeded wind (time-shifted screens) and per-step ("propagation") results
+    np.random.seed(555)
+    ch = make_channel(pa, **spec_kwargs(spec))
+    times = [0.0, 0.02, 0.05]
+    tc = simulations.TimeCoherenceResult(ch, times, max_size=4)
+    bwc = simulations.TimeBWcorrSimulation(ch, times, max_size=4)
+    simulations.Simulation([tc, bwc]).run()
+    g["wind_times"] = np.array(times)
+    g["wind_eta"] = np.array(tc.measures[0].data)
+    g["wind_mean_x"] = np.array(bwc.measures[0].data)
+    g["wind_mean_y"] = np.array(bwc.measures[1].data)
+    np.random.seed(777)
+    ch = make_channel(pa, **spec_kwargs(spec))
+    si = simulations.SIResult(ch, max_size=4)
+    simulations.Simulation([si]).run()
+    g["si_center"] = np.array(si.measures[0].data, dtype=float)
+
     out = os.path.join(HERE, "golden.npz")
     np.savez_compressed(out, **{k: np.asarray(v) for k, v in g.items()})
     print("wrote", out, os.path.getsize(out), "bytes")

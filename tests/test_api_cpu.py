@@ -67,9 +67,33 @@ def test_batched_path_classification():
     sim = simulations.Simulation([simulations.BeamResult(ch, max_size=2), simulations.PDTResult(ch, max_size=2),
                                   simulations.TrackedPDTResult(ch, max_size=2)])
     plans = sim._batch_plan()
-    kinds = sorted({k[0] for _, k in plans[ch]})
+    kinds = sorted({k[0] for _, k, _ in plans[ch]})
     assert kinds == ["pupil", "slot", "tracked"]
     sim2 = simulations.Simulation(measures_list=[simulations.Measure(ch, "atmosphere", lambda c, output: 0.0)])
     assert sim2._batch_plan() is None
-    sim3 = simulations.Simulation(measures_list=[simulations.Measure(ch, "pupil", measures.eta, time=[0, 1])])
-    assert sim3._batch_plan() is None
+    # wind (time-shifted) and per-step measures are fused too; screen statistics are not
+    sim3 = simulations.Simulation([simulations.TimeCoherenceResult(ch, [0, 1], max_size=2),
+                                   simulations.SIResult(ch, max_size=2),
+                                   simulations.BeamPropagationResult(ch, max_size=2)])
+    plans3 = sim3._batch_plan()
+    assert sorted({(k[0], t) for _, k, t in plans3[ch]}) == [("pupil", (0, 1)), ("step", None),
+                                                              ("step_mean_r", None), ("step_mean_r2", None)]
+    sim4 = simulations.Simulation([simulations.StructureFunctionResult(ch, max_size=2)])
+    assert sim4._batch_plan() is None
+
+
+def test_step_values_resolve_to_screens_then_receiver():
+    from pyatmosphere_gb300.engine import _lib
+    from pyatmosphere_gb300.simulations.fused import resolve
+    n, pupils = 3, [(0.1, 0.0, 0.0)]
+    base = _lib.OUT_PUPIL0 + 1
+    out = np.zeros((2, base + _lib.STEP_SLOTS * n))
+    out[:, _lib.OUT_I_CENTER] = [7.0, 8.0]
+    for i in range(n):
+        out[:, base + i * _lib.STEP_SLOTS + _lib.OUT_I_CENTER] = [i, 10 + i]
+        out[:, base + i * _lib.STEP_SLOTS + _lib.OUT_MEAN_X] = 3.0
+        out[:, base + i * _lib.STEP_SLOTS + _lib.OUT_MEAN_Y] = 4.0
+    v = resolve(("step", _lib.OUT_I_CENTER), out, pupils, [], n)
+    assert v.tolist() == [[0, 1, 2, 7], [10, 11, 12, 8]]
+    r = resolve(("step_mean_r",), out, pupils, [], n)
+    assert r[:, :3].tolist() == [[5.0] * 3] * 2 and r[:, 3].tolist() == [0.0, 0.0]

@@ -150,3 +150,64 @@ def test_fft_screen_channel_conserves_energy():
     np.random.seed(1)
     u = ch.run(pupil=False)
     assert measures.eta(ch, output=u) == pytest.approx(1.0, abs=2e-5)
+
+
+def test_seeded_wind_results_reproduce_reference(golden):
+    """TimeCoherenceResult / TimeBWcorrSimulation (time-shifted screens, one
+    spectrum per realisation) on the batched engine path."""
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import simulations
+    np.random.seed(555)
+    ch = small_channel(pa)
+    times = list(golden["wind_times"])
+    tc = simulations.TimeCoherenceResult(ch, times, max_size=4)
+    bwc = simulations.TimeBWcorrSimulation(ch, times, max_size=4)
+    sim = simulations.Simulation([tc, bwc])
+    assert sim._batch_plan() is not None, "wind measures must take the batched path"
+    sim.run()
+    np.testing.assert_allclose(np.array(tc.measures[0].data), golden["wind_eta"], rtol=1e-3)
+    np.testing.assert_allclose(np.array(bwc.measures[0].data), golden["wind_mean_x"], rtol=2e-2, atol=2e-5)
+    np.testing.assert_allclose(np.array(bwc.measures[1].data), golden["wind_mean_y"], rtol=2e-2, atol=2e-5)
+    assert len(tc.tc) == 3 and tc.tc[0] == pytest.approx(1.0)
+
+
+def test_seeded_si_result_reproduces_reference(golden):
+    """SIResult: on-axis intensity after every screen and at the receiver,
+    from the engine's per-step measures."""
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import simulations
+    np.random.seed(777)
+    ch = small_channel(pa)
+    si = simulations.SIResult(ch, max_size=4)
+    sim = simulations.Simulation([si])
+    assert sim._batch_plan() is not None, "SIResult must take the batched path"
+    sim.run()
+    got = np.array(si.measures[0].data, float)
+    assert got.shape == golden["si_center"].shape == (4, 4)
+    # one pixel of a speckled field: the reference's FP32 screens move it by ~1e-3
+    np.testing.assert_allclose(got, golden["si_center"], rtol=5e-3)
+
+
+def test_batched_propagation_and_wind_equal_per_realisation_path():
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import gpu, simulations
+    results = []
+    for batched in (True, False):
+        np.random.seed(21)
+        ch = small_channel(pa)
+        bp = simulations.BeamPropagationResult(ch, max_size=3)
+        si = simulations.SIResult(ch, max_size=3)
+        tc = simulations.TimeCoherenceResult(ch, [0.0, 0.03], max_size=3)
+        sim = simulations.Simulation([bp, si, tc])
+        if batched:
+            gpu.config["batch"] = 2
+            sim.run()
+        else:
+            while not sim.is_measures_done():
+                sim.iter()
+        results.append([np.array(m.data, float) for m in (bp.measures[0], bp.measures[1], si.measures[0],
+                                                           tc.measures[0])])
+    gpu.config["batch"] = 256
+    for a, b in zip(*results):
+        assert a.shape == b.shape
+        np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-9)

@@ -234,3 +234,57 @@ def test_autotune_keeps_results(torch_cuda, N):
             for cv in (0, 1):
                 plan.set_variants(rv, ct, cv)
                 np.testing.assert_array_equal(plan.run(*sp).cpu().numpy(), before, err_msg=f"{rv} {ct} {cv}")
+
+
+def test_step_measures_match_oracle(torch_cuda):
+    """ATM_FLAG_STEP_MEASURES: moments and centre intensity of the field just
+    after every screen (the reference generator's yields) against FP64."""
+    torch = torch_cuda
+    from pyatmosphere_gb300.engine import _lib
+    spec = o.ChannelSpec(N=256, delta=4e-3, w0=0.08, length=8e3, count=3, points=256, Cn2=2e-15, pupil_radius=0.1)
+    plan, base = make_plan(spec, batch=2, flags=_lib.FLAG_STEP_MEASURES)
+    assert plan.n_out == _lib.OUT_PUPIL0 + 1 + _lib.STEP_SLOTS * 3
+    rho, theta, value = spectra(spec, base, seed=13, R=2)
+    out = plan.run(*to_dev(torch, rho, theta, value)).cpu().numpy()
+    positions = o.screen_positions(spec.length, spec.count, spec.position)
+    u0 = o.gaussian_source(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0)
+    base_slot = _lib.OUT_PUPIL0 + 1
+    for r in range(2):
+        screens = [o.ss_screen(rho[r, i], theta[r, i], value[r, i], spec.N, spec.delta) for i in range(3)]
+        u, steps = o.propagate(u0, screens, positions, spec.length, spec.k, spec.delta, path_output_loss=False,
+                               keep_steps=True)
+        ref_final = o.measures(u, spec.delta, [0.1])
+        assert out[r, _lib.OUT_ETA_TOTAL] == pytest.approx(ref_final["eta_total"], rel=1e-5)
+        for i, ui in enumerate(steps):
+            ref = o.measures(ui, spec.delta)
+            blk = out[r, base_slot + i * _lib.STEP_SLOTS: base_slot + (i + 1) * _lib.STEP_SLOTS]
+            assert blk[_lib.OUT_ETA_TOTAL] == pytest.approx(ref["eta_total"], rel=1e-5)
+            assert blk[_lib.OUT_MEAN_X2] == pytest.approx(ref["mean_x2"], rel=1e-4)
+            assert blk[_lib.OUT_MEAN_Y2] == pytest.approx(ref["mean_y2"], rel=1e-4)
+            assert blk[_lib.OUT_MEAN_X] == pytest.approx(ref["mean_x"], rel=1e-3, abs=1e-7)
+            c = spec.N // 2
+            assert blk[_lib.OUT_I_CENTER] == pytest.approx(abs(ui[c, c]) ** 2, rel=1e-4)
+    # the final measures do not depend on the flag
+    plain, _ = make_plan(spec, batch=2)
+    np.testing.assert_array_equal(plain.run(*to_dev(torch, rho, theta, value)).cpu().numpy(),
+                                  out[:, :plain.n_out])
+
+
+def test_shifted_screens_match_oracle(torch_cuda):
+    """Screens moved by (0, t) (the wind shift of Simulation.iter) through
+    atm_plan_update, against FP64 screens evaluated at y + t."""
+    torch = torch_cuda
+    spec = o.ChannelSpec(N=256, delta=4e-3, w0=0.08, length=8e3, count=2, points=256, Cn2=2e-15, pupil_radius=0.1)
+    plan, base = make_plan(spec, batch=1)
+    rho, theta, value = spectra(spec, base, seed=4, R=1)
+    dev = to_dev(torch, rho, theta, value)
+    field = torch.empty((1, spec.N, spec.N), dtype=torch.complex64, device="cuda")
+    positions = o.screen_positions(spec.length, spec.count, spec.position)
+    u0 = o.gaussian_source(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0)
+    for t in (0.0, 0.037, -0.2):
+        plan.set_shift((0.0, t))
+        plan.run(*dev, field_out=field)
+        screens = [o.ss_screen(rho[0, i], theta[0, i], value[0, i], spec.N, spec.delta, shift=(0.0, t))
+                   for i in range(2)]
+        u = o.propagate(u0, screens, positions, spec.length, spec.k, spec.delta, path_output_loss=False)
+        assert o.rel_l2(field.cpu().numpy()[0], u) < FIELD_TOL, t
