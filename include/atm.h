@@ -247,6 +247,14 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
  * the FFT calls of utils.py:42-50 (the boundary item atm_autotune). */
 int atm_autotune(AtmPlan* plan, int32_t batch, int32_t repeats, void* stream);
 
+/* Phase structure function of `batch` screens phi [batch][N][N] (float32,
+ * device) along x, averaged over rows: sf_out[b][r - 1] = (1/N) sum_y
+ * (1/(N - r)) sum_{x < N - r} (phi[b][y][x] - phi[b][y][x + r])^2 for
+ * r = 1 .. N - 1 (FP64, device).  Replaces calculate_sf
+ * (theory/phase_screens/sf.py:4-8) followed by the row mean of
+ * calculate_structure_function (simulations/structure_function.py:11-12). */
+int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* sf_out, void* stream);
+
 /* Sets the launch choices atm_autotune makes (row-pass variant 0..2, column
  * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..1)
  * by hand.  Launch shapes only: results do not change.  No reference

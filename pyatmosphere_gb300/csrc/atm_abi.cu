@@ -932,6 +932,14 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   return ATM_OK;
 }
 
+int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* sf_out, void* stream) {
+  if (!phi || !sf_out) return fail(ATM_ERR_INVALID, "phi / sf_out is NULL");
+  if (batch < 1 || batch > 65535) return fail(ATM_ERR_INVALID, "batch %d out of range", batch);
+  if (N < 2 || N > 8192) return fail(ATM_ERR_INVALID, "N %d out of range [2, 8192]", N);
+  ATM_CUDA(atm::launch_structure_function(phi, batch, N, sf_out, (cudaStream_t)stream));
+  return ATM_OK;
+}
+
 int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, int32_t col_variant) {
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
   if (row_variant < 0 || row_variant > 2) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..2", row_variant);

@@ -161,6 +161,7 @@ cudaError_t launch_fft_screen_finish(int B, const FftScreenArgs& a, cudaStream_t
 cudaError_t launch_finalize(int B, const FinalArgs& a, cudaStream_t st);
 cudaError_t launch_tracked(int B, const TrackedArgs& a, cudaStream_t st);
 cudaError_t launch_fma_probe(int blocks, int iters, cudaStream_t st);
+cudaError_t launch_structure_function(const float* phi, int B, int N, double* out, cudaStream_t st);
 cudaError_t launch_draw_spectra(uint64_t seed, uint64_t first, int n, int P, const float* fbase, const float* sqrt_psd,
                                 int B, float* rho, float* theta, float2* value, cudaStream_t st);
 int row_pass_rows(int N);          // rows per CTA of the row pass

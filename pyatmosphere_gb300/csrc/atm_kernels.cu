@@ -1213,6 +1213,96 @@ cudaError_t launch_tracked(int B, const TrackedArgs& a, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // FP32 FMA throughput probe: 8 independent chains per thread
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// phase structure function along x, averaged over rows
+// (simulations/structure_function.py:11-12, theory/phase_screens/sf.py:4-8):
+//   D[b][r-1] = (1/N) sum_y (1/(N-r)) sum_{x < N-r} (phi[b][y][x] - phi[b][y][x+r])^2
+// One CTA per (chunk of kSfThreads * kSfLags lags, screen), all rows; a
+// thread owns kSfLags consecutive lags and slides a register window over the
+// row in shared memory (two loads per 8 x 8 difference-squares).  Sums: FP32
+// over blocks of 256 x, FP64 across blocks and rows; deterministic.
+// ---------------------------------------------------------------------------
+constexpr int kSfThreads = 128;
+constexpr int kSfLags = 8;
+
+__global__ void __launch_bounds__(kSfThreads) structure_function_kernel(const float* __restrict__ phi, int N,
+                                                                         double* __restrict__ out) {
+  extern __shared__ float row[];
+  const int b = blockIdx.y;
+  const int r0 = 1 + ((int)blockIdx.x * kSfThreads + (int)threadIdx.x) * kSfLags;
+  double tot[kSfLags];
+#pragma unroll
+  for (int j = 0; j < kSfLags; ++j) tot[j] = 0.0;
+  const float* src = phi + (size_t)b * N * N;
+  for (int y = 0; y < N; ++y) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += kSfThreads) row[i] = src[(size_t)y * N + i];
+    __syncthreads();
+    if (r0 > N - 1) continue;
+    double rs[kSfLags];
+#pragma unroll
+    for (int j = 0; j < kSfLags; ++j) rs[j] = 0.0;
+    // x in [0, xa): every lag of the thread is in range (x + r0 + 7 < N)
+    const int xa = max(0, N - r0 - (kSfLags - 1));
+    int x = 0;
+    while (x < xa) {
+      const int xe = min(xa, x + 256);
+      float acc[kSfLags];
+#pragma unroll
+      for (int j = 0; j < kSfLags; ++j) acc[j] = 0.f;
+      for (; x + 8 <= xe; x += 8) {
+        float w[16];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) w[k] = (x + r0 + k < N) ? row[x + r0 + k] : 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const float a = row[x + u];
+#pragma unroll
+          for (int j = 0; j < kSfLags; ++j) {
+            const float d = a - w[u + j];
+            acc[j] = fmaf(d, d, acc[j]);
+          }
+        }
+      }
+      for (; x < xe; ++x) {
+        const float a = row[x];
+#pragma unroll
+        for (int j = 0; j < kSfLags; ++j) {
+          const float d = a - row[x + r0 + j];
+          acc[j] = fmaf(d, d, acc[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kSfLags; ++j) rs[j] += (double)acc[j];
+    }
+    // tail: x in [xa, N - r0), lag r0 + j only while x + r0 + j < N
+    for (; x < N - r0; ++x) {
+      const float a = row[x];
+#pragma unroll
+      for (int j = 0; j < kSfLags; ++j)
+        if (x + r0 + j < N) {
+          const float d = a - row[x + r0 + j];
+          rs[j] += (double)(d * d);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kSfLags; ++j)
+      if (r0 + j <= N - 1) tot[j] += rs[j] / (double)(N - (r0 + j));
+  }
+#pragma unroll
+  for (int j = 0; j < kSfLags; ++j)
+    if (r0 + j <= N - 1) out[(size_t)b * (N - 1) + (r0 + j - 1)] = tot[j] / (double)N;
+}
+
+cudaError_t launch_structure_function(const float* phi, int B, int N, double* out, cudaStream_t st) {
+  if (B < 1 || B > 65535 || N < 2 || N > 8192) return cudaErrorInvalidValue;
+  const int per = kSfThreads * kSfLags;
+  dim3 grid((N - 1 + per - 1) / per, B);
+  const size_t smem = (size_t)N * sizeof(float);
+  structure_function_kernel<<<grid, kSfThreads, smem, st>>>(phi, N, out);
+  return cudaGetLastError();
+}
+
 __device__ float g_fma_sink[256];
 
 __global__ void __launch_bounds__(256) fma_probe_kernel(int iters) {

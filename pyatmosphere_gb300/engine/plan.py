@@ -241,6 +241,19 @@ class EnginePlan:
         return {k: {"ms": ms[i], "launches": cnt[i]} for i, k in enumerate(_lib.KIND_NAMES)}
 
 
+def structure_function(phi: torch.Tensor) -> torch.Tensor:
+    """Phase structure function along x averaged over rows
+    (atm_structure_function): phi [B][N][N] float32 CUDA -> [B][N-1] float64."""
+    if phi.dim() != 3 or phi.shape[1] != phi.shape[2] or not phi.is_cuda:
+        raise ValueError("phi must be a [B][N][N] CUDA tensor")
+    phi = phi.to(torch.float32).contiguous()
+    B, N = int(phi.shape[0]), int(phi.shape[1])
+    out = torch.empty((B, N - 1), dtype=torch.float64, device=phi.device)
+    with torch.cuda.device(phi.device):
+        check(load().atm_structure_function(_tptr(phi), B, N, _tptr(out), _stream(phi.device)))
+    return out
+
+
 def fma_peak_tflops(device=None, blocks: int = 0, iters: int = 4096) -> float:
     """Measured FP32 FMA throughput of the device (TFLOP/s), from the
     engine's probe kernel; best of three launches after a warm-up."""

@@ -44,6 +44,11 @@ def classify(channel, mtype, ops):
         return None
     if mtype == "pupil" and len(ops) == 1 and ops[0] is M.eta and channel.pupil is not None:
         return ("pupil", (float(channel.pupil.radius), 0.0, 0.0))
+    if mtype == "phase_screen" and len(ops) == 1 and len(getattr(channel.path, "phase_screens", ())) > 0:
+        from .structure_function import calculate_structure_function
+        if ops[0] is calculate_structure_function:
+            return ("screen_sf",)  # of the first screen, from atm_screen + atm_structure_function
+        return None
     if mtype == "propagation" and len(ops) == 1 and len(getattr(channel.path, "phase_screens", ())) > 0:
         # after every screen and at the receiver (the engine's per-step measures)
         from .si import intensity_at_center

@@ -158,20 +158,32 @@ class Simulation:
             dev = to_device(*spectra)
             # screens move by (0, t) for each time value (Simulation.iter's shift=(0, time))
             shifts = sorted({float(t or 0) for _, _, T in entries for t in (T or (0,))})
-            outs = {}
+            outs, sfs = {}, {}
+            want_sf = any(k[0] == "screen_sf" for _, k, _ in entries)
             try:
                 for t in shifts:
                     plan.set_shift((0.0, t))
                     outs[t] = plan.run(*dev).cpu().numpy()
+                    if want_sf:
+                        import torch
+                        from ..engine.plan import structure_function
+                        phi = torch.empty((R, plan.N, plan.N), dtype=torch.float32, device=plan.device)
+                        plan.screen(*dev, 0, phi_out=phi)
+                        sfs[t] = structure_function(phi).cpu().numpy()
             finally:
                 plan.set_shift((0.0, 0.0))
             n = plan.n_screens
+            def values(kind, t):
+                if kind[0] == "screen_sf":
+                    return sfs[t]
+                return resolve(kind, outs[t], pupils, tracked, n)
+
             for m, kind, T in entries:
                 if T is None:
-                    vals = resolve(kind, outs[0.0], pupils, tracked, n)
+                    vals = values(kind, 0.0)
                     rows = [vals[r] for r in range(R)]
                 else:
-                    vs = [resolve(kind, outs[float(t or 0)], pupils, tracked, n) for t in T]
+                    vs = [values(kind, float(t or 0)) for t in T]
                     rows = [[v[r] for v in vs] for r in range(R)]
                 for r in range(R):
                     if m.is_done:

@@ -18,7 +18,15 @@ def calculate_sf(screen):
 
 
 def calculate_structure_function(channel, output):
-    return gpu.get_array(calculate_sf(output).mean(dim=1))
+    """Row mean of calculate_sf; CUDA screens go through the engine's
+    atm_structure_function kernel."""
+    import torch
+    if isinstance(output, torch.Tensor) and output.is_cuda and output.dim() == 2 and not output.is_complex():
+        from ..engine.plan import structure_function
+        return structure_function(output[None])[0].cpu().numpy()
+    if not isinstance(output, torch.Tensor):
+        output = torch.from_numpy(np.asarray(output))
+    return gpu.get_array(calculate_sf(output.real if output.is_complex() else output).mean(dim=1))
 
 
 class StructureFunctionResult(Result):

@@ -248,6 +248,12 @@ def main(ref_path):
     si = simulations.SIResult(ch, max_size=4)
     simulations.Simulation([si]).run()
     g["si_center"] = np.array(si.measures[0].data, dtype=float)
+    np.random.seed(888)
+    ch = make_channel(pa, **spec_kwargs(spec))
+    ch.path.init_phase_screens()  # the result reads phase_screen.wvl through the channel
+    sfr = simulations.StructureFunctionResult(ch, max_size=2)
+    simulations.Simulation([sfr]).run()
+    g["sf_seeded"] = np.array(sfr.measures[0].data, dtype=float)
 
     out = os.path.join(HERE, "golden.npz")
     np.savez_compressed(out, **{k: np.asarray(v) for k, v in g.items()})

@@ -71,7 +71,7 @@ def test_batched_path_classification():
     assert kinds == ["pupil", "slot", "tracked"]
     sim2 = simulations.Simulation(measures_list=[simulations.Measure(ch, "atmosphere", lambda c, output: 0.0)])
     assert sim2._batch_plan() is None
-    # wind (time-shifted) and per-step measures are fused too; screen statistics are not
+    # wind (time-shifted), per-step and first-screen structure-function measures are fused too
     sim3 = simulations.Simulation([simulations.TimeCoherenceResult(ch, [0, 1], max_size=2),
                                    simulations.SIResult(ch, max_size=2),
                                    simulations.BeamPropagationResult(ch, max_size=2)])
@@ -79,7 +79,7 @@ def test_batched_path_classification():
     assert sorted({(k[0], t) for _, k, t in plans3[ch]}) == [("pupil", (0, 1)), ("step", None),
                                                               ("step_mean_r", None), ("step_mean_r2", None)]
     sim4 = simulations.Simulation([simulations.StructureFunctionResult(ch, max_size=2)])
-    assert sim4._batch_plan() is None
+    assert [k for _, k, _ in sim4._batch_plan()[ch]] == [("screen_sf",)]
 
 
 def test_step_values_resolve_to_screens_then_receiver():

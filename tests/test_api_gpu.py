@@ -211,3 +211,22 @@ def test_batched_propagation_and_wind_equal_per_realisation_path():
     for a, b in zip(*results):
         assert a.shape == b.shape
         np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-9)
+
+
+def test_seeded_structure_function_result_reproduces_reference(golden):
+    """StructureFunctionResult of the first screen on the batched path
+    (atm_screen + atm_structure_function) against the reference's own run."""
+    import pyatmosphere_gb300 as pa
+    from pyatmosphere_gb300 import simulations
+    np.random.seed(888)
+    ch = small_channel(pa)
+    sfr = simulations.StructureFunctionResult(ch, max_size=2)
+    sim = simulations.Simulation([sfr])
+    assert sim._batch_plan() is not None
+    sim.run()
+    got = np.array(sfr.measures[0].data, float)
+    ref = golden["sf_seeded"]
+    assert got.shape == ref.shape == (2, 127)
+    # the reference builds its screens with float32 phase arguments
+    np.testing.assert_allclose(got, ref, rtol=1e-2)
+    assert sfr.structure_function.shape == (127,)

@@ -288,3 +288,21 @@ def test_shifted_screens_match_oracle(torch_cuda):
                    for i in range(2)]
         u = o.propagate(u0, screens, positions, spec.length, spec.k, spec.delta, path_output_loss=False)
         assert o.rel_l2(field.cpu().numpy()[0], u) < FIELD_TOL, t
+
+
+@pytest.mark.parametrize("N,B", [(100, 2), (1000, 1), (1024, 3)])
+def test_structure_function_kernel_matches_numpy(torch_cuda, N, B):
+    """atm_structure_function against the FP64 restatement of calculate_sf
+    (theory/phase_screens/sf.py:4-8) and its row mean, any N (ragged lag
+    chunks and row tails)."""
+    torch = torch_cuda
+    from pyatmosphere_gb300.engine.plan import structure_function
+    rng = np.random.default_rng(N)
+    # a rough screen with a large tilt, like a low-frequency phase
+    phi = (np.cumsum(rng.standard_normal((B, N, N)), axis=2) * 0.05 + 30.0 * np.linspace(-1, 1, N)).astype(np.float32)
+    got = structure_function(torch.from_numpy(phi).cuda()).cpu().numpy()
+    s = phi.astype(np.float64)
+    ref = np.stack([np.stack([((s[b, :, :-r] - s[b, :, r:]) ** 2).sum(axis=1) / (N - r) for r in range(1, N)]).mean(axis=1)
+                    for b in range(B)])
+    assert got.shape == (B, N - 1)
+    np.testing.assert_allclose(got, ref, rtol=2e-5)
