@@ -274,7 +274,12 @@ def run_gb300(args, rank, world, local_rank):
              "tc-cpasync": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_CPASYNC}[args.gemm]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
                       pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags)
-    tuned = plan.autotune(repeats=2) if args.autotune else None
+    if args.variants:
+        rv, ct, cv = (int(v) for v in args.variants.split(","))
+        plan.set_variants(rv, ct, cv)
+        tuned = {"col_tile": ct, "row_variant": rv, "col_variant": cv, "tuned": 0}
+    else:
+        tuned = plan.autotune(repeats=2) if args.autotune else None
     n_steps = args.warmup + args.steps
     # distinct seeded inputs per step (weak scaling: each rank its own realisations)
     host = []
@@ -466,6 +471,8 @@ def main():
     ap.add_argument("--cpu-realisations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", type=int, default=1, help="time the FFT-pass launch variants first (atm_autotune)")
+    ap.add_argument("--variants", default="",
+                    help="row_variant,col_tile,col_variant set by hand instead of atm_autotune (e.g. 2,4,0)")
     ap.add_argument("--mixed-channels", type=int, default=16,
                     help="channels of the mixed-size workload leg (0: skip)")
     ap.add_argument("--surrogate-points", type=int, default=8,

@@ -185,8 +185,26 @@ ATM_HD float2 twiddle(const float2* tw, int e) {
   return DIR < 0 ? w : cconj(w);
 }
 
+// twiddles w[m] = W_{LR}^{i m}, 1 <= m < R.  TWREC = 0: every one from the
+// table; TWREC = 1: only W^i, W^2i, W^4i, W^8i from the table, the rest as
+// products of at most three of them (a few ulp instead of half an ulp; fewer
+// shared-memory loads)
+template <int N, int LR, int R, int DIR, int TWPAD, int TWREC>
+ATM_HD void stage_twiddles(const float2* tw, int i, float2 (&w)[R]) {
+  if constexpr (TWREC == 0) {
+#pragma unroll
+    for (int m = 1; m < R; ++m) w[m] = twiddle<N, LR, DIR, TWPAD>(tw, i * m);
+  } else {
+#pragma unroll
+    for (int m = 1; m < R; ++m) {
+      const int hp = (m >= 8) ? 8 : (m >= 4) ? 4 : (m >= 2) ? 2 : 1;  // highest power of two <= m
+      w[m] = (m == hp) ? twiddle<N, LR, DIR, TWPAD>(tw, i * m) : cmul(w[hp], w[m - hp]);
+    }
+  }
+}
+
 // butterflies of stage s on register inputs; results to shared memory
-template <int N, int s, int DIR, int TWPAD = 0>
+template <int N, int s, int DIR, int TWPAD = 0, int TWREC = 0>
 ATM_HD void stage_to_smem(float2 (&v)[16], float2* sm, int t, const float2* tw) {
   constexpr int R = StageRadix<N, s>::value;
   constexpr int L = StageL<N, s>::value;
@@ -200,8 +218,10 @@ ATM_HD void stage_to_smem(float2 (&v)[16], float2* sm, int t, const float2* tw) 
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
     if (L > 1) {
+      float2 w[R];
+      stage_twiddles<N, L * R, R, DIR, TWPAD, TWREC>(tw, i, w);
 #pragma unroll
-      for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR, TWPAD>(tw, i * m));
+      for (int m = 1; m < R; ++m) a[m] = cmul(a[m], w[m]);
     }
     dft<R, DIR>(a);
     const int j = (k - i) * R + i;
@@ -224,7 +244,7 @@ ATM_HD void stage_from_smem(float2 (&v)[16], const float2* sm, int t) {
 }
 
 // last stage: outputs stay in registers, v[m] = element t + m T
-template <int N, int DIR, int TWPAD = 0>
+template <int N, int DIR, int TWPAD = 0, int TWREC = 0>
 ATM_HD void stage_last(float2 (&v)[16], int t, const float2* tw) {
   constexpr int s = FftPlan<N>::S - 1;
   constexpr int R = StageRadix<N, s>::value;
@@ -239,8 +259,10 @@ ATM_HD void stage_last(float2 (&v)[16], int t, const float2* tw) {
     float2 a[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
+    float2 w[R];
+    stage_twiddles<N, L * R, R, DIR, TWPAD, TWREC>(tw, i, w);
 #pragma unroll
-    for (int m = 1; m < R; ++m) a[m] = cmul(a[m], twiddle<N, L * R, DIR, TWPAD>(tw, i * m));
+    for (int m = 1; m < R; ++m) a[m] = cmul(a[m], w[m]);
     dft<R, DIR>(a);
 #pragma unroll
     for (int q = 0; q < R; ++q) o[b + B * q] = a[q];

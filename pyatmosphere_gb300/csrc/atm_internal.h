@@ -64,7 +64,8 @@ struct ColArgs {
   const float2* hy;         // [N] transfer function along y incl. exp(i k dz) / N^2
   const float2* hx;         // [N] transfer function along x
   int inv_only;             // 1: inverse column FFT only (no forward FFT, no H)
-  int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per column tile
+  int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per column tile,
+                            // 2: persistent pipeline with twiddles from powers of two (fewer shared loads)
 };
 
 // FFT screen (phase_screens.py:42-67) without shifts: screen[y][x] =

@@ -21,16 +21,16 @@ namespace atm {
 // ---------------------------------------------------------------------------
 // FFT driver over the stages of FftPlan<N> (see atm_common.cuh)
 // ---------------------------------------------------------------------------
-template <int N, int DIR, int s = 0, int TWPAD = 0>
+template <int N, int DIR, int s = 0, int TWPAD = 0, int TWREC = 0>
 __device__ __forceinline__ void fft_dev(float2 (&v)[16], float2* sm, int t, const float2* __restrict__ tw) {
   if constexpr (s == FftPlan<N>::S - 1) {
-    stage_last<N, DIR, TWPAD>(v, t, tw);
+    stage_last<N, DIR, TWPAD, TWREC>(v, t, tw);
   } else {
-    stage_to_smem<N, s, DIR, TWPAD>(v, sm, t, tw);
+    stage_to_smem<N, s, DIR, TWPAD, TWREC>(v, sm, t, tw);
     __syncthreads();
     stage_from_smem<N, s + 1>(v, sm, t);
     __syncthreads();
-    fft_dev<N, DIR, s + 1, TWPAD>(v, sm, t, tw);
+    fft_dev<N, DIR, s + 1, TWPAD, TWREC>(v, sm, t, tw);
   }
 }
 
@@ -83,8 +83,10 @@ int row_pass_rows(int N) {
 bool supported_n(int N) { return row_pass_rows(N) > 0; }
 
 // ---------------------------------------------------------------------------
-// measures of one row: per-thread FP32 sums over 16 pixels, then FP64 block
-// reduction; one partial vector per CTA and realisation
+// measures of one row: per-thread FP32 sums over 16 pixels, FP32 warp
+// reduction (512 pixels per warp at N >= 512), FP64 sum over the warps of the
+// CTA; one partial vector per CTA and realisation.  GB300 runs FP64 at a small
+// fraction of the FP32 rate, so FP64 is kept to the few cross-warp adds.
 // ---------------------------------------------------------------------------
 template <int N, int ROWS>
 __device__ __forceinline__ void measure_row(const RowArgs& a, const float2 (&v)[16], int t, int y, int r,
@@ -93,9 +95,10 @@ __device__ __forceinline__ void measure_row(const RowArgs& a, const float2 (&v)[
   constexpr int NT = ROWS * T;
   constexpr int NW = (NT + 31) / 32;
   constexpr int MM = 6 + kMaxPupils;
-  __shared__ double red[NW][MM];
+  __shared__ float red[NW][MM];
   const float d = (float)a.delta;
   const int np = a.n_pupils;
+  const int nm = a.n_meas;  // 6 + np
   float s0 = 0.f, s1 = 0.f, s3 = 0.f;
   float sp[kMaxPupils];
   int2 iv[kMaxPupils];
@@ -114,36 +117,39 @@ __device__ __forceinline__ void measure_row(const RowArgs& a, const float2 (&v)[
     s1 += I * xc;
     s3 += I * xc * xc;
 #pragma unroll
-    for (int p = 0; p < kMaxPupils; ++p)
+    for (int p = 0; p < kMaxPupils; ++p) {
+      if (p >= np) break;
       if (x >= iv[p].x && x <= iv[p].y) sp[p] += I;
+    }
     if (a.mean_I) atomicAdd(a.mean_I + (size_t)y * N + x, I);
     if (a.intensity) a.intensity[(size_t)r * plane + (size_t)y * N + x] = I;
     if (y == N / 2 && x == N / 2) a.center[r] = I;
   }
-  const double yc = (double)(y - N / 2) * a.delta64;
-  double val[MM];
+  const float yc = (float)(y - N / 2) * d;
+  float val[MM];
   val[MS_I] = s0;
   val[MS_IX] = s1;
-  val[MS_IMY] = -yc * (double)s0;
+  val[MS_IMY] = -yc * s0;
   val[MS_IX2] = s3;
-  val[MS_IMXY] = -yc * (double)s1;
-  val[MS_IY2] = yc * yc * (double)s0;
+  val[MS_IMXY] = -yc * s1;
+  val[MS_IY2] = yc * yc * s0;
 #pragma unroll
   for (int p = 0; p < kMaxPupils; ++p) val[MS_PUPIL0 + p] = sp[p];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < MM; ++k) {
-    double x = val[k];
+    if (k >= nm) break;
+    float x = val[k];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
     if (lane == 0) red[w][k] = x;
   }
   __syncthreads();
-  if (threadIdx.x < a.n_meas) {
+  if (threadIdx.x < nm) {
     double s = 0.0;
 #pragma unroll
-    for (int i = 0; i < NW; ++i) s += red[i][threadIdx.x];
-    a.partials[((size_t)r * n_parts + part) * a.n_meas + threadIdx.x] = s;
+    for (int i = 0; i < NW; ++i) s += (double)red[i][threadIdx.x];
+    a.partials[((size_t)r * n_parts + part) * nm + threadIdx.x] = s;
   }
   __syncthreads();  // red[] is reused by the next row of a persistent CTA
 }
@@ -466,7 +472,7 @@ struct ColPipe {
   static constexpr size_t SMEM = 2 * STAGE + TW + HY;
 };
 
-template <int N, int C>
+template <int N, int C, int TWREC>
 __global__ void __launch_bounds__(C * (N / 16))
 col_pass_pipe_kernel(ColArgs a, int n_items) {
   constexpr int T = N / 16;
@@ -508,12 +514,12 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
     __syncthreads();  // the exchange below overwrites the staged tile
     float2* sm = tile + c * S;
     if (!a.inv_only) {
-      fft_dev<N, -1, 0, 1>(v, sm, t, tws);
+      fft_dev<N, -1, 0, 1, TWREC>(v, sm, t, tws);
       const float2 hx = a.hx[x];
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(hys[t + m * T], hx));
     }
-    fft_dev<N, 1, 0, 1>(v, sm, t, tws);
+    fft_dev<N, 1, 0, 1, TWREC>(v, sm, t, tws);
     float2* f = a.field + (size_t)r * N * N + x;
 #pragma unroll
     for (int m = 0; m < 16; ++m) f[(size_t)(t + m * T) * N] = v[m];
@@ -522,17 +528,17 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
   cp_async_wait<0>();
 }
 
-template <int N, int C>
+template <int N, int C, int TWREC>
 static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
   static LaunchCache cache;
   const int threads = C * (N / 16);
   const size_t smem = ColPipe<N, C>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(col_pass_pipe_kernel<N, C>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(col_pass_pipe_kernel<N, C, TWREC>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / C);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  col_pass_pipe_kernel<N, C><<<grid, threads, smem, st>>>(a, n_items);
+  col_pass_pipe_kernel<N, C, TWREC><<<grid, threads, smem, st>>>(a, n_items);
   return cudaGetLastError();
 }
 
@@ -556,7 +562,9 @@ static cudaError_t col_plain_launch(int B, const ColArgs& a, cudaStream_t st) {
 template <int N, int C>
 static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
   if (C >= 2 && aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024 && a.variant == 0)
-    return col_pipe_launch<N, C>(B, a, st);
+    return col_pipe_launch<N, C, 0>(B, a, st);
+  if (C >= 2 && aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024 && a.variant == 2)
+    return col_pipe_launch<N, C, 1>(B, a, st);
   return col_plain_launch<N, C>(B, a, st);
 }
 

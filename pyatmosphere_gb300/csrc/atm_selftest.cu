@@ -13,19 +13,19 @@ struct Regs {
   float2 v[16];
 };
 
-template <int N, int DIR, int s>
+template <int N, int DIR, int s, int TWREC>
 void host_stages(std::vector<Regs>& R, float2* sm, const float2* tw) {
   constexpr int T = N / 16;
   if constexpr (s == atm::FftPlan<N>::S - 1) {
-    for (int t = 0; t < T; ++t) atm::stage_last<N, DIR>(R[t].v, t, tw);
+    for (int t = 0; t < T; ++t) atm::stage_last<N, DIR, 0, TWREC>(R[t].v, t, tw);
   } else {
-    for (int t = 0; t < T; ++t) atm::stage_to_smem<N, s, DIR>(R[t].v, sm, t, tw);
+    for (int t = 0; t < T; ++t) atm::stage_to_smem<N, s, DIR, 0, TWREC>(R[t].v, sm, t, tw);
     for (int t = 0; t < T; ++t) atm::stage_from_smem<N, s + 1>(R[t].v, sm, t);
-    host_stages<N, DIR, s + 1>(R, sm, tw);
+    host_stages<N, DIR, s + 1, TWREC>(R, sm, tw);
   }
 }
 
-template <int N>
+template <int N, int TWREC = 0>
 int host_fft(int dir, const float* in, float* out) {
   constexpr int T = N / 16;
   std::vector<float2> tw(N), sm(atm::Padded<N>::value);
@@ -37,9 +37,9 @@ int host_fft(int dir, const float* in, float* out) {
   for (int t = 0; t < T; ++t)
     for (int m = 0; m < 16; ++m) R[t].v[m] = make_float2(in[2 * (t + m * T)], in[2 * (t + m * T) + 1]);
   if (dir < 0)
-    host_stages<N, -1, 0>(R, sm.data(), tw.data());
+    host_stages<N, -1, 0, TWREC>(R, sm.data(), tw.data());
   else
-    host_stages<N, 1, 0>(R, sm.data(), tw.data());
+    host_stages<N, 1, 0, TWREC>(R, sm.data(), tw.data());
   for (int t = 0; t < T; ++t)
     for (int m = 0; m < 16; ++m) {
       out[2 * (t + m * T)] = R[t].v[m].x;
@@ -62,6 +62,20 @@ int atm_selftest_fft(int N, int dir, const float* in, float* out) {
     case 1024: return host_fft<1024>(dir, in, out);
     case 2048: return host_fft<2048>(dir, in, out);
     case 4096: return host_fft<4096>(dir, in, out);
+  }
+  return -1;
+}
+
+// the same with twiddles formed from powers of two (column-pass variant 2)
+int atm_selftest_fft_twrec(int N, int dir, const float* in, float* out) {
+  switch (N) {
+    case 64: return host_fft<64, 1>(dir, in, out);
+    case 128: return host_fft<128, 1>(dir, in, out);
+    case 256: return host_fft<256, 1>(dir, in, out);
+    case 512: return host_fft<512, 1>(dir, in, out);
+    case 1024: return host_fft<1024, 1>(dir, in, out);
+    case 2048: return host_fft<2048, 1>(dir, in, out);
+    case 4096: return host_fft<4096, 1>(dir, in, out);
   }
   return -1;
 }

@@ -58,10 +58,14 @@ def test_kernel_fft_arithmetic_on_host(built, N):
     rng = np.random.default_rng(N)
     x = (rng.standard_normal(N) + 1j * rng.standard_normal(N)).astype(np.complex64)
     for d in (-1, 1):
+        ref = np.fft.fft(x.astype(np.complex128)) if d < 0 else np.fft.ifft(x.astype(np.complex128)) * N
         out = np.zeros(N, np.complex64)
         assert lib.atm_selftest_fft(N, d, x.ctypes.data, out.ctypes.data) == 0
-        ref = np.fft.fft(x.astype(np.complex128)) if d < 0 else np.fft.ifft(x.astype(np.complex128)) * N
         assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 3e-7
+        # twiddles formed from powers of two (column-pass variant 2): a few ulp more
+        out2 = np.zeros(N, np.complex64)
+        assert lib.atm_selftest_fft_twrec(N, d, x.ctypes.data, out2.ctypes.data) == 0
+        assert np.linalg.norm(out2 - ref) / np.linalg.norm(ref) < 5e-7
 
 
 def test_bessel_coefficients_on_host(built):
