@@ -911,6 +911,13 @@ __global__ void __launch_bounds__(256) screen_table_kernel(ScreenArgs a) {
 
 // tensor-core layout of the high-frequency tables: thread (term q, row j)
 // writes A[j][2q..2q+1] and B[j][2q..2q+1] as FP16 hi / lo pairs
+// sin / cos of pi x for half-turns x in [-1, 1] (already reduced exactly):
+// the SFU forms, absolute error below 2^-21 (the FP16 hi / lo operand split
+// itself keeps 2^-22 relative)
+__device__ __forceinline__ void sincospi_sfu(float x, float* s, float* c) {
+  __sincosf(x * 3.14159265358979323846f, s, c);
+}
+
 __device__ __forceinline__ void split_pair(float u, float w, __half2* hi, __half2* lo) {
   const __half uh = __float2half_rn(u), wh = __float2half_rn(w);
   *hi = __halves2half2(uh, wh);
@@ -925,8 +932,8 @@ __global__ void __launch_bounds__(128) screen_table_tc_kernel(ScreenArgs a) {
   const HighTerm h = a.hterms[(size_t)r * (a.KH / 2) + q];
   const uint64_t ju = (uint64_t)j;
   float sy, cy, sx, cx;
-  sincospif(fixed_to_halfturns(h.sy * ju + h.oy), &sy, &cy);
-  sincospif(fixed_to_halfturns(h.sx * ju + h.ox), &sx, &cx);
+  sincospi_sfu(fixed_to_halfturns(h.sy * ju + h.oy), &sy, &cy);
+  sincospi_sfu(fixed_to_halfturns(h.sx * ju + h.ox), &sx, &cx);
   const size_t o = ((size_t)r * N + j) * a.Kp + 2 * q;
   split_pair(h.v.x * cy - h.v.y * sy, -(h.v.x * sy + h.v.y * cy), reinterpret_cast<__half2*>(a.ta_hi + o),
              reinterpret_cast<__half2*>(a.ta_lo + o));
