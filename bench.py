@@ -184,7 +184,7 @@ def surrogate_leg(args, dev):
     rng = np.random.default_rng(args.seed + 7)
     n_q = 100_000
     params = box.sample(n_q, rng)
-    X_host = torch.from_numpy(features(params, box)).pin_memory()
+    X_host = torch.from_numpy(features(params, box, s.physics)).pin_memory()
     X = X_host.to(dev)
     for _ in range(3):
         s.predict(X)
@@ -212,7 +212,7 @@ def surrogate_leg(args, dev):
     n_pts, n_real = args.surrogate_points, 4096
     pts = box.sample(n_pts, np.random.default_rng(args.seed + 8))
     pts["l0"] = np.round(pts["l0"] * 1e3) / 1e3
-    probs = s.predict(torch.from_numpy(features(pts, box)).to(dev))[0].cpu().numpy()
+    probs = s.predict(torch.from_numpy(features(pts, box, s.physics)).to(dev))[0].cpu().numpy()
     sim = PointSimulator(SimConfig(N=512, realisations=2048, seed=args.seed + 9), device=dev)
     ks, t_sim = [], 0.0
     for i in range(n_pts):

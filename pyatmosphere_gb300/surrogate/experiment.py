@@ -44,7 +44,7 @@ def evaluate(s: Surrogate, box: Box, n_points: int, n_real: int, seed: int, trai
     rng = np.random.default_rng(seed)
     P = box.sample(n_points, rng)
     P["l0"] = np.round(P["l0"] * 1e3) / 1e3
-    X = features(P, box)
+    X = features(P, box, s.physics)
     probs, _, oor = s.predict(torch.from_numpy(X).to(s.device))
     probs = probs.cpu().numpy()
     cfg = SimConfig(N=N, realisations=min(n_real, 2048), seed=seed)
@@ -70,7 +70,7 @@ def evaluate(s: Surrogate, box: Box, n_points: int, n_real: int, seed: int, trai
 
 def speed(s: Surrogate, box: Box, n_queries=100_000, seed=3):
     rng = np.random.default_rng(seed)
-    X = torch.from_numpy(features(box.sample(n_queries, rng), box)).to(s.device)
+    X = torch.from_numpy(features(box.sample(n_queries, rng), box, s.physics)).to(s.device)
     for _ in range(3):
         s.predict(X)
     torch.cuda.synchronize()
@@ -111,15 +111,18 @@ def main():
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--weight-decay", type=float, default=1e-4)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--raw-features", action="store_true", help="the 8 raw inputs only (no physics features)")
     a = ap.parse_args()
     box = Box()
     t0 = time.perf_counter()
     P, X, Y, _ = Surrogate.generate(box, a.points, SimConfig(realisations=a.realisations), seed=a.seed)
+    if a.raw_features:
+        X = X[:, :8]
     t_gen = time.perf_counter() - t0
     n_tr = int(0.9 * len(X))
     perm = np.random.default_rng(a.seed).permutation(len(X))
     tr, va = perm[:n_tr], perm[n_tr:]
-    s = Surrogate(box)
+    s = Surrogate(box, widths=(X.shape[1], 256, 256, 256, N_HIST + 3))
     t0 = time.perf_counter()
     losses = s.fit(X[tr], Y[tr], steps=a.steps, batch=a.batch, log_every=max(1, a.steps // 20), lr=a.lr,
                    weight_decay=a.weight_decay)

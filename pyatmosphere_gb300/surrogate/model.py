@@ -28,7 +28,8 @@ from .mlp import EngineMLP
 
 N_HIST = 64
 N_MOM = 3
-FEATURES = ["log10_Cn2", "log10_L", "w0", "wvl_um", "L_over_F0", "aperture", "l0_mm", "log10_L0"]
+FEATURES = ["log10_Cn2", "log10_L", "w0", "wvl_um", "L_over_F0", "aperture", "l0_mm", "log10_L0",
+            "log10_rytov", "log10_a_over_W", "log10_a_over_W_LT", "log10_Lambda"]
 
 
 @dataclass
@@ -58,12 +59,41 @@ class Box:
         }
 
 
-def features(p: Dict[str, np.ndarray], box: Box) -> np.ndarray:
-    """Raw features scaled to [0, 1] over the box (outside the box: outside [0, 1])."""
+N_RAW = 8
+N_PHYS = 4
+
+
+def physics_features(p: Dict[str, np.ndarray]) -> np.ndarray:
+    """Analytic combinations of the raw parameters that the PDT depends on
+    smoothly (weak-to-strong turbulence theory of a Gaussian beam):
+    plane-wave Rytov variance sigma_R^2 = 1.23 Cn2 k^(7/6) L^(11/6), the
+    vacuum beam radius at the receiver W = w0 sqrt(Theta0^2 + Lambda0^2)
+    (Theta0 = 1 - L/F0, Lambda0 = 2 L / (k w0^2)), a long-term radius
+    W_LT = W sqrt(1 + 1.33 sigma_R^2 Lambda^(5/6)) with the receiver-plane
+    Fresnel ratio Lambda = Lambda0 / (Theta0^2 + Lambda0^2), and the aperture
+    radius over both radii; each log10 mapped to about [0, 1] over the box."""
+    k = 2 * np.pi / p["wvl"]
+    L, w0, a = p["L"], p["w0"], p["aperture"]
+    theta0 = 1.0 - np.asarray(p["focused"], dtype=np.float64)   # F0 = L when focused, else infinity
+    lam0 = 2 * L / (k * w0 ** 2)
+    W = w0 * np.sqrt(theta0 ** 2 + lam0 ** 2)
+    lam = lam0 / (theta0 ** 2 + lam0 ** 2)
+    sr2 = 1.23 * p["Cn2"] * k ** (7 / 6) * L ** (11 / 6)
+    wlt = W * np.sqrt(1 + 1.33 * sr2 * lam ** (5 / 6))
+    return np.stack([(np.log10(sr2) + 3) / 5, (np.log10(a / W) + 2) / 3, (np.log10(a / wlt) + 2) / 3,
+                     (np.log10(lam) + 3) / 4], axis=1)
+
+
+def features(p: Dict[str, np.ndarray], box: Box, physics: bool = True) -> np.ndarray:
+    """Raw features scaled to [0, 1] over the box (outside the box: outside
+    [0, 1]), followed by the physics features when `physics`."""
     raw = np.stack([np.log10(p["Cn2"]), np.log10(p["L"]), p["w0"], p["wvl"] * 1e6, p["focused"], p["aperture"],
                     p["l0"] * 1e3, np.log10(p["L0"])], axis=1).astype(np.float64)
     lo, hi = box.features_lo_hi()
-    return ((raw - lo) / np.where(hi > lo, hi - lo, 1.0)).astype(np.float32)
+    X = (raw - lo) / np.where(hi > lo, hi - lo, 1.0)
+    if physics:
+        X = np.concatenate([X, physics_features(p)], axis=1)
+    return X.astype(np.float32)
 
 
 @dataclass
@@ -160,16 +190,21 @@ def ks_hist(probs: np.ndarray, samples: np.ndarray) -> float:
 class Surrogate:
     """MLP surrogate of the PDT with simulator fallback outside its box."""
 
-    def __init__(self, box: Optional[Box] = None, widths=(8, 256, 256, 256, N_HIST + N_MOM), device=None,
-                 max_batch=4096):
+    def __init__(self, box: Optional[Box] = None, widths=None, device=None, max_batch=4096):
         self.box = box or Box()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        widths = tuple(widths) if widths is not None else (N_RAW + N_PHYS, 256, 256, 256, N_HIST + N_MOM)
+        if widths[0] not in (N_RAW, N_RAW + N_PHYS):
+            raise ValueError(f"input width {widths[0]} is neither {N_RAW} nor {N_RAW + N_PHYS}")
+        self.physics = widths[0] == N_RAW + N_PHYS
         self.mlp = EngineMLP(widths, max_batch=max_batch, device=self.device)
         self.mom_mean = np.zeros(N_MOM, np.float32)
         self.mom_std = np.ones(N_MOM, np.float32)
-        # the box in feature space, with a margin for float32 rounding of the edges
-        lo = np.full(8, -1e-3, np.float32)
-        hi = np.full(8, 1 + 1e-3, np.float32)
+        # the box in feature space, with a margin for float32 rounding of the edges; the
+        # physics features follow from the raw ones and are not range-checked
+        lo = np.full(widths[0], -1e30, np.float32)
+        hi = np.full(widths[0], 1e30, np.float32)
+        lo[:N_RAW], hi[:N_RAW] = -1e-3, 1 + 1e-3
         self.lo = torch.from_numpy(lo).to(self.device)
         self.hi = torch.from_numpy(hi).to(self.device)
 
@@ -230,7 +265,7 @@ class Surrogate:
 
     def query(self, params: Dict[str, np.ndarray], fallback_cfg: Optional[SimConfig] = None):
         """PDT histograms for parameter points; out-of-box points are simulated."""
-        X = torch.from_numpy(features(params, self.box)).to(self.device)
+        X = torch.from_numpy(features(params, self.box, self.physics)).to(self.device)
         probs, mom, oor = self.predict(X)
         probs = probs.cpu().numpy()
         oor = oor.cpu().numpy().astype(bool)

@@ -46,7 +46,9 @@ def test_features_and_ks():
     box = Box()
     p = box.sample(100, np.random.default_rng(1))
     X = features(p, box)
-    assert X.shape == (100, 8) and X.min() >= -1e-6 and X.max() <= 1 + 1e-6
+    assert X.shape == (100, 12) and X[:, :8].min() >= -1e-6 and X[:, :8].max() <= 1 + 1e-6
+    assert np.isfinite(X).all() and X[:, 8:].min() > -0.5 and X[:, 8:].max() < 1.5
+    assert features(p, box, physics=False).shape == (100, 8)
     samples = np.random.default_rng(2).random(20000)
     assert ks_hist(np.full(64, 1 / 64), samples) < 0.02
     assert ks_hist(np.eye(64)[0], samples) > 0.9
