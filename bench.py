@@ -272,7 +272,8 @@ def run_gb300(args, rank, world, local_rank):
     pos = positions(w["length"], w["count"])
     from pyatmosphere_gb300.engine import _lib
     flags = {"tc": _lib.FLAG_TC_GEMM, "simt": _lib.FLAG_SIMT_GEMM, "auto": 0,
-             "tc-cpasync": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_CPASYNC}[args.gemm]
+             "tc-cpasync": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_CPASYNC,
+             "tc256": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_N256}[args.gemm]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
                       pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags)
     if args.variants:
@@ -441,7 +442,8 @@ def run_gb300(args, rank, world, local_rank):
             "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B, "gemm": args.gemm,
                        "l2": "inputs larger than L2 (field batch 8.6 GB per step)", "gemm_k": K,
                        "low_annuli": info["low_annuli"], "cheb_terms": info["cheb_terms"], "autotune": tuned,
-                       "gemm_form": ["fp32 simt", "tcgen05 cp.async", "tcgen05 persistent tma"][info["gemm_form"]]},
+                       "gemm_form": ["fp32 simt", "tcgen05 cp.async", "tcgen05 persistent tma 128x128",
+                                     "tcgen05 persistent tma 128x256"][info["gemm_form"]]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "plain": {"value": plain, "unit": UNIT, "realisations": args.plain,
                       "batched_over_plain": (value / world / plain) if plain else None},
@@ -478,9 +480,9 @@ def main():
                     help="channels of the mixed-size workload leg (0: skip)")
     ap.add_argument("--surrogate-points", type=int, default=8,
                     help="held-out points of the surrogate check (0: skip the surrogate leg)")
-    ap.add_argument("--gemm", choices=["auto", "tc", "tc-cpasync", "simt"], default="auto",
-                    help="screen GEMM on tensor cores (tc: persistent TMA form, the default at 2048^2; "
-                         "tc-cpasync: one CTA per tile) or FP32 SIMT cores")
+    ap.add_argument("--gemm", choices=["auto", "tc", "tc256", "tc-cpasync", "simt"], default="auto",
+                    help="screen GEMM on tensor cores (tc: persistent TMA form with 128 x 128 tiles, the default "
+                         "at 2048^2; tc256: 128 x 256 tiles; tc-cpasync: one CTA per tile) or FP32 SIMT cores")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -53,6 +53,8 @@ extern "C" {
 #define ATM_FLAG_TC_CPASYNC 4    /* tensor-core GEMM in its one-CTA-per-tile cp.async form instead of the
                                     persistent TMA form */
 #define ATM_FLAG_STEP_MEASURES 8 /* also measure the field just after every screen (per-step measures) */
+#define ATM_FLAG_TC_N256 16      /* persistent TMA GEMM with 128 x 256 tiles, two stages and one accumulator pair
+                                    (default: 128 x 128 tiles, three stages, double-buffered accumulators) */
 
 /* per-realisation doubles in measures_out (slot index).  With
  * ATM_FLAG_STEP_MEASURES, ATM_STEP_SLOTS more doubles per screen i follow the
@@ -116,7 +118,8 @@ typedef struct AtmPlanInfo {
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile,
                                  2: persistent pipelined with twiddles formed from powers of two */
   int32_t tuned;              /* 1 after a successful atm_autotune */
-  int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA form */
+  int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
+                                 form (128 x 128 tiles, the default), 3 the same with 128 x 256 tiles */
 } AtmPlanInfo;
 
 /* ABI version of the loaded library (ATM_ABI_VERSION). */
@@ -231,7 +234,8 @@ int atm_mlp_infer(AtmMlp* mlp, const float* x, int32_t batch, const float* lo, c
 /* Unit-test entry point of the tensor-core screen GEMM: out[s][m][n] =
  * scale * sum_k A[s][m][k] B[s][n][k] for FP32 device arrays (row stride K),
  * computed with tcgen05 MMAs on FP16 hi/lo slices; M % 128 == 0,
- * N % 256 == 0.  variant 0: persistent TMA form, 1: cp.async form.
+ * N % 256 == 0.  variant 0: persistent TMA form (128 x 128 tiles), 1: cp.async
+ * form, 2: persistent TMA form with 128 x 256 tiles.
  * Allocates its slice scratch; synchronises the stream.  No reference
  * counterpart (the reference's screen product is a cupy/numpy complex GEMM,
  * phase_screens.py:125-126). */

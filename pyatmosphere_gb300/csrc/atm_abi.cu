@@ -164,6 +164,7 @@ struct AtmPlan {
   bool step_meas = false;
   int step_slot0 = 0;
   atm::TcPlan* tcp = nullptr;  // TMA descriptors of the screen GEMM (null: cp.async form)
+  bool tc_n256 = false;        // the TMA form with 128 x 256 tiles (default: 128 x 128, double-buffered)
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
     int64_t s = 0;
@@ -468,7 +469,9 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
     }
     if (!(d->flags & ATM_FLAG_TC_CPASYNC))
       pl->tcp = atm::tc_plan_create(pl->B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p,
-                                    (const __half*)pl->ta_lo.p, (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p);
+                                    (const __half*)pl->ta_lo.p, (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p,
+                                    (d->flags & ATM_FLAG_TC_N256) ? 256 : 128);
+    pl->tc_n256 = pl->tcp && (d->flags & ATM_FLAG_TC_N256);
   }
   if (pl->n > 0) {
     const size_t simt_rows = pl->use_tc ? 0 : 1;  // FP32 SIMT tables only without tensor cores
@@ -561,7 +564,7 @@ int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
   info->row_variant = pl->row_variant;
   info->col_variant = pl->col_variant;
   info->tuned = pl->tuned;
-  info->gemm_form = pl->n == 0 ? 0 : (!pl->use_tc ? 0 : (pl->tcp ? 2 : 1));
+  info->gemm_form = pl->n == 0 ? 0 : (!pl->use_tc ? 0 : (pl->tcp ? (pl->tc_n256 ? 3 : 2) : 1));
   return ATM_OK;
 }
 

@@ -178,7 +178,7 @@ size_t tc_smem_bytes();
 // slices), encoded once on the host; null when the driver offers no encoder
 struct TcPlan;
 TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
-                       const __half* b_lo);
+                       const __half* b_lo, int tn);  // tn: output tile width 256 or 128
 void tc_plan_destroy(TcPlan* p);
 // fold_y [S][M] / fold_x [S][Nn] (nullable, turns): added to every output
 cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,

@@ -13,11 +13,14 @@
 //
 // tc_gemm_tma_kernel (default): persistent, warp-specialised.  Warp 0 loads
 // the four 128-byte-swizzled operand boxes of a K tile with TMA
-// (cp.async.bulk.tensor) into a two-stage ring, running ahead into the next
-// tile while warps 2-9 drain the accumulators (tcgen05.ld, combine, scale,
-// store, optionally adding 1-D phases fold_y[y] + fold_x[x]); warp 1 issues
-// the MMAs of each 128 x 256 output tile.  mbarriers: full / empty per
-// stage, full / empty for the accumulator pair.
+// (cp.async.bulk.tensor) into a ring of stages, running ahead into the next
+// tile; warp 1 issues the MMAs; warps 2-9 drain the accumulators (tcgen05.ld,
+// combine, scale, optionally add 1-D phases fold_y[y] + fold_x[x], store).
+// Default: 128 x 128 output tiles, three stages and two accumulator pairs
+// (4 x 128 TMEM columns), so a tile's drain overlaps the next tile's MMAs;
+// the 128 x 256 form (two stages, one pair) moves a third less operand data
+// per FLOP but waits for each drain.  mbarriers: full / empty per stage,
+// full / empty per accumulator pair.
 // tc_gemm_kernel: the first form, one CTA per tile, operands through cp.async
 // by all threads (kept for comparison and as the fallback when the driver
 // offers no tensor-map encoder).
@@ -262,15 +265,43 @@ __global__ void __launch_bounds__(THREADS, 1) tc_gemm_kernel(TcArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// persistent, warp-specialised form: TMA producer, MMA issuer, epilogue warps
+// persistent, warp-specialised form: TMA producer, MMA issuer, epilogue warps.
+// Template: output tile 128 x TNT, STG operand stages, NACC accumulator pairs
+// in TMEM (NACC = 2: the epilogue of one tile overlaps the next tile's MMAs).
+//   <256, 2, 1>: 2 x 256 TMEM columns, 96 KB stages
+//   <128, 3, 2>: 4 x 128 TMEM columns, 64 KB stages
 // ---------------------------------------------------------------------------
-constexpr int P_STAGES = 2;
-constexpr int P_THREADS = 320;  // warp 0: TMA, warp 1: MMA, warps 2-9: epilogue
-constexpr int P_SMEM = P_STAGES * STAGE + 1024;
+constexpr int P_THREADS = 320;    // warp 0: TMA, warp 1: MMA, warps 2-9: epilogue
 constexpr int EPI_THREADS = 256;  // two warps per TMEM lane quarter, each draining half of the columns
 
+template <int TNT, int STG, int NACC>
+struct TmaCfg {
+  static constexpr int B_SL = TNT * ROWB;                 // one FP16 slice of the B tile
+  static constexpr int STAGE_B = 2 * A_SLICE + 2 * B_SL;  // A_hi, A_lo, B_hi, B_lo
+  static constexpr int SMEM = STG * STAGE_B + 1024;
+  static_assert(NACC * 2 * TNT <= 512, "accumulators exceed the 512 TMEM columns");
+  static_assert(SMEM <= 227 * 1024, "stages exceed shared memory");
+};
+
+template <int NT>
+__host__ __device__ constexpr uint32_t instr_desc_n() {
+  return (1u << 4)                          // D format F32
+         | (0u << 7) | (0u << 10)           // A, B format F16
+         | ((uint32_t)(NT >> 3) << 17)      // N
+         | ((uint32_t)(TM >> 4) << 24);     // M
+}
+
+template <int NT>
+__device__ __forceinline__ void mma_f16_n(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(instr_desc_n<NT>()), "r"(accumulate)
+      : "memory");
+}
+
 struct TmaOperands {
-  CUtensorMap ah, al, bh, bl;  // [S][rows][Kp] FP16, boxes of 64 (K) x 128 or 256 rows
+  CUtensorMap ah, al, bh, bl;  // [S][rows][Kp] FP16, boxes of 64 (K) x 128 or TNT rows
 };
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
@@ -311,35 +342,39 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity
   }
 }
 
-__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int* s, int* m0, int* n0) {
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int tn, int* s, int* m0, int* n0) {
   const int per = tiles_m * tiles_n;
   *s = t / per;
   const int r = t - *s * per;
   *m0 = (r / tiles_n) * TM;
-  *n0 = (r - (r / tiles_n) * tiles_n) * TN;
+  *n0 = (r - (r / tiles_n) * tiles_n) * tn;
 }
 
+template <int TNT, int STG, int NACC>
 __global__ void __launch_bounds__(P_THREADS, 1)
     tc_gemm_tma_kernel(const __grid_constant__ TmaOperands ops, float* __restrict__ out, int S, int M, int Nn, int Kp,
                        float scale, const float* __restrict__ fold_y, const float* __restrict__ fold_x) {
+  using Cfg = TmaCfg<TNT, STG, NACC>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[P_STAGES], empty_bar[P_STAGES], accf_bar, acce_bar, drain_bar;
+  __shared__ __align__(8) uint64_t full_bar[STG], empty_bar[STG], accf_bar[NACC], acce_bar[NACC], drain_bar;
   __shared__ uint32_t tmem_holder;
   __shared__ int abort_word;
   volatile int* abort_flag = &abort_word;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t base = (smem_u32(smem_raw) + 1023) & ~1023u;
   const int KT = Kp / TK;
-  const int tiles_m = M / TM, tiles_n = Nn / TN;
+  const int tiles_m = M / TM, tiles_n = Nn / TNT;
   const int n_tiles = S * tiles_m * tiles_n;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < P_STAGES; ++i) {
+    for (int i = 0; i < STG; ++i) {
       mbar_init(smem_u32(&full_bar[i]), 1);
       mbar_init(smem_u32(&empty_bar[i]), 1);
     }
-    mbar_init(smem_u32(&accf_bar), 1);
-    mbar_init(smem_u32(&acce_bar), EPI_THREADS);
+    for (int i = 0; i < NACC; ++i) {
+      mbar_init(smem_u32(&accf_bar[i]), 1);
+      mbar_init(smem_u32(&acce_bar[i]), EPI_THREADS);
+    }
     mbar_init(smem_u32(&drain_bar), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -359,28 +394,28 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       // ---- TMA producer ----
       int stage = 0;
       uint32_t phase = 0;
-      bool issued[P_STAGES] = {};
-      uint32_t issued_phase[P_STAGES] = {};
+      bool issued[STG] = {};
+      uint32_t issued_phase[STG] = {};
       bool stop = false;
       for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
         int s, m0, n0;
-        tile_coords(t, tiles_m, tiles_n, &s, &m0, &n0);
+        tile_coords(t, tiles_m, tiles_n, TNT, &s, &m0, &n0);
         for (int kt = 0; kt < KT; ++kt) {
           if (!mbar_wait_or_abort(smem_u32(&empty_bar[stage]), phase ^ 1u, abort_flag)) {
             stop = true;
             break;
           }
           const uint32_t fb = smem_u32(&full_bar[stage]);
-          mbar_arrive_expect_tx(fb, (uint32_t)STAGE);
-          const uint32_t st = base + stage * STAGE;
+          mbar_arrive_expect_tx(fb, (uint32_t)Cfg::STAGE_B);
+          const uint32_t st = base + stage * Cfg::STAGE_B;
           const int x = kt * TK;
           tma_load_3d(st, &ops.ah, x, m0, s, fb);
           tma_load_3d(st + A_SLICE, &ops.al, x, m0, s, fb);
           tma_load_3d(st + 2 * A_SLICE, &ops.bh, x, n0, s, fb);
-          tma_load_3d(st + 2 * A_SLICE + B_SLICE, &ops.bl, x, n0, s, fb);
+          tma_load_3d(st + 2 * A_SLICE + Cfg::B_SL, &ops.bl, x, n0, s, fb);
           issued[stage] = true;
           issued_phase[stage] = phase;
-          if (++stage == P_STAGES) {
+          if (++stage == STG) {
             stage = 0;
             phase ^= 1u;
           }
@@ -389,45 +424,46 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       // before teardown: every issued copy has landed, and (normal path) the
       // MMAs have released every stage
       const bool aborted = *abort_flag != 0;
-      for (int i = 0; i < P_STAGES; ++i)
-        if (issued[i])
-          mbar_wait(smem_u32(aborted ? &full_bar[i] : &empty_bar[i]), issued_phase[i]);
+      for (int i = 0; i < STG; ++i)
+        if (issued[i]) mbar_wait(smem_u32(aborted ? &full_bar[i] : &empty_bar[i]), issued_phase[i]);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      int stage = 0;
-      uint32_t phase = 0, aphase = 0;
+      int stage = 0, n_done = 0;
+      uint32_t phase = 0;
       bool stop = false;
-      const uint32_t d0 = tmem, d1 = tmem + TN;  // columns [0, 256) and [256, 512)
-      for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
-        // the epilogue has drained the previous tile's accumulators
-        if (!mbar_wait_or_abort(smem_u32(&acce_bar), aphase ^ 1u, abort_flag)) break;
+      for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x, ++n_done) {
+        const int acc = n_done % NACC;
+        const uint32_t aphase = (uint32_t)(n_done / NACC) & 1u;
+        // the epilogue has drained this accumulator pair's previous tile
+        if (!mbar_wait_or_abort(smem_u32(&acce_bar[acc]), aphase ^ 1u, abort_flag)) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t d0 = tmem + (uint32_t)(acc * 2 * TNT), d1 = d0 + TNT;
         for (int kt = 0; kt < KT; ++kt) {
           if (!mbar_wait_or_abort(smem_u32(&full_bar[stage]), phase, abort_flag)) {
             stop = true;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-          const uint32_t sa = base + stage * STAGE, sal = sa + A_SLICE, sb = sa + 2 * A_SLICE, sbl = sb + B_SLICE;
+          const uint32_t sa = base + stage * Cfg::STAGE_B, sal = sa + A_SLICE, sb = sa + 2 * A_SLICE,
+                         sbl = sb + Cfg::B_SL;
 #pragma unroll
           for (int k4 = 0; k4 < TK / 16; ++k4) {
             const uint32_t off = k4 * 32;  // 16 FP16 of K = 32 bytes inside the swizzle atom
-            const uint32_t acc = (kt > 0 || k4 > 0) ? 1u : 0u;
-            mma_f16(d0, smem_desc(sa + off), smem_desc(sb + off), acc);
-            mma_f16(d1, smem_desc(sa + off), smem_desc(sbl + off), acc);
-            mma_f16(d1, smem_desc(sal + off), smem_desc(sb + off), 1u);
+            const uint32_t first = (kt > 0 || k4 > 0) ? 1u : 0u;
+            mma_f16_n<TNT>(d0, smem_desc(sa + off), smem_desc(sb + off), first);
+            mma_f16_n<TNT>(d1, smem_desc(sa + off), smem_desc(sbl + off), first);
+            mma_f16_n<TNT>(d1, smem_desc(sal + off), smem_desc(sb + off), 1u);
           }
           mma_commit(smem_u32(&empty_bar[stage]));
-          if (++stage == P_STAGES) {
+          if (++stage == STG) {
             stage = 0;
             phase ^= 1u;
           }
         }
         if (stop) break;
-        mma_commit(smem_u32(&accf_bar));
-        aphase ^= 1u;
+        mma_commit(smem_u32(&accf_bar[acc]));
       }
       // every MMA of this thread has finished before TMEM is freed
       mma_commit(smem_u32(&drain_bar));
@@ -437,22 +473,25 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     // ---- epilogue: warps 2-9; TMEM lane quarter warp % 4, column half (warp - 2) / 4 ----
     const int q = warp & 3;
     const int row = q * 32 + lane;
-    const int cbeg = ((warp - 2) >> 2) * (TN / 2);
-    uint32_t aphase = 0;
-    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int cbeg = ((warp - 2) >> 2) * (TNT / 2);
+    int n_done = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++n_done) {
+      const int acc = n_done % NACC;
+      const uint32_t aphase = (uint32_t)(n_done / NACC) & 1u;
       int s, m0, n0;
-      tile_coords(t, tiles_m, tiles_n, &s, &m0, &n0);
+      tile_coords(t, tiles_m, tiles_n, TNT, &s, &m0, &n0);
       int ok = 0;
-      if (lane == 0) ok = mbar_wait_or_abort(smem_u32(&accf_bar), aphase, abort_flag) ? 1 : 0;
+      if (lane == 0) ok = mbar_wait_or_abort(smem_u32(&accf_bar[acc]), aphase, abort_flag) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+      const uint32_t d0 = tmem + (uint32_t)(acc * 2 * TNT) + lane_addr, d1 = d0 + TNT;
       float* o = out + ((size_t)s * M + m0 + row) * Nn + n0;
       const float fy = fold_y ? fold_y[(size_t)s * M + m0 + row] : 0.f;
       const float* fx = fold_x ? fold_x + (size_t)s * Nn + n0 : nullptr;
 #pragma unroll 1
-      for (int c0 = cbeg; c0 < cbeg + TN / 2; c0 += 32) {
+      for (int c0 = cbeg; c0 < cbeg + TNT / 2; c0 += 32) {
         uint32_t h[32], l[32];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -461,7 +500,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
               "=r"(h[8]), "=r"(h[9]), "=r"(h[10]), "=r"(h[11]), "=r"(h[12]), "=r"(h[13]), "=r"(h[14]), "=r"(h[15]),
               "=r"(h[16]), "=r"(h[17]), "=r"(h[18]), "=r"(h[19]), "=r"(h[20]), "=r"(h[21]), "=r"(h[22]), "=r"(h[23]),
               "=r"(h[24]), "=r"(h[25]), "=r"(h[26]), "=r"(h[27]), "=r"(h[28]), "=r"(h[29]), "=r"(h[30]), "=r"(h[31])
-            : "r"(tmem + lane_addr + c0));
+            : "r"(d0 + c0));
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
@@ -469,7 +508,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
               "=r"(l[8]), "=r"(l[9]), "=r"(l[10]), "=r"(l[11]), "=r"(l[12]), "=r"(l[13]), "=r"(l[14]), "=r"(l[15]),
               "=r"(l[16]), "=r"(l[17]), "=r"(l[18]), "=r"(l[19]), "=r"(l[20]), "=r"(l[21]), "=r"(l[22]), "=r"(l[23]),
               "=r"(l[24]), "=r"(l[25]), "=r"(l[26]), "=r"(l[27]), "=r"(l[28]), "=r"(l[29]), "=r"(l[30]), "=r"(l[31])
-            : "r"(tmem + TN + lane_addr + c0));
+            : "r"(d1 + c0));
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
         const float lo_scale = scale / kTcLoScale;
 #pragma unroll
@@ -492,8 +531,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      mbar_arrive(smem_u32(&acce_bar));
-      aphase ^= 1u;
+      mbar_arrive(smem_u32(&acce_bar[acc]));
     }
   }
 
@@ -561,11 +599,13 @@ static bool encode_operand(EncodeTiledFn fn, CUtensorMap* map, const __half* bas
 struct TcPlan {
   TmaOperands ops;
   int S, M, Nn, Kp;
+  int tn;  // output tile width: 256 (two stages, one accumulator pair) or 128 (three stages, two pairs)
 };
 
 TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
-                       const __half* b_lo) {
-  if (S < 1 || M % TM || Nn % TN || Kp % TK || Kp < TK) return nullptr;
+                       const __half* b_lo, int tn) {
+  if (tn != 128 && tn != 256) return nullptr;
+  if (S < 1 || M % TM || Nn % tn || Kp % TK || Kp < TK) return nullptr;
   EncodeTiledFn fn = encode_tiled();
   if (!fn) return nullptr;
   TcPlan* p = new TcPlan{};
@@ -573,8 +613,9 @@ TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const _
   p->M = M;
   p->Nn = Nn;
   p->Kp = Kp;
+  p->tn = tn;
   if (!encode_operand(fn, &p->ops.ah, a_hi, S, M, Kp, TM) || !encode_operand(fn, &p->ops.al, a_lo, S, M, Kp, TM) ||
-      !encode_operand(fn, &p->ops.bh, b_hi, S, Nn, Kp, TN) || !encode_operand(fn, &p->ops.bl, b_lo, S, Nn, Kp, TN)) {
+      !encode_operand(fn, &p->ops.bh, b_hi, S, Nn, Kp, tn) || !encode_operand(fn, &p->ops.bl, b_lo, S, Nn, Kp, tn)) {
     delete p;
     return nullptr;
   }
@@ -583,27 +624,37 @@ TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const _
 
 void tc_plan_destroy(TcPlan* p) { delete p; }
 
-cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
-                               const float* fold_x, cudaStream_t st) {
-  if (!p || S < 1 || S > p->S || !out || (!fold_y) != (!fold_x)) return cudaErrorInvalidValue;
-  if (((uintptr_t)fold_x & 15) != 0) return cudaErrorMisalignedAddress;
+template <int TNT, int STG, int NACC>
+static cudaError_t launch_tma_form(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
+                                   const float* fold_x, cudaStream_t st) {
+  using Cfg = TmaCfg<TNT, STG, NACC>;
   static int sms[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (sms[dev] == 0) {
-    e = cudaFuncSetAttribute(tc_gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM);
+    e = cudaFuncSetAttribute(tc_gemm_tma_kernel<TNT, STG, NACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Cfg::SMEM);
     if (e != cudaSuccess) return e;
     int n = 0;
     e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     sms[dev] = std::max(n, 1);
   }
-  const int n_tiles = S * (p->M / TM) * (p->Nn / TN);
+  const int n_tiles = S * (p->M / TM) * (p->Nn / TNT);
   const int grid = std::min(n_tiles, sms[dev]);
-  tc_gemm_tma_kernel<<<grid, P_THREADS, P_SMEM, st>>>(p->ops, out, S, p->M, p->Nn, p->Kp, scale, fold_y, fold_x);
+  tc_gemm_tma_kernel<TNT, STG, NACC><<<grid, P_THREADS, Cfg::SMEM, st>>>(p->ops, out, S, p->M, p->Nn, p->Kp, scale,
+                                                                          fold_y, fold_x);
   return cudaGetLastError();
+}
+
+cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
+                               const float* fold_x, cudaStream_t st) {
+  if (!p || S < 1 || S > p->S || !out || (!fold_y) != (!fold_x)) return cudaErrorInvalidValue;
+  if (((uintptr_t)fold_x & 15) != 0) return cudaErrorMisalignedAddress;
+  if (p->tn == 128) return launch_tma_form<128, 3, 2>(p, S, out, scale, fold_y, fold_x, st);
+  return launch_tma_form<256, 2, 1>(p, S, out, scale, fold_y, fold_x, st);
 }
 
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
@@ -648,7 +699,8 @@ cudaError_t tc_error_flag(int* host_flag, bool reset) {
 // unit-test entry point of the tensor-core GEMM (device pointers):
 //   out[s][m][n] = scale * sum_k A[s][m][k] B[s][n][k]  for FP32 A, B with K
 //   columns (row strides K), via the FP16 hi/lo split; M % 128 == 0,
-//   N % 256 == 0; variant 0 = TMA form, 1 = cp.async form.  Scratch for the
+//   N % 256 == 0; variant 0 = TMA form with 128 x 128 tiles and double-buffered
+//   accumulators, 1 = cp.async form, 2 = TMA form with 128 x 256 tiles.  Scratch for the
 //   slices is allocated here (test path).
 // ---------------------------------------------------------------------------
 extern "C" int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32_t N, int32_t K,
@@ -656,7 +708,7 @@ extern "C" int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32
   if (!A || !B || !out || S < 1 || M < 1 || N < 1 || K < 1)
     return atm::set_error(ATM_ERR_INVALID, "bad tc gemm arguments");
   if (M % 128 || N % 256) return atm::set_error(ATM_ERR_UNSUPPORTED, "M %% 128 and N %% 256 must be 0");
-  if (variant != 0 && variant != 1) return atm::set_error(ATM_ERR_INVALID, "variant %d is not 0 or 1", variant);
+  if (variant < 0 || variant > 2) return atm::set_error(ATM_ERR_INVALID, "variant %d is not 0, 1 or 2", variant);
   cudaStream_t st = (cudaStream_t)stream;
   const int Kp = (K + 63) / 64 * 64;
   __half *ah = nullptr, *al = nullptr, *bh = nullptr, *bl = nullptr;
@@ -673,12 +725,12 @@ extern "C" int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32
   cudaError_t e = atm::launch_split_fp16(A, S * M, K, K, Kp, ah, al, st);
   if (e == cudaSuccess) e = atm::launch_split_fp16(B, S * N, K, K, Kp, bh, bl, st);
   atm::TcPlan* tp = nullptr;
-  if (e == cudaSuccess && variant == 0) {
-    tp = atm::tc_plan_create(S, M, N, Kp, ah, al, bh, bl);
+  if (e == cudaSuccess && variant != 1) {
+    tp = atm::tc_plan_create(S, M, N, Kp, ah, al, bh, bl, variant == 2 ? 256 : 128);
     if (!tp) e = cudaErrorNotSupported;
   }
   if (e == cudaSuccess)
-    e = variant == 0 ? atm::launch_tc_gemm_tma(tp, S, out, scale, nullptr, nullptr, st)
+    e = variant != 1 ? atm::launch_tc_gemm_tma(tp, S, out, scale, nullptr, nullptr, st)
                      : atm::launch_tc_gemm(S, M, N, Kp, ah, al, bh, bl, out, scale, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   int flag = 0;

@@ -21,6 +21,7 @@ FLAG_SIMT_GEMM = 1
 FLAG_TC_GEMM = 2
 FLAG_TC_CPASYNC = 4
 FLAG_STEP_MEASURES = 8
+FLAG_TC_N256 = 16
 STEP_SLOTS = 8
 SOURCE_GAUSSIAN = 0
 SOURCE_PLANE = 1

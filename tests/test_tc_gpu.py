@@ -8,11 +8,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("S,M,N,K", [(1, 128, 256, 64), (2, 256, 512, 200), (1, 512, 512, 768), (3, 2048, 2048, 768)])
 def test_tc_gemm_matches_fp64(S, M, N, K, variant):
-    """Both forms (0: persistent TMA, 1: cp.async per tile), including more
-    tiles than SMs so the persistent loop wraps."""
+    """Every form (0: persistent TMA 128 x 128 with double-buffered
+    accumulators, 1: cp.async per tile, 2: persistent TMA 128 x 256),
+    including more tiles than SMs so the persistent loop wraps."""
     import torch
     from pyatmosphere_gb300.engine import _lib
     lib = _lib.load()
@@ -91,8 +92,9 @@ def test_tc_channel_4096_matches_oracle():
 
 
 def test_tc_forms_agree_on_a_channel():
-    """The persistent TMA form is the default; the cp.async form (flag) gives
-    the same measures to FP32 round-off."""
+    """The persistent TMA form (128 x 128 tiles) is the default; its 128 x 256
+    form gives the same measures, the cp.async form (flag) the same to FP32
+    round-off."""
     import torch
     from oracle import atm_oracle as o
     from pyatmosphere_gb300.engine import EnginePlan, _lib
@@ -107,6 +109,10 @@ def test_tc_forms_agree_on_a_channel():
     cpa = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, f_base=base,
                      pupils=[(0.1,)], batch=4, flags=_lib.FLAG_TC_CPASYNC)
     assert tma.info["gemm_form"] == 2 and cpa.info["gemm_form"] == 1
+    t256 = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, f_base=base,
+                      pupils=[(0.1,)], batch=4, flags=_lib.FLAG_TC_N256)
+    assert t256.info["gemm_form"] == 3
+    np.testing.assert_allclose(t256.run(*sp).cpu().numpy(), tma.run(*sp).cpu().numpy(), rtol=1e-6, atol=1e-12)
     a, b = tma.run(*sp).cpu().numpy(), cpa.run(*sp).cpu().numpy()
     # the TMA form also folds the 1-D phases into the GEMM output (one FP32
     # rounding more): integrated measures to 2e-5, the one-pixel intensity to 1e-4
