@@ -114,9 +114,11 @@ typedef struct AtmPlanInfo {
   int32_t row_parts;          /* row-pass CTAs per realisation */
   int32_t col_tile;           /* columns per CTA of the column pass */
   int32_t row_variant;        /* 0: persistent pipelined row pass, 1: one CTA per row block,
-                                 2: persistent pipelined with one row per CTA */
+                                 2: persistent pipelined with one row per CTA,
+                                 3: as 2 with rows loaded by bulk copies (TMA) */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile,
-                                 2: persistent pipelined with twiddles formed from powers of two */
+                                 2: persistent pipelined with twiddles formed from powers of two,
+                                 3: persistent with tiles loaded by TMA (loads overlap the FFTs) */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
                                  form (128 x 128 tiles, the default), 3 the same with 128 x 256 tiles */
@@ -244,9 +246,9 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
 
 /* Times the launch variants of the FFT passes on this plan's own workspace
  * (`batch` realisations, `repeats` timed launches each after one warm-up)
- * and keeps the fastest: row-pass variant (three forms), column tile
+ * and keeps the fastest: row-pass variant (four forms), column tile
  * (2..16 columns, at most 512 threads per CTA) and column-pass variant
- * (three forms).  Every form but column variant 2 computes the same bits;
+ * (four forms).  Every form but column variant 2 computes the same bits;
  * column variant 2 forms most twiddles as products of table values and so
  * rounds differently (FP32 round-off, well inside the 1e-4 field bound).  Overwrites the
  * plan's field / screen workspace (zeroes) and blocks until the timing
@@ -264,9 +266,9 @@ int atm_autotune(AtmPlan* plan, int32_t batch, int32_t repeats, void* stream);
 int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* sf_out, void* stream);
 
 /* Sets the launch choices atm_autotune makes (row-pass variant 0..2, column
- * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..2)
- * by hand.  Results do not change, except for FP32 round-off with column
- * variant 2.  No reference counterpart. */
+ * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..3)
+ * by hand (row variant 0..3).  Results do not change, except for FP32
+ * round-off with column variant 2.  No reference counterpart. */
 int atm_plan_set_variants(AtmPlan* plan, int32_t row_variant, int32_t col_tile, int32_t col_variant);
 
 /* Launch categories reported by atm_profile_end. */

@@ -55,7 +55,8 @@ struct RowArgs {
   double* step_partials;    // [B][gridDim.x][6] partials of the post-screen field (ROW_STEP)
   float* step_center;       // [B] post-screen intensity at the grid origin (ROW_STEP)
   int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per row block,
-                            // 2: persistent pipeline with one row per CTA (row blocks of several rows otherwise)
+                            // 2: persistent pipeline with one row per CTA (row blocks of several rows otherwise),
+                            // 3: as 2 with the rows moved by bulk copies (TMA) from one thread
 };
 
 struct ColArgs {
@@ -65,7 +66,8 @@ struct ColArgs {
   const float2* hx;         // [N] transfer function along x
   int inv_only;             // 1: inverse column FFT only (no forward FFT, no H)
   int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per column tile,
-                            // 2: persistent pipeline with twiddles from powers of two (fewer shared loads)
+                            // 2: persistent pipeline with twiddles from powers of two (fewer shared loads),
+                            // 3: persistent, tiles loaded by TMA (one thread) so loads overlap the FFTs
 };
 
 // FFT screen (phase_screens.py:42-67) without shifts: screen[y][x] =
@@ -180,6 +182,9 @@ struct TcPlan;
 TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                        const __half* b_lo, int tn);  // tn: output tile width 256 or 128
 void tc_plan_destroy(TcPlan* p);
+// tensor map (128-byte storage of a CUtensorMap) of a complex64 field [B][N][N]
+// in boxes of C columns x box_rows rows; false without an encoder or alignment
+bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int box_rows);
 // fold_y [S][M] / fold_x [S][Nn] (nullable, turns): added to every output
 cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
                                const float* fold_x, cudaStream_t st);

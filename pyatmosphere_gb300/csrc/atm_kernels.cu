@@ -10,6 +10,8 @@
 //   row_pass      (inverse row FFT, exp(-i phi) multiply, forward row FFT)
 //   col_pass      (forward column FFT, H(fy,fx,dz), inverse column FFT)
 // and one last row_pass with the pupil / moment reductions, then finalize.
+#include <cuda.h>  // CUtensorMap (the column pass's TMA form)
+
 #include <algorithm>
 #include <cstdint>
 
@@ -60,6 +62,31 @@ __device__ __forceinline__ float2 phasor_turns(float t) {
   float s, c;
   __sincosf(r * 6.28318530717958647692f, &s, &c);
   return make_float2(c, -s);
+}
+
+// ---------------------------------------------------------------------------
+// bounded mbarrier waits of the TMA-fed passes (error word set on timeout)
+// ---------------------------------------------------------------------------
+__device__ int g_pass_error;
+
+__device__ __forceinline__ uint64_t pass_timer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool pass_mbar_wait(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = pass_timer();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (pass_timer() - t0 > 2000000000ull) return false;
+  }
 }
 
 // rows per CTA of the row pass: about 256 threads per CTA
@@ -239,8 +266,13 @@ struct RowPipe {
 };
 
 // ROWS rows per CTA: RowRows<N> (about 256 threads) or 1 (N/16 threads, so
-// the exchange barriers of a row never wait for another row)
-template <int N, int ROWS>
+// the exchange barriers of a row never wait for another row).  BULK = 0: every
+// thread stages the next rows with 16-byte cp.async; BULK = 1: one thread
+// moves each next row with one bulk copy (TMA) onto an mbarrier, so the
+// other threads never hold for the memory system and the copies overlap the
+// FFTs (bounded waits: on timeout the CTA records an error, waits for its
+// copies in flight and returns).
+template <int N, int ROWS, int BULK>
 __global__ void __launch_bounds__(ROWS * (N / 16), (ROWS * (N / 16) <= 128) ? 4 : ((ROWS * (N / 16) <= 256) ? 2 : 1))
 row_pass_pipe_kernel(RowArgs a, int n_items) {
   constexpr int T = N / 16;
@@ -257,12 +289,37 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
   auto fbuf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * RowPipe<N, ROWS>::STAGE); };
   float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * RowPipe<N, ROWS>::STAGE);
   load_twiddles<N>(tws, a.tw);
+  __shared__ __align__(8) uint64_t full_bar[2];
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
+  if constexpr (BULK) {
+    if (tid == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+  }
+  bool pending[2] = {false, false};  // BULK, thread 0: copies issued and not yet waited for
   auto prefetch = [&](int item, int s) {
     const int r = item / NRB, y0 = (item - r * NRB) * ROWS;
     const size_t off = (size_t)r * N * N + (size_t)y0 * N;
-    if (load_field) {
-      const float2* src = a.field + off;
-      float2* dst = fbuf(s);
+    if (!load_field) return;
+    const float2* src = a.field + off;
+    float2* dst = fbuf(s);
+    if constexpr (BULK) {
+      if (tid != 0) return;
+      const uint32_t bar = bar0 + 8 * s;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                   "r"((uint32_t)(ROWS * N * sizeof(float2)))
+                   : "memory");
+      for (int row = 0; row < ROWS; ++row)
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                (uint32_t)__cvta_generic_to_shared(dst + row * P)),
+            "l"(src + (size_t)row * N), "r"((uint32_t)(N * sizeof(float2))), "r"(bar)
+            : "memory");
+      pending[s] = true;
+    } else {
       for (int c = tid; c < ROWS * N / 2; c += NT) {
         const int row = c / (N / 2), col = (c - row * (N / 2)) * 2;
         cp_async16(dst + row * P + col, src + (size_t)row * N + col);
@@ -270,15 +327,25 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
     }
   };
 
-  int item = blockIdx.x, s = 0;
+  int item = blockIdx.x, s = 0, k = 0;
   if (item < n_items) prefetch(item, 0);
-  cp_async_commit();
-  for (; item < n_items; item += gridDim.x, s ^= 1) {
+  if constexpr (!BULK) cp_async_commit();
+  for (; item < n_items; item += gridDim.x, s ^= 1, ++k) {
     const int next = item + gridDim.x;
     if (next < n_items) prefetch(next, s ^ 1);
-    cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
+    if constexpr (BULK) {
+      // item k of this CTA uses stage k & 1 for the (k >> 1)-th time
+      const bool ok = !load_field || pass_mbar_wait(bar0 + 8 * s, (uint32_t)((k >> 1) & 1));
+      if (tid == 0 && ok) pending[s] = false;
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) atomicExch(&g_pass_error, 1);
+        break;
+      }
+    } else {
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+    }
     const int r = item / NRB, rb = item - r * NRB;
     const int y = rb * ROWS + rl;
     float2* sm = fbuf(s) + rl * P;
@@ -325,9 +392,17 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
       for (int m = 0; m < 16; ++m) dst[rowoff + t + m * T] = v[m];
     }
     if (flags & ROW_MEAS) measure_row<N, ROWS>(a, v, t, y, r, rb, NRB);
+    if constexpr (BULK) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // refilled by TMA
     __syncthreads();  // stage s is refilled by the next iteration's prefetch
   }
-  cp_async_wait<0>();
+  if constexpr (BULK) {
+    // no copy may land after the CTA leaves: wait (bounded) for any still pending
+    if (tid == 0)
+      for (int q = 0; q < 2; ++q)
+        if (pending[q]) pass_mbar_wait(bar0 + 8 * q, (uint32_t)(((k + (q != s)) >> 1) & 1));
+  } else {
+    cp_async_wait<0>();
+  }
 }
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
@@ -361,17 +436,17 @@ struct LaunchCache {
   }
 };
 
-template <int N, int ROWS>
+template <int N, int ROWS, int BULK = 0>
 static cudaError_t row_pipe_launch(int B, const RowArgs& a, cudaStream_t st) {
   static LaunchCache cache;
   const int threads = ROWS * (N / 16);
   const size_t smem = RowPipe<N, ROWS>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(row_pass_pipe_kernel<N, ROWS>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(row_pass_pipe_kernel<N, ROWS, BULK>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / ROWS);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  row_pass_pipe_kernel<N, ROWS><<<grid, threads, smem, st>>>(a, n_items);
+  row_pass_pipe_kernel<N, ROWS, BULK><<<grid, threads, smem, st>>>(a, n_items);
   return cudaGetLastError();
 }
 
@@ -397,11 +472,18 @@ template <int N>
 static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
-  // measure partials are laid out per block of RowRows<N> rows: variant 2 falls back to 0 there
-  const int variant = (a.flags & (ROW_MEAS | ROW_STEP)) && a.variant == 2 ? 0 : a.variant;
+  // measure partials are laid out per block of RowRows<N> rows: one-row forms fall back there
+  const bool meas = (a.flags & (ROW_MEAS | ROW_STEP)) != 0;
+  const int variant = meas && a.variant == 2 ? 0 : a.variant;
+  // one row per CTA only where a row fills at least four warps
+  constexpr bool one_row = RowRows<N>::value > 1 && N / 16 >= 128;
   if (field_ok && phi_ok && variant == 2) {
-    // one row per CTA only where a row fills at least four warps
-    if constexpr (RowRows<N>::value > 1 && N / 16 >= 128) return row_pipe_launch<N, 1>(B, a, st);
+    if constexpr (one_row) return row_pipe_launch<N, 1>(B, a, st);
+  }
+  if (field_ok && phi_ok && variant == 3) {
+    if constexpr (one_row)
+      if (!meas) return row_pipe_launch<N, 1, 1>(B, a, st);
+    return row_pipe_launch<N, RowRows<N>::value, 1>(B, a, st);
   }
   if (field_ok && phi_ok && variant != 1) return row_pipe_launch<N, RowRows<N>::value>(B, a, st);
   return row_plain_launch<N>(B, a, st);
@@ -528,6 +610,122 @@ col_pass_pipe_kernel(ColArgs a, int n_items) {
   cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// persistent column pass whose tiles arrive by TMA: one thread issues the next
+// tile's 2-D tensor copies (C columns x 256 rows per box) on an mbarrier and
+// every thread goes on with the current tile's FFTs.  With per-thread
+// cp.async staging the issuing threads hold until the memory system takes
+// their requests, so the loads and the FFTs of the pipelined form run one
+// after the other; here they overlap.  Every wait is bounded (%globaltimer,
+// 2 s): on timeout the CTA records an error, waits for its copies in flight
+// and returns.
+// ---------------------------------------------------------------------------
+template <int N, int C>
+struct ColTma {
+  static constexpr int BOX_ROWS = N < 256 ? N : 256;
+  static constexpr int BOXES = N / BOX_ROWS;
+  static constexpr size_t TILE = (size_t)N * C * sizeof(float2);
+  static constexpr size_t STAGE = ColPipe<N, C>::STAGE;   // a multiple of 128 bytes
+  static constexpr size_t SMEM = ColPipe<N, C>::SMEM + 128;  // + slack to align the stages to 128 bytes
+};
+
+template <int N, int C>
+__global__ void __launch_bounds__(C * (N / 16))
+col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
+  constexpr int T = N / 16;
+  constexpr int S = ColStride<N, C>::value;
+  constexpr int NCT = N / C;  // column tiles per realisation
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[2];
+  const int tid = threadIdx.x;
+  const int c = tid % C, t = tid / C;
+  // TMA destinations start on 128-byte boundaries
+  unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
+  auto buf = [&](int s) { return reinterpret_cast<float2*>(sbase + s * ColTma<N, C>::STAGE); };
+  float2* tws = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE);
+  load_twiddles<N>(tws, a.tw);
+  float2* hys = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE + ColPipe<N, C>::TW);
+  if (!a.inv_only)
+    for (int i = tid; i < N; i += blockDim.x) hys[i] = a.hy[i];
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  bool pending[2] = {false, false};  // thread 0: copies issued and not yet waited for
+  auto prefetch = [&](int item, int s) {
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
+    const uint32_t bar = bar0 + 8 * s;
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(buf(s));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                 "r"((uint32_t)ColTma<N, C>::TILE)
+                 : "memory");
+#pragma unroll 1
+    for (int b = 0; b < ColTma<N, C>::BOXES; ++b)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+          "[%5];\n" ::"r"(dst + (uint32_t)(b * ColTma<N, C>::BOX_ROWS * C * sizeof(float2))),
+          "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(2 * x0), "r"(b * ColTma<N, C>::BOX_ROWS), "r"(r), "r"(bar)
+          : "memory");
+    pending[s] = true;
+  };
+  int item = blockIdx.x, s = 0, k = 0;
+  if (tid == 0 && item < n_items) prefetch(item, 0);
+  for (; item < n_items; item += gridDim.x, s ^= 1, ++k) {
+    const int next = item + gridDim.x;
+    if (tid == 0 && next < n_items) prefetch(next, s ^ 1);
+    // item k of this CTA uses stage k & 1 for the (k >> 1)-th time
+    const bool ok = pass_mbar_wait(bar0 + 8 * s, (uint32_t)((k >> 1) & 1));
+    if (tid == 0 && ok) pending[s] = false;
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(&g_pass_error, 1);
+      break;
+    }
+    const int r = item / NCT, x = (item - r * NCT) * C + c;
+    float2* tile = buf(s);
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = tile[(t + m * T) * C + c];
+    __syncthreads();  // the exchange below overwrites the staged tile
+    float2* sm = tile + c * S;
+    if (!a.inv_only) {
+      fft_dev<N, -1, 0, 1>(v, sm, t, tws);
+      const float2 hx = a.hx[x];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(hys[t + m * T], hx));
+    }
+    fft_dev<N, 1, 0, 1>(v, sm, t, tws);
+    float2* f = a.field + (size_t)r * N * N + x;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) f[(size_t)(t + m * T) * N] = v[m];
+    // stage s is refilled by TMA (the async proxy) after the next barrier
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+  }
+  // no copy may land after the CTA leaves: wait (bounded) for any still pending
+  if (tid == 0)
+    for (int q = 0; q < 2; ++q)
+      if (pending[q]) pass_mbar_wait(bar0 + 8 * q, (uint32_t)(((k + (q != s)) >> 1) & 1));
+}
+
+template <int N, int C>
+static cudaError_t col_tma_launch(int B, const ColArgs& a, cudaStream_t st) {
+  alignas(128) CUtensorMap map;
+  if (!encode_field_tiles(&map, a.field, N, B, C, ColTma<N, C>::BOX_ROWS)) return cudaErrorNotSupported;
+  static LaunchCache cache;
+  const int threads = C * (N / 16);
+  const size_t smem = ColTma<N, C>::SMEM;
+  int grid_max = 0;
+  cudaError_t e = cache.get(col_pass_tma_kernel<N, C>, threads, smem, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_items = B * (N / C);
+  const int grid = std::max(1, std::min(n_items, grid_max));
+  col_pass_tma_kernel<N, C><<<grid, threads, smem, st>>>(map, a, n_items);
+  return cudaGetLastError();
+}
+
 template <int N, int C, int TWREC>
 static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
   static LaunchCache cache;
@@ -565,6 +763,13 @@ static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
     return col_pipe_launch<N, C, 0>(B, a, st);
   if (C >= 2 && aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024 && a.variant == 2)
     return col_pipe_launch<N, C, 1>(B, a, st);
+  if constexpr (C == 2 || C == 4) {
+    if (aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024 && a.variant == 3) {
+      const cudaError_t e = col_tma_launch<N, C>(B, a, st);
+      if (e != cudaErrorNotSupported) return e;  // no tensor-map encoder: the pipelined form
+      return col_pipe_launch<N, C, 0>(B, a, st);
+    }
+  }
   return col_plain_launch<N, C>(B, a, st);
 }
 

@@ -596,6 +596,20 @@ static bool encode_operand(EncodeTiledFn fn, CUtensorMap* map, const __half* bas
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// tensor map of a complex64 field [B][N][N] seen as FP32 [B][N][2N], boxes of
+// C columns (2C floats) x box_rows rows: the column pass's tiles
+bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int box_rows) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !map || ((uintptr_t)field & 15) != 0 || (2 * C * 4) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)2 * N, (cuuint64_t)N, (cuuint64_t)B};
+  const cuuint64_t strides[2] = {(cuuint64_t)N * sizeof(float2), (cuuint64_t)N * N * sizeof(float2)};
+  const cuuint32_t box[3] = {(cuuint32_t)(2 * C), (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(field), dims,
+            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 struct TcPlan {
   TmaOperands ops;
   int S, M, Nn, Kp;

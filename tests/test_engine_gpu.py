@@ -224,7 +224,7 @@ def test_autotune_keeps_results(torch_cuda, N):
     choice = plan.autotune(repeats=2)
     assert choice["tuned"] == 1
     assert choice["col_tile"] in (2, 4, 8, 16) and choice["col_tile"] * N // 16 <= 512
-    assert choice["row_variant"] in (0, 1, 2) and choice["col_variant"] in (0, 1, 2)
+    assert choice["row_variant"] in (0, 1, 2, 3) and choice["col_variant"] in (0, 1, 2, 3)
     after = plan.run(*sp).cpu().numpy()
     if choice["col_variant"] == 2:
         np.testing.assert_allclose(after, before, rtol=2e-5, atol=1e-9)
@@ -232,11 +232,11 @@ def test_autotune_keeps_results(torch_cuda, N):
         np.testing.assert_array_equal(after, before)
     # every launch form computes the same arithmetic, except the product
     # twiddles of column variant 2 (FP32 round-off)
-    for rv in (0, 1, 2):
+    for rv in (0, 1, 2, 3):
         for ct in (2, 4, 8, 16):
             if ct * N // 16 > 512:
                 continue
-            for cv in (0, 1, 2):
+            for cv in (0, 1, 2, 3):
                 plan.set_variants(rv, ct, cv)
                 got = plan.run(*sp).cpu().numpy()
                 if cv == 2:
