@@ -115,7 +115,8 @@ typedef struct AtmPlanInfo {
   int32_t col_tile;           /* columns per CTA of the column pass */
   int32_t row_variant;        /* 0: persistent pipelined row pass, 1: one CTA per row block,
                                  2: persistent pipelined with one row per CTA,
-                                 3: as 2 with rows loaded by bulk copies (TMA) */
+                                 3: as 2 with rows loaded by bulk copies (TMA),
+                                 4: as 3 with twiddles formed from powers of two */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile,
                                  2: persistent pipelined with twiddles formed from powers of two,
                                  3: persistent with tiles loaded by TMA (loads overlap the FFTs) */
@@ -246,11 +247,11 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
 
 /* Times the launch variants of the FFT passes on this plan's own workspace
  * (`batch` realisations, `repeats` timed launches each after one warm-up)
- * and keeps the fastest: row-pass variant (four forms), column tile
+ * and keeps the fastest: row-pass variant (five forms), column tile
  * (2..16 columns, at most 512 threads per CTA) and column-pass variant
- * (four forms).  Every form but column variant 2 computes the same bits;
- * column variant 2 forms most twiddles as products of table values and so
- * rounds differently (FP32 round-off, well inside the 1e-4 field bound).  Overwrites the
+ * (four forms).  Every form but row variant 4 and column variant 2 computes
+ * the same bits; those two form most twiddles as products of table values
+ * and so round differently (FP32 round-off, well inside the 1e-4 field bound).  Overwrites the
  * plan's field / screen workspace (zeroes) and blocks until the timing
  * launches finish, so it is called outside CUDA-graph capture, before the
  * runs it tunes.  The reference has no tuner: cupy picks cuFFT plans inside
@@ -267,8 +268,8 @@ int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* s
 
 /* Sets the launch choices atm_autotune makes (row-pass variant 0..2, column
  * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..3)
- * by hand (row variant 0..3).  Results do not change, except for FP32
- * round-off with column variant 2.  No reference counterpart. */
+ * by hand (row variant 0..4).  Results do not change, except for FP32
+ * round-off with row variant 4 and column variant 2.  No reference counterpart. */
 int atm_plan_set_variants(AtmPlan* plan, int32_t row_variant, int32_t col_tile, int32_t col_variant);
 
 /* Launch categories reported by atm_profile_end. */

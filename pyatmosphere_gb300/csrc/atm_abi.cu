@@ -897,7 +897,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   ra.loss = 1.f;
   double best_row = -1.0;
   int row_variant = 0;
-  for (int v = 0; v < 4; ++v) {
+  for (int v = 0; v < 5; ++v) {
     ra.variant = v;
     const double ms = time_it([&] { return atm::launch_row_pass(N, batch, ra, st); });
     if (ms >= 0 && (best_row < 0 || ms < best_row)) {
@@ -945,7 +945,7 @@ int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* s
 
 int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, int32_t col_variant) {
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
-  if (row_variant < 0 || row_variant > 3) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..3", row_variant);
+  if (row_variant < 0 || row_variant > 4) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4", row_variant);
   if (col_variant < 0 || col_variant > 3) return fail(ATM_ERR_INVALID, "col_variant %d not in 0..3", col_variant);
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
     return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);

@@ -56,7 +56,8 @@ struct RowArgs {
   float* step_center;       // [B] post-screen intensity at the grid origin (ROW_STEP)
   int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per row block,
                             // 2: persistent pipeline with one row per CTA (row blocks of several rows otherwise),
-                            // 3: as 2 with the rows moved by bulk copies (TMA) from one thread
+                            // 3: as 2 with the rows moved by bulk copies (TMA) from one thread,
+                            // 4: as 3 with twiddles formed from powers of two (fewer shared loads)
 };
 
 struct ColArgs {

@@ -272,7 +272,7 @@ struct RowPipe {
 // other threads never hold for the memory system and the copies overlap the
 // FFTs (bounded waits: on timeout the CTA records an error, waits for its
 // copies in flight and returns).
-template <int N, int ROWS, int BULK>
+template <int N, int ROWS, int BULK, int TWREC = 0>
 __global__ void __launch_bounds__(ROWS * (N / 16), (ROWS * (N / 16) <= 128) ? 4 : ((ROWS * (N / 16) <= 256) ? 2 : 1))
 row_pass_pipe_kernel(RowArgs a, int n_items) {
   constexpr int T = N / 16;
@@ -368,7 +368,7 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
       for (int m = 0; m < 16; ++m) ph[m] = src[t + m * T];
     }
     __syncthreads();  // the exchange below overwrites the staged rows
-    if (flags & ROW_INV) fft_dev<N, 1, 0, 1>(v, sm, t, tws);
+    if (flags & ROW_INV) fft_dev<N, 1, 0, 1, TWREC>(v, sm, t, tws);
     if (load_phi && (flags & ROW_FOLDED)) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cscale(phasor_turns(ph[m]), a.loss));
@@ -385,7 +385,7 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
       for (int m = 0; m < 16; ++m) v[m] = cscale(v[m], a.loss);
     }
     if (flags & ROW_STEP) measure_step<N, ROWS>(a, v, t, y, r, rb, NRB);
-    if (flags & ROW_FWD) fft_dev<N, -1, 0, 1>(v, sm, t, tws);
+    if (flags & ROW_FWD) fft_dev<N, -1, 0, 1, TWREC>(v, sm, t, tws);
     if (flags & ROW_STORE) {
       float2* dst = (a.store_out && a.out) ? a.out : a.field;
 #pragma unroll
@@ -436,17 +436,17 @@ struct LaunchCache {
   }
 };
 
-template <int N, int ROWS, int BULK = 0>
+template <int N, int ROWS, int BULK = 0, int TWREC = 0>
 static cudaError_t row_pipe_launch(int B, const RowArgs& a, cudaStream_t st) {
   static LaunchCache cache;
   const int threads = ROWS * (N / 16);
   const size_t smem = RowPipe<N, ROWS>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(row_pass_pipe_kernel<N, ROWS, BULK>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(row_pass_pipe_kernel<N, ROWS, BULK, TWREC>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / ROWS);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  row_pass_pipe_kernel<N, ROWS, BULK><<<grid, threads, smem, st>>>(a, n_items);
+  row_pass_pipe_kernel<N, ROWS, BULK, TWREC><<<grid, threads, smem, st>>>(a, n_items);
   return cudaGetLastError();
 }
 
@@ -484,6 +484,11 @@ static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
     if constexpr (one_row)
       if (!meas) return row_pipe_launch<N, 1, 1>(B, a, st);
     return row_pipe_launch<N, RowRows<N>::value, 1>(B, a, st);
+  }
+  if (field_ok && phi_ok && variant == 4) {
+    if constexpr (one_row)
+      if (!meas) return row_pipe_launch<N, 1, 1, 1>(B, a, st);
+    return row_pipe_launch<N, RowRows<N>::value, 1, 1>(B, a, st);
   }
   if (field_ok && phi_ok && variant != 1) return row_pipe_launch<N, RowRows<N>::value>(B, a, st);
   return row_plain_launch<N>(B, a, st);
