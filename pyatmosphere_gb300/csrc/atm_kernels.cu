@@ -980,18 +980,31 @@ __global__ void __launch_bounds__(kEvalCols) screen_eval_kernel(ScreenArgs a) {
   float* Mf = reinterpret_cast<float*>(S + D * D);
   const float2* s_int = a.s_int + (size_t)r * nlc * Di * Di;
   const double2* s_edge = a.s_edge + (size_t)r * nlc * (2 * D - 1);
-  // chunk sums in chunk order, then M = eps_e eps_d i^(e+d) S
+  // chunk sums in chunk order, then M = eps_e eps_d i^(e+d) S.  The interior
+  // (e, d >= 1) only feeds the FP32 Chebyshev columns: compensated FP32 sums
+  // (about the rounding of an FP64 sum to FP32), no FP64 work; the edge row /
+  // column (piston, tilts) stays FP64.
   for (int ed = tid; ed < D * D; ed += blockDim.x) {
     const int e = ed / D, d = ed - e * D;
-    double2 s = make_double2(0.0, 0.0);
     if (e >= 1 && d >= 1) {
       const int idx = (e - 1) * Di + (d - 1);
+      // Re M needs Re S for even e + d, Im S for odd
+      const bool odd = (e + d) & 1;
+      float sum = 0.f, comp = 0.f;
       for (int c = 0; c < nlc; ++c) {
         const float2 v = s_int[(size_t)c * Di * Di + idx];
-        s.x += (double)v.x;
-        s.y += (double)v.y;
+        const float yv = (odd ? v.y : v.x) - comp;
+        const float tv = sum + yv;
+        comp = (tv - sum) - yv;
+        sum = tv;
       }
-    } else {
+      // Re(i^(e+d) S): +Re S, -Im S, -Re S, +Im S for (e + d) mod 4 = 0, 1, 2, 3; eps_e eps_d = 4
+      const int q = (e + d) & 3;
+      Mf[ed] = 4.f * ((q == 0 || q == 3) ? sum : -sum);
+      continue;
+    }
+    double2 s = make_double2(0.0, 0.0);
+    {
       const int idx = e == 0 ? d : D - 1 + e;
       for (int c = 0; c < nlc; ++c) {
         const double2 v = s_edge[(size_t)c * (2 * D - 1) + idx];
@@ -1135,24 +1148,30 @@ __device__ __forceinline__ void split_pair(float u, float w, __half2* hi, __half
                        __float2half_rn((w - __half2float(wh)) * kTcLoScale));
 }
 
+constexpr int kTableRows = 16;  // grid rows per thread: one term record load serves them all
+
 __global__ void __launch_bounds__(128) screen_table_tc_kernel(ScreenArgs a) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y, r = blockIdx.z, N = a.N;
+  const int j0 = blockIdx.y * kTableRows, r = blockIdx.z, N = a.N;
   if (q >= a.P_H) return;
   const HighTerm h = a.hterms[(size_t)r * (a.KH / 2) + q];
-  const uint64_t ju = (uint64_t)j;
-  float sy, cy, sx, cx;
-  sincospi_sfu(fixed_to_halfturns(h.sy * ju + h.oy), &sy, &cy);
-  sincospi_sfu(fixed_to_halfturns(h.sx * ju + h.ox), &sx, &cx);
-  const size_t o = ((size_t)r * N + j) * a.Kp + 2 * q;
-  split_pair(h.v.x * cy - h.v.y * sy, -(h.v.x * sy + h.v.y * cy), reinterpret_cast<__half2*>(a.ta_hi + o),
-             reinterpret_cast<__half2*>(a.ta_lo + o));
-  split_pair(cx, sx, reinterpret_cast<__half2*>(a.tb_hi + o), reinterpret_cast<__half2*>(a.tb_lo + o));
+  const int jn = min(kTableRows, N - j0);
+  for (int jj = 0; jj < jn; ++jj) {
+    const int j = j0 + jj;
+    const uint64_t ju = (uint64_t)j;
+    float sy, cy, sx, cx;
+    sincospi_sfu(fixed_to_halfturns(h.sy * ju + h.oy), &sy, &cy);
+    sincospi_sfu(fixed_to_halfturns(h.sx * ju + h.ox), &sx, &cx);
+    const size_t o = ((size_t)r * N + j) * a.Kp + 2 * q;
+    split_pair(h.v.x * cy - h.v.y * sy, -(h.v.x * sy + h.v.y * cy), reinterpret_cast<__half2*>(a.ta_hi + o),
+               reinterpret_cast<__half2*>(a.ta_lo + o));
+    split_pair(cx, sx, reinterpret_cast<__half2*>(a.tb_hi + o), reinterpret_cast<__half2*>(a.tb_lo + o));
+  }
 }
 
 cudaError_t launch_screen_table_tc(int B, const ScreenArgs& a, cudaStream_t st) {
   if (a.P_H == 0) return cudaSuccess;
-  dim3 grid((a.P_H + 127) / 128, a.N, B);
+  dim3 grid((a.P_H + 127) / 128, (a.N + kTableRows - 1) / kTableRows, B);
   screen_table_tc_kernel<<<grid, 128, 0, st>>>(a);
   return cudaGetLastError();
 }
