@@ -36,7 +36,7 @@ UNIT = "samples/s"
 WORKLOAD = dict(N=2048, delta=1.5e-3, wvl=808e-9, w0=0.12, F0=float("inf"), length=50e3, count=5,
                 Cn2=5e-16, l0=6e-3, L0=1e3, points=1024, f_min=1 / 1e3 / 15, f_max=2 / 6e-3,
                 pupil_radius=0.2)
-WORKLOAD_NAME = ("config-2 advanced channel: 2048^2 grid, delta 1.5 mm, 808 nm, w0 0.12 m, 50 km, "
+WORKLOAD_NAME = ("advanced channel: 2048^2 grid, delta 1.5 mm, 808 nm, w0 0.12 m, 50 km, "
                  "5 SS screens x 1024 annuli, MVK Cn2 5e-16, pupil 0.2 m")
 
 
@@ -282,7 +282,7 @@ def run_gb300(args, rank, world, local_rank):
              "tc-cpasync": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_CPASYNC,
              "tc256": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_N256}[args.gemm]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
-                      pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags)
+                      pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags, cheb_cut=args.cheb_cut)
     if args.variants:
         rv, ct, cv = (int(v) for v in args.variants.split(","))
         plan.set_variants(rv, ct, cv)
@@ -357,7 +357,7 @@ def run_gb300(args, rank, world, local_rank):
     plain = None
     if args.plain > 0 and rank == 0:
         p1 = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
-                        pupils=[(w["pupil_radius"],)], batch=1, device=dev, flags=flags)
+                        pupils=[(w["pupil_radius"],)], batch=1, device=dev, flags=flags, cheb_cut=args.cheb_cut)
         one = [t[:1].contiguous() for t in devin[0]]
         for _ in range(2):
             p1.run(*one)
@@ -481,6 +481,8 @@ def main():
     ap.add_argument("--cpu-realisations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", type=int, default=1, help="time the FFT-pass launch variants first (atm_autotune)")
+    ap.add_argument("--cheb-cut", type=float, default=0.0,
+                    help="annuli below cheb_cut / (N delta) go into the Chebyshev block (0: the engine default)")
     ap.add_argument("--variants", default="",
                     help="row_variant,col_tile,col_variant set by hand instead of atm_autotune (e.g. 2,4,0)")
     ap.add_argument("--mixed-channels", type=int, default=16,

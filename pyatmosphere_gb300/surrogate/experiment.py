@@ -8,8 +8,10 @@
 2. Training on 90 % of the points (engine MLP kernels, Adam).
 3. Held-out evaluation: for `holdout` fresh points the surrogate's CDF is
    compared (KS) with the empirical CDF of `eval-realisations` new
-   realisations of that point; the same is done for the nearest training
-   point's histogram (the method without the network) for comparison.
+   realisations of that point; the same is done for the methods without
+   the network: the nearest training point's histogram and the analytic
+   PDT models fitted to the fresh realisations' own moments
+   (surrogate/baselines.py).
 4. Speed: surrogate queries/s on 100,000 feature vectors against simulated
    queries/s (one point = 256 realisations at N = 1024, the fallback).
 """
@@ -22,6 +24,7 @@ import time
 import numpy as np
 import torch
 
+from .baselines import MODELS, analytic_ks
 from .model import (N_HIST, Box, PointSimulator, SimConfig, Surrogate, features, ks_binned, ks_hist,
                     targets_from_measures)
 
@@ -39,8 +42,11 @@ def load(path: str, device=None) -> Surrogate:
     return s
 
 
-def evaluate(s: Surrogate, box: Box, n_points: int, n_real: int, seed: int, train=None, N=512):
-    """KS of the surrogate (and of nearest-training-point lookup) against fresh simulations."""
+def evaluate(s: Surrogate, box: Box, n_points: int, n_real: int, seed: int, train=None, N=512, baselines=True):
+    """KS of the surrogate against fresh simulations, beside the methods
+    without it: the nearest training point's histogram (given `train`) and
+    the analytic PDT models fitted to the fresh realisations' own moments
+    (`baselines`)."""
     rng = np.random.default_rng(seed)
     P = box.sample(n_points, rng)
     P["l0"] = np.round(P["l0"] * 1e3) / 1e3
@@ -50,22 +56,40 @@ def evaluate(s: Surrogate, box: Box, n_points: int, n_real: int, seed: int, trai
     cfg = SimConfig(N=N, realisations=min(n_real, 2048), seed=seed)
     sim = PointSimulator(cfg, device=s.device)
     ks, ks_nn, kb, kb_nn = [], [], [], []
+    kb_an = {name: [] for name in MODELS}
     for i in range(n_points):
         q = {k: v[i] for k, v in P.items()}
-        etas = []
+        etas, ms = [], []
         for c in range(max(1, n_real // cfg.realisations)):
-            _, eta = targets_from_measures(sim.run(q, 50_000_000 + i * 64 + c), q["aperture"])
+            m = sim.run(q, 50_000_000 + i * 64 + c)
+            _, eta = targets_from_measures(m, q["aperture"])
             etas.append(eta)
+            if baselines:
+                ms.append(m.detach().cpu().numpy())
         eta = np.concatenate(etas)
         ks.append(ks_hist(probs[i], eta))
         kb.append(ks_binned(probs[i], eta))
+        if baselines:
+            for name, v in analytic_ks(np.concatenate(ms), q["aperture"], q["w0"], seed=seed + i).items():
+                kb_an[name].append(v)
         if train is not None:
             Xt, Yt = train
             j = int(np.argmin(((Xt - X[i]) ** 2).sum(axis=1)))
             ks_nn.append(ks_hist(Yt[j, :N_HIST], eta))
             kb_nn.append(ks_binned(Yt[j, :N_HIST], eta))
     sim.plan.close()
-    return {"ks": np.array(ks), "ks_binned": np.array(kb), "ks_nn": np.array(ks_nn), "ks_binned_nn": np.array(kb_nn)}
+    return {"ks": np.array(ks), "ks_binned": np.array(kb), "ks_nn": np.array(ks_nn), "ks_binned_nn": np.array(kb_nn),
+            "ks_binned_analytic": {k: np.array(v) for k, v in kb_an.items()}}
+
+
+def analytic_report(ev) -> dict:
+    """Median / p90 / fraction <= 0.02 of the bin-edge KS per analytic model."""
+    out = {}
+    for name, v in ev.get("ks_binned_analytic", {}).items():
+        if len(v):
+            out[name] = {"median": float(np.median(v)), "p90": float(np.quantile(v, 0.9)),
+                         "frac_le_0.02": float((v <= 0.02).mean())}
+    return out
 
 
 def speed(s: Surrogate, box: Box, n_queries=100_000, seed=3):
@@ -112,8 +136,23 @@ def main():
     ap.add_argument("--weight-decay", type=float, default=1e-4)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--raw-features", action="store_true", help="the 8 raw inputs only (no physics features)")
+    ap.add_argument("--eval-only", default="", help="evaluate this saved model (no data generation or training)")
     a = ap.parse_args()
     box = Box()
+    if a.eval_only:
+        s = load(a.eval_only)
+        t0 = time.perf_counter()
+        ev = evaluate(s, box, a.holdout, a.eval_realisations, seed=a.seed + 100)
+        kb = ev["ks_binned"]
+        rep = {"model": a.eval_only, "holdout_points": a.holdout, "eval_realisations": a.eval_realisations,
+               "ks_binned_median": float(np.median(kb)), "ks_binned_p90": float(np.quantile(kb, 0.9)),
+               "ks_binned_frac_le_0.02": float((kb <= 0.02).mean()), "ks_median": float(np.median(ev["ks"])),
+               "analytic": analytic_report(ev), "ks_noise_floor": 0.87 / np.sqrt(a.eval_realisations),
+               "seconds": time.perf_counter() - t0}
+        with open(a.report, "w") as f:
+            json.dump(rep, f, indent=1)
+        print(json.dumps(rep))
+        return
     t0 = time.perf_counter()
     P, X, Y, _ = Surrogate.generate(box, a.points, SimConfig(realisations=a.realisations), seed=a.seed)
     if a.raw_features:
@@ -147,7 +186,7 @@ def main():
         "ks_binned_mean": float(kb.mean()), "ks_binned_median": float(np.median(kb)),
         "ks_binned_frac_le_0.02": float((kb <= 0.02).mean()), "ks_binned_p90": float(np.quantile(kb, 0.9)),
         "ks_binned_nearest_train_mean": float(kb_nn.mean()), "ks_binned_nearest_train_median": float(np.median(kb_nn)),
-        "ks_noise_floor": 0.87 / np.sqrt(a.eval_realisations),
+        "ks_noise_floor": 0.87 / np.sqrt(a.eval_realisations), "analytic": analytic_report(ev),
         "queries_per_s": q_s, "simulated_queries_per_s": sim_q_s, "speedup": q_s / sim_q_s,
     }
     with open(a.report, "w") as f:

@@ -186,12 +186,12 @@ def main(ref_path):
     res, _, _ = run_realisations(pa, c1, seed=1234, R=4)
     for k, v in res.items():
         g[f"c1_{k}"] = v
-    print(f"config-1 realisations: {time.time() - t:.1f}s")
+    print(f"512^2 channel realisations: {time.time() - t:.1f}s")
     t = time.time()
     res, _, _ = run_realisations(pa, c2, seed=99, R=2, tracked=False)
     for k, v in res.items():
         g[f"c2_{k}"] = v
-    print(f"config-2 realisations: {time.time() - t:.1f}s")
+    print(f"2048^2 channel realisations: {time.time() - t:.1f}s")
 
     # 7. FFT screen with 3 subharmonic levels, normals injected
     rng = np.random.default_rng(5)

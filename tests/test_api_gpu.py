@@ -111,6 +111,28 @@ def test_vacuum_channel_length_override_and_known_answer():
         assert w == pytest.approx(ch.source.get_w(L), rel=1e-3)
 
 
+def test_theory_vacuum_propagation_matches_oracle_and_runs_backwards():
+    """theory.vacuum.vacuum_propagation (theory/vacuum.py:5-7) on the engine:
+    a forward step equals the FP64 oracle's; a step back undoes it."""
+    import torch
+    from pyatmosphere_gb300.theory.vacuum import vacuum_propagation
+    N, delta, wvl, L = 256, 4e-3, 1550e-9, 3e3
+    k = 2 * np.pi / wvl
+    rng = np.random.default_rng(12)
+    x = (np.arange(N) - N // 2) * delta
+    u = (np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / 0.1 ** 2) *
+         np.exp(1j * rng.uniform(0, 0.5, (N, N)))).astype(np.complex64)
+    got = vacuum_propagation(torch.from_numpy(u), L, k, delta, f_delta=1 / (N * delta))
+    assert got.is_cuda and got.dtype == torch.complex64
+    ref = o.vacuum(u, L, k, delta)
+    g = got.cpu().numpy()
+    assert np.linalg.norm(g - ref) / np.linalg.norm(ref) < 2e-5
+    back = vacuum_propagation(got, -L, k, delta).cpu().numpy()
+    assert np.linalg.norm(back - u) / np.linalg.norm(u) < 2e-5
+    with pytest.raises(ValueError):
+        vacuum_propagation(torch.from_numpy(u), L, k, delta, f_delta=2 / (N * delta))
+
+
 def test_screen_generate_matches_oracle():
     import pyatmosphere_gb300 as pa
     ch = small_channel(pa)

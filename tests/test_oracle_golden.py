@@ -61,7 +61,7 @@ def test_psd_matches_reference(golden, cfg):
 
 
 def test_simulation_measures_match_reference(golden):
-    """Beam / PDT / tracked-PDT scalars of 4 config-1 realisations (512^2, 5 screens,
+    """Beam / PDT / tracked-PDT scalars of 4 realisations of the basic channel (512^2, 5 screens,
     1024 spectral points) through the reference's Simulation."""
     spec = o.ChannelSpec()
     base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
