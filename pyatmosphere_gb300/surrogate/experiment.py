@@ -148,6 +148,7 @@ def main():
                "ks_binned_median": float(np.median(kb)), "ks_binned_p90": float(np.quantile(kb, 0.9)),
                "ks_binned_frac_le_0.02": float((kb <= 0.02).mean()), "ks_median": float(np.median(ev["ks"])),
                "analytic": analytic_report(ev), "ks_noise_floor": 0.87 / np.sqrt(a.eval_realisations),
+               "per_point": {"surrogate": kb.tolist(), **{k: v.tolist() for k, v in ev["ks_binned_analytic"].items()}},
                "seconds": time.perf_counter() - t0}
         with open(a.report, "w") as f:
             json.dump(rep, f, indent=1)
