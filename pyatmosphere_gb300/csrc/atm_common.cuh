@@ -20,9 +20,42 @@ namespace atm {
 
 // ---------------------------------------------------------------------------
 // complex helpers (complex64 = float2, complex128 = double2)
+//
+// On the device a complex add or subtract is one packed FP32x2 instruction
+// (add / sub .rn.f32x2, sm_100 and later): each lane rounds like a scalar
+// FADD, so the results are the scalar ones bit for bit, in half the issue
+// slots.  The FFT butterflies are mostly such adds.
 // ---------------------------------------------------------------------------
-ATM_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-ATM_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ uint64_t f2_bits(float2 a) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 bits_f2(uint64_t r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+#endif
+ATM_HD float2 cadd(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__)
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return bits_f2(d);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+ATM_HD float2 csub(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__)
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return bits_f2(d);
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 ATM_HD float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
