@@ -119,7 +119,9 @@ typedef struct AtmPlanInfo {
                                  4: as 3 with twiddles formed from powers of two */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile,
                                  2: persistent pipelined with twiddles formed from powers of two,
-                                 3: persistent with tiles loaded by TMA (loads overlap the FFTs) */
+                                 3: persistent with tiles loaded by TMA (loads overlap the FFTs),
+                                 4: as 3 with the FFT exchanges alternating between two buffers
+                                    (one barrier per exchange instead of two) */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
                                  form (128 x 128 tiles, the default), 3 the same with 128 x 256 tiles */
@@ -266,10 +268,10 @@ int atm_autotune(AtmPlan* plan, int32_t batch, int32_t repeats, void* stream);
  * calculate_structure_function (simulations/structure_function.py:11-12). */
 int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* sf_out, void* stream);
 
-/* Sets the launch choices atm_autotune makes (row-pass variant 0..2, column
- * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..3)
- * by hand (row variant 0..4).  Results do not change, except for FP32
- * round-off with row variant 4 and column variant 2.  No reference counterpart. */
+/* Sets the launch choices atm_autotune makes (row-pass variant 0..4, column
+ * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..4)
+ * by hand.  Results do not change, except for FP32 round-off with row
+ * variant 4 and column variant 2.  No reference counterpart. */
 int atm_plan_set_variants(AtmPlan* plan, int32_t row_variant, int32_t col_tile, int32_t col_variant);
 
 /* Launch categories reported by atm_profile_end. */

@@ -915,7 +915,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   int col_tile = pl->col_tile, col_variant = 0;
   for (int C : {2, 4, 8, 16}) {
     if (C * (N / 16) > 512 || C > N) continue;
-    for (int v = 0; v < 4; ++v) {
+    for (int v = 0; v < 5; ++v) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
       if (ms >= 0 && (best_col < 0 || ms < best_col)) {
@@ -946,7 +946,7 @@ int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* s
 int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, int32_t col_variant) {
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
   if (row_variant < 0 || row_variant > 4) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4", row_variant);
-  if (col_variant < 0 || col_variant > 3) return fail(ATM_ERR_INVALID, "col_variant %d not in 0..3", col_variant);
+  if (col_variant < 0 || col_variant > 4) return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4", col_variant);
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
     return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);
   if (col_tile * (pl->N / 16) > 512 || col_tile > pl->N)

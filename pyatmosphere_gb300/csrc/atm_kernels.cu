@@ -36,6 +36,27 @@ __device__ __forceinline__ void fft_dev(float2 (&v)[16], float2* sm, int t, cons
   }
 }
 
+// The same with the exchanges alternating between two buffers: exchange e
+// writes smA (e even) or smB (e odd) and needs one barrier, not two, since
+// the barrier after the next exchange's writes also certifies that every
+// thread has finished reading this one.  For plans of three stages (N >=
+// 512), so consecutive transforms keep alternating A, B, A, B; the caller
+// owns the barrier between the last read of smB and a later write to it.
+template <int N, int DIR, int s = 0, int TWPAD = 0, int TWREC = 0>
+__device__ __forceinline__ void fft_dev_db(float2 (&v)[16], float2* smA, float2* smB, int t,
+                                           const float2* __restrict__ tw) {
+  static_assert(FftPlan<N>::S == 3, "alternating exchanges need three stages");
+  if constexpr (s == FftPlan<N>::S - 1) {
+    stage_last<N, DIR, TWPAD, TWREC>(v, t, tw);
+  } else {
+    float2* sm = (s & 1) ? smB : smA;
+    stage_to_smem<N, s, DIR, TWPAD, TWREC>(v, sm, t, tw);
+    __syncthreads();
+    stage_from_smem<N, s + 1>(v, sm, t);
+    fft_dev_db<N, DIR, s + 1, TWPAD, TWREC>(v, smA, smB, t, tw);
+  }
+}
+
 // twiddle table copied into shared memory with the pad16 layout
 template <int N>
 __device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restrict__ tw) {
@@ -632,9 +653,14 @@ struct ColTma {
   static constexpr size_t TILE = (size_t)N * C * sizeof(float2);
   static constexpr size_t STAGE = ColPipe<N, C>::STAGE;   // a multiple of 128 bytes
   static constexpr size_t SMEM = ColPipe<N, C>::SMEM + 128;  // + slack to align the stages to 128 bytes
+  // alternating exchanges: a third exchange buffer instead of the hy table
+  static constexpr size_t SMEM_DB = 3 * STAGE + ColPipe<N, C>::TW + 128;
 };
 
-template <int N, int C>
+// DBX = 1: the FFT exchanges alternate between the staged tile and a third
+// buffer (one barrier per exchange instead of two, fft_dev_db); hy is then
+// read through L1 instead of shared memory, which holds the third buffer.
+template <int N, int C, int DBX = 0>
 __global__ void __launch_bounds__(C * (N / 16))
 col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
   constexpr int T = N / 16;
@@ -650,7 +676,8 @@ col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_
   float2* tws = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE);
   load_twiddles<N>(tws, a.tw);
   float2* hys = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE + ColPipe<N, C>::TW);
-  if (!a.inv_only)
+  float2* xbuf = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE + ColPipe<N, C>::TW);
+  if (!DBX && !a.inv_only)
     for (int i = tid; i < N; i += blockDim.x) hys[i] = a.hy[i];
   const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
   if (tid == 0) {
@@ -695,13 +722,24 @@ col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_
     for (int m = 0; m < 16; ++m) v[m] = tile[(t + m * T) * C + c];
     __syncthreads();  // the exchange below overwrites the staged tile
     float2* sm = tile + c * S;
-    if (!a.inv_only) {
-      fft_dev<N, -1, 0, 1>(v, sm, t, tws);
-      const float2 hx = a.hx[x];
+    if constexpr (DBX) {
+      float2* sm2 = xbuf + c * S;
+      if (!a.inv_only) {
+        fft_dev_db<N, -1, 0, 1>(v, sm, sm2, t, tws);
+        const float2 hx = a.hx[x];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(hys[t + m * T], hx));
+        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(__ldg(a.hy + t + m * T), hx));
+      }
+      fft_dev_db<N, 1, 0, 1>(v, sm, sm2, t, tws);
+    } else {
+      if (!a.inv_only) {
+        fft_dev<N, -1, 0, 1>(v, sm, t, tws);
+        const float2 hx = a.hx[x];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(hys[t + m * T], hx));
+      }
+      fft_dev<N, 1, 0, 1>(v, sm, t, tws);
     }
-    fft_dev<N, 1, 0, 1>(v, sm, t, tws);
     float2* f = a.field + (size_t)r * N * N + x;
 #pragma unroll
     for (int m = 0; m < 16; ++m) f[(size_t)(t + m * T) * N] = v[m];
@@ -715,19 +753,19 @@ col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_
       if (pending[q]) pass_mbar_wait(bar0 + 8 * q, (uint32_t)(((k + (q != s)) >> 1) & 1));
 }
 
-template <int N, int C>
+template <int N, int C, int DBX = 0>
 static cudaError_t col_tma_launch(int B, const ColArgs& a, cudaStream_t st) {
   alignas(128) CUtensorMap map;
   if (!encode_field_tiles(&map, a.field, N, B, C, ColTma<N, C>::BOX_ROWS)) return cudaErrorNotSupported;
   static LaunchCache cache;
   const int threads = C * (N / 16);
-  const size_t smem = ColTma<N, C>::SMEM;
+  const size_t smem = DBX ? ColTma<N, C>::SMEM_DB : ColTma<N, C>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(col_pass_tma_kernel<N, C>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(col_pass_tma_kernel<N, C, DBX>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / C);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  col_pass_tma_kernel<N, C><<<grid, threads, smem, st>>>(map, a, n_items);
+  col_pass_tma_kernel<N, C, DBX><<<grid, threads, smem, st>>>(map, a, n_items);
   return cudaGetLastError();
 }
 
@@ -773,6 +811,13 @@ static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
       const cudaError_t e = col_tma_launch<N, C>(B, a, st);
       if (e != cudaErrorNotSupported) return e;  // no tensor-map encoder: the pipelined form
       return col_pipe_launch<N, C, 0>(B, a, st);
+    }
+    if constexpr (FftPlan<N>::S == 3 && ColTma<N, C>::SMEM_DB <= 226 * 1024) {
+      if (aligned16(a.field) && a.variant == 4) {
+        const cudaError_t e = col_tma_launch<N, C, 1>(B, a, st);
+        if (e != cudaErrorNotSupported) return e;
+        return col_pipe_launch<N, C, 0>(B, a, st);
+      }
     }
   }
   return col_plain_launch<N, C>(B, a, st);

@@ -224,7 +224,7 @@ def test_autotune_keeps_results(torch_cuda, N):
     choice = plan.autotune(repeats=2)
     assert choice["tuned"] == 1
     assert choice["col_tile"] in (2, 4, 8, 16) and choice["col_tile"] * N // 16 <= 512
-    assert choice["row_variant"] in (0, 1, 2, 3, 4) and choice["col_variant"] in (0, 1, 2, 3)
+    assert choice["row_variant"] in (0, 1, 2, 3, 4) and choice["col_variant"] in (0, 1, 2, 3, 4)
     after = plan.run(*sp).cpu().numpy()
     if choice["col_variant"] == 2 or choice["row_variant"] == 4:
         np.testing.assert_allclose(after, before, rtol=2e-5, atol=1e-9)
@@ -236,7 +236,7 @@ def test_autotune_keeps_results(torch_cuda, N):
         for ct in (2, 4, 8, 16):
             if ct * N // 16 > 512:
                 continue
-            for cv in (0, 1, 2, 3):
+            for cv in (0, 1, 2, 3, 4):
                 plan.set_variants(rv, ct, cv)
                 got = plan.run(*sp).cpu().numpy()
                 if cv == 2 or rv == 4:
