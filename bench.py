@@ -280,7 +280,8 @@ def run_gb300(args, rank, world, local_rank):
     from pyatmosphere_gb300.engine import _lib
     flags = {"tc": _lib.FLAG_TC_GEMM, "simt": _lib.FLAG_SIMT_GEMM, "auto": 0,
              "tc-cpasync": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_CPASYNC,
-             "tc256": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_N256}[args.gemm]
+             "tc256": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_N256,
+             "tc128": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_N128}[args.gemm]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
                       pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags, cheb_cut=args.cheb_cut)
     if args.variants:
@@ -489,9 +490,10 @@ def main():
                     help="channels of the mixed-size workload leg (0: skip)")
     ap.add_argument("--surrogate-points", type=int, default=8,
                     help="held-out points of the surrogate check (0: skip the surrogate leg)")
-    ap.add_argument("--gemm", choices=["auto", "tc", "tc256", "tc-cpasync", "simt"], default="auto",
-                    help="screen GEMM on tensor cores (tc: persistent TMA form with 128 x 128 tiles, the default "
-                         "at 2048^2; tc256: 128 x 256 tiles; tc-cpasync: one CTA per tile) or FP32 SIMT cores")
+    ap.add_argument("--gemm", choices=["auto", "tc", "tc256", "tc128", "tc-cpasync", "simt"], default="auto",
+                    help="screen GEMM on tensor cores (tc / tc256: persistent TMA form with 128 x 256 tiles, the "
+                         "default at 2048^2; tc128: 128 x 128 tiles with double-buffered accumulators; "
+                         "tc-cpasync: one CTA per tile) or FP32 SIMT cores")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

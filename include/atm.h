@@ -53,8 +53,10 @@ extern "C" {
 #define ATM_FLAG_TC_CPASYNC 4    /* tensor-core GEMM in its one-CTA-per-tile cp.async form instead of the
                                     persistent TMA form */
 #define ATM_FLAG_STEP_MEASURES 8 /* also measure the field just after every screen (per-step measures) */
-#define ATM_FLAG_TC_N256 16      /* persistent TMA GEMM with 128 x 256 tiles, two stages and one accumulator pair
-                                    (default: 128 x 128 tiles, three stages, double-buffered accumulators) */
+#define ATM_FLAG_TC_N256 16      /* persistent TMA GEMM with 128 x 256 tiles, two stages, one accumulator pair
+                                    and TMA-stored result blocks (the default form; the flag is kept) */
+#define ATM_FLAG_TC_N128 32      /* persistent TMA GEMM with 128 x 128 tiles, three stages and double-buffered
+                                    accumulators instead of the default 128 x 256 form */
 
 /* per-realisation doubles in measures_out (slot index).  With
  * ATM_FLAG_STEP_MEASURES, ATM_STEP_SLOTS more doubles per screen i follow the
@@ -124,7 +126,8 @@ typedef struct AtmPlanInfo {
                                     (one barrier per exchange instead of two) */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
-                                 form (128 x 128 tiles, the default), 3 the same with 128 x 256 tiles */
+                                 form with 128 x 128 tiles (ATM_FLAG_TC_N128), 3 the same with 128 x 256
+                                 tiles and TMA-stored result blocks (the default) */
 } AtmPlanInfo;
 
 /* ABI version of the loaded library (ATM_ABI_VERSION). */

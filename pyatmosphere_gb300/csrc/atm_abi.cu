@@ -164,7 +164,7 @@ struct AtmPlan {
   bool step_meas = false;
   int step_slot0 = 0;
   atm::TcPlan* tcp = nullptr;  // TMA descriptors of the screen GEMM (null: cp.async form)
-  bool tc_n256 = false;        // the TMA form with 128 x 256 tiles (default: 128 x 128, double-buffered)
+  bool tc_n256 = false;        // the TMA form with 128 x 256 tiles (the default; ATM_FLAG_TC_N128: 128 x 128)
   std::vector<DevBuf*> bufs;
   int64_t bytes() const {
     int64_t s = 0;
@@ -470,8 +470,8 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
     if (!(d->flags & ATM_FLAG_TC_CPASYNC))
       pl->tcp = atm::tc_plan_create(pl->B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p,
                                     (const __half*)pl->ta_lo.p, (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p,
-                                    (d->flags & ATM_FLAG_TC_N256) ? 256 : 128);
-    pl->tc_n256 = pl->tcp && (d->flags & ATM_FLAG_TC_N256);
+                                    (d->flags & ATM_FLAG_TC_N128) ? 128 : 256);
+    pl->tc_n256 = pl->tcp && !(d->flags & ATM_FLAG_TC_N128);
   }
   if (pl->n > 0) {
     const size_t simt_rows = pl->use_tc ? 0 : 1;  // FP32 SIMT tables only without tensor cores

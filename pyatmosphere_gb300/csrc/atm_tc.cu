@@ -16,10 +16,16 @@
 // (cp.async.bulk.tensor) into a ring of stages, running ahead into the next
 // tile; warp 1 issues the MMAs; warps 2-9 drain the accumulators (tcgen05.ld,
 // combine, scale, optionally add 1-D phases fold_y[y] + fold_x[x], store).
-// Default: 128 x 128 output tiles, three stages and two accumulator pairs
-// (4 x 128 TMEM columns), so a tile's drain overlaps the next tile's MMAs;
-// the 128 x 256 form (two stages, one pair) moves a third less operand data
-// per FLOP but waits for each drain.  mbarriers: full / empty per stage,
+// Default: 128 x 256 output tiles, two stages and one accumulator pair
+// (2 x 256 TMEM columns).  Its MMAs run near the tensor peak (the operands of
+// a 128-wide MMA need more shared-memory bandwidth per FLOP), but the pair
+// must be drained before the next tile starts, so the drain is kept short:
+// each epilogue warp reads its TMEM block, releases the pair after its last
+// read, and stores the block through a 4 KB swizzled staging buffer with a
+// TMA tensor store (one store per 32 x 32 block instead of 32 rows per store
+// instruction).  The 128 x 128 form (three stages, two accumulator pairs:
+// the drain overlaps the next tile's MMAs, global stores from registers)
+// stays behind ATM_FLAG_TC_N128.  mbarriers: full / empty per stage,
 // full / empty per accumulator pair.
 // tc_gemm_kernel: the first form, one CTA per tile, operands through cp.async
 // by all threads (kept for comparison and as the fallback when the driver
@@ -274,13 +280,18 @@ __global__ void __launch_bounds__(THREADS, 1) tc_gemm_kernel(TcArgs a) {
 constexpr int P_THREADS = 320;    // warp 0: TMA, warp 1: MMA, warps 2-9: epilogue
 constexpr int EPI_THREADS = 256;  // two warps per TMEM lane quarter, each draining half of the columns
 
-template <int TNT, int STG, int NACC>
+// EPI = 1: each epilogue warp writes its 32 x 32 result blocks into its own
+// 4 KB staging buffer (128-byte swizzle) and one lane stores the block with a
+// TMA tensor store, instead of 32 rows per store instruction from registers.
+constexpr int EPI_STAGE = 32 * 32 * 4;  // bytes per epilogue warp
+template <int TNT, int STG, int NACC, int EPI = 0>
 struct TmaCfg {
   static constexpr int B_SL = TNT * ROWB;                 // one FP16 slice of the B tile
   static constexpr int STAGE_B = 2 * A_SLICE + 2 * B_SL;  // A_hi, A_lo, B_hi, B_lo
-  static constexpr int SMEM = STG * STAGE_B + 1024;
+  static constexpr int SMEM = STG * STAGE_B + (EPI ? 8 * EPI_STAGE : 0) + 1024;
   static_assert(NACC * 2 * TNT <= 512, "accumulators exceed the 512 TMEM columns");
-  static_assert(SMEM <= 227 * 1024, "stages exceed shared memory");
+  static_assert(SMEM <= 227 * 1024 - 256, "stages exceed shared memory");
+  static_assert(STAGE_B % 1024 == 0, "staging buffers need 1024-byte alignment for the 128-byte swizzle");
 };
 
 template <int NT>
@@ -312,6 +323,17 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, uint32_t src, int x, int y, int z) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];\n" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z), "r"(src)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// the staging buffer may be rewritten: every committed store has read it
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+// every committed store has completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
 }
@@ -350,11 +372,12 @@ __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int
   *n0 = (r - (r / tiles_n) * tiles_n) * tn;
 }
 
-template <int TNT, int STG, int NACC>
+template <int TNT, int STG, int NACC, int EPI = 0>
 __global__ void __launch_bounds__(P_THREADS, 1)
-    tc_gemm_tma_kernel(const __grid_constant__ TmaOperands ops, float* __restrict__ out, int S, int M, int Nn, int Kp,
-                       float scale, const float* __restrict__ fold_y, const float* __restrict__ fold_x) {
-  using Cfg = TmaCfg<TNT, STG, NACC>;
+    tc_gemm_tma_kernel(const __grid_constant__ TmaOperands ops, const __grid_constant__ CUtensorMap outmap,
+                       float* __restrict__ out, int S, int M, int Nn, int Kp, float scale,
+                       const float* __restrict__ fold_y, const float* __restrict__ fold_x) {
+  using Cfg = TmaCfg<TNT, STG, NACC, EPI>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STG], empty_bar[STG], accf_bar[NACC], acce_bar[NACC], drain_bar;
   __shared__ uint32_t tmem_holder;
@@ -474,6 +497,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     const int q = warp & 3;
     const int row = q * 32 + lane;
     const int cbeg = ((warp - 2) >> 2) * (TNT / 2);
+    const uint32_t stg = base + (uint32_t)(STG * Cfg::STAGE_B) + (uint32_t)((warp - 2) * EPI_STAGE);
     int n_done = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++n_done) {
       const int acc = n_done % NACC;
@@ -510,7 +534,20 @@ __global__ void __launch_bounds__(P_THREADS, 1)
               "=r"(l[24]), "=r"(l[25]), "=r"(l[26]), "=r"(l[27]), "=r"(l[28]), "=r"(l[29]), "=r"(l[30]), "=r"(l[31])
             : "r"(d1 + c0));
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if constexpr (EPI) {
+          // this thread's last TMEM read of the tile: the MMAs of the next
+          // tile may start while the block is combined and stored
+          if (c0 + 32 == cbeg + TNT / 2) {
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            mbar_arrive(smem_u32(&acce_bar[acc]));
+          }
+        }
         const float lo_scale = scale / kTcLoScale;
+        if constexpr (EPI) {
+          // the previous block's store has read the staging buffer
+          if (lane == 0) bulk_wait_read_all();
+          __syncwarp();
+        }
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
           // the 1-D phases (turns, each in [-1/2, 1/2]) join the product
@@ -527,12 +564,33 @@ __global__ void __launch_bounds__(P_THREADS, 1)
           v.y = fmaf(__uint_as_float(l[j + 1]), lo_scale, fmaf(__uint_as_float(h[j + 1]), scale, f.y));
           v.z = fmaf(__uint_as_float(l[j + 2]), lo_scale, fmaf(__uint_as_float(h[j + 2]), scale, f.z));
           v.w = fmaf(__uint_as_float(l[j + 3]), lo_scale, fmaf(__uint_as_float(h[j + 3]), scale, f.w));
-          *reinterpret_cast<float4*>(o + c0 + j) = v;
+          if constexpr (EPI) {
+            // row `lane`, 16-byte chunk j / 4, 128-byte swizzle (chunk ^ row % 8)
+            const uint32_t a16 = stg + (uint32_t)lane * 128u + ((uint32_t)((j >> 2) ^ (lane & 7)) << 4);
+            asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"r"(a16), "f"(v.x), "f"(v.y), "f"(v.z),
+                         "f"(v.w)
+                         : "memory");
+          } else {
+            *reinterpret_cast<float4*>(o + c0 + j) = v;
+          }
+        }
+        if constexpr (EPI) {
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          __syncwarp();
+          if (lane == 0) {
+            tma_store_3d(&outmap, stg, n0 + c0, m0 + q * 32, s);
+            bulk_commit();
+          }
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      mbar_arrive(smem_u32(&acce_bar[acc]));
+      if constexpr (!EPI) {
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        mbar_arrive(smem_u32(&acce_bar[acc]));
+      }
     }
+    // no store may read the staging buffer after the CTA leaves
+    if constexpr (EPI)
+      if (lane == 0) bulk_wait_all();
   }
 
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -638,17 +696,35 @@ TcPlan* tc_plan_create(int S, int M, int Nn, int Kp, const __half* a_hi, const _
 
 void tc_plan_destroy(TcPlan* p) { delete p; }
 
-template <int TNT, int STG, int NACC>
+// [S][M][Nn] FP32 output, boxes of 32 x 32, 128-byte swizzle: the staged
+// epilogue's TMA stores
+static bool encode_output(EncodeTiledFn fn, CUtensorMap* map, float* out, int S, int M, int Nn) {
+  if (((uintptr_t)out & 15) != 0 || (Nn * 4) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)Nn, (cuuint64_t)M, (cuuint64_t)S};
+  const cuuint64_t strides[2] = {(cuuint64_t)Nn * sizeof(float), (cuuint64_t)M * Nn * sizeof(float)};
+  const cuuint32_t box[3] = {32, 32, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, out, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int TNT, int STG, int NACC, int EPI>
 static cudaError_t launch_tma_form(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
                                    const float* fold_x, cudaStream_t st) {
-  using Cfg = TmaCfg<TNT, STG, NACC>;
+  using Cfg = TmaCfg<TNT, STG, NACC, EPI>;
+  alignas(64) CUtensorMap outmap{};
+  if (EPI) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn || !encode_output(fn, &outmap, out, S, p->M, p->Nn)) return cudaErrorNotSupported;
+  }
   static int sms[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (sms[dev] == 0) {
-    e = cudaFuncSetAttribute(tc_gemm_tma_kernel<TNT, STG, NACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(tc_gemm_tma_kernel<TNT, STG, NACC, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              Cfg::SMEM);
     if (e != cudaSuccess) return e;
     int n = 0;
@@ -658,8 +734,8 @@ static cudaError_t launch_tma_form(const TcPlan* p, int S, float* out, float sca
   }
   const int n_tiles = S * (p->M / TM) * (p->Nn / TNT);
   const int grid = std::min(n_tiles, sms[dev]);
-  tc_gemm_tma_kernel<TNT, STG, NACC><<<grid, P_THREADS, Cfg::SMEM, st>>>(p->ops, out, S, p->M, p->Nn, p->Kp, scale,
-                                                                          fold_y, fold_x);
+  tc_gemm_tma_kernel<TNT, STG, NACC, EPI><<<grid, P_THREADS, Cfg::SMEM, st>>>(p->ops, outmap, out, S, p->M, p->Nn,
+                                                                               p->Kp, scale, fold_y, fold_x);
   return cudaGetLastError();
 }
 
@@ -667,8 +743,8 @@ cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, 
                                const float* fold_x, cudaStream_t st) {
   if (!p || S < 1 || S > p->S || !out || (!fold_y) != (!fold_x)) return cudaErrorInvalidValue;
   if (((uintptr_t)fold_x & 15) != 0) return cudaErrorMisalignedAddress;
-  if (p->tn == 128) return launch_tma_form<128, 3, 2>(p, S, out, scale, fold_y, fold_x, st);
-  return launch_tma_form<256, 2, 1>(p, S, out, scale, fold_y, fold_x, st);
+  if (p->tn == 128) return launch_tma_form<128, 3, 2, 0>(p, S, out, scale, fold_y, fold_x, st);
+  return launch_tma_form<256, 2, 1, 1>(p, S, out, scale, fold_y, fold_x, st);
 }
 
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,

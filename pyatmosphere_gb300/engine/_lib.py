@@ -22,6 +22,7 @@ FLAG_TC_GEMM = 2
 FLAG_TC_CPASYNC = 4
 FLAG_STEP_MEASURES = 8
 FLAG_TC_N256 = 16
+FLAG_TC_N128 = 32
 STEP_SLOTS = 8
 SOURCE_GAUSSIAN = 0
 SOURCE_PLANE = 1

@@ -92,9 +92,9 @@ def test_tc_channel_4096_matches_oracle():
 
 
 def test_tc_forms_agree_on_a_channel():
-    """The persistent TMA form (128 x 128 tiles) is the default; its 128 x 256
-    form gives the same measures, the cp.async form (flag) the same to FP32
-    round-off."""
+    """The persistent TMA form with 128 x 256 tiles is the default; its 128 x
+    128 form (flag) gives the same measures, the cp.async form (flag) the same
+    to FP32 round-off."""
     import torch
     from oracle import atm_oracle as o
     from pyatmosphere_gb300.engine import EnginePlan, _lib
@@ -108,11 +108,11 @@ def test_tc_forms_agree_on_a_channel():
                      pupils=[(0.1,)], batch=4)
     cpa = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, f_base=base,
                      pupils=[(0.1,)], batch=4, flags=_lib.FLAG_TC_CPASYNC)
-    assert tma.info["gemm_form"] == 2 and cpa.info["gemm_form"] == 1
-    t256 = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, f_base=base,
-                      pupils=[(0.1,)], batch=4, flags=_lib.FLAG_TC_N256)
-    assert t256.info["gemm_form"] == 3
-    np.testing.assert_allclose(t256.run(*sp).cpu().numpy(), tma.run(*sp).cpu().numpy(), rtol=1e-6, atol=1e-12)
+    assert tma.info["gemm_form"] == 3 and cpa.info["gemm_form"] == 1
+    t128 = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, f_base=base,
+                      pupils=[(0.1,)], batch=4, flags=_lib.FLAG_TC_N128)
+    assert t128.info["gemm_form"] == 2
+    np.testing.assert_allclose(t128.run(*sp).cpu().numpy(), tma.run(*sp).cpu().numpy(), rtol=1e-6, atol=1e-12)
     a, b = tma.run(*sp).cpu().numpy(), cpa.run(*sp).cpu().numpy()
     # the TMA form also folds the 1-D phases into the GEMM output (one FP32
     # rounding more): integrated measures to 2e-5, the one-pixel intensity to 1e-4
