@@ -390,7 +390,10 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
     }
     __syncthreads();  // the exchange below overwrites the staged rows
     if (flags & ROW_INV) fft_dev<N, 1, 0, 1, TWREC>(v, sm, t, tws);
-    if (load_phi && (flags & ROW_FOLDED)) {
+    if (load_phi && (flags & ROW_FOLDED) && a.loss == 1.0f) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], phasor_turns(ph[m]));  // lossless step: no scaling
+    } else if (load_phi && (flags & ROW_FOLDED)) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cscale(phasor_turns(ph[m]), a.loss));
     } else if (load_phi) {
