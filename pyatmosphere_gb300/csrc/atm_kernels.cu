@@ -245,7 +245,12 @@ row_pass_kernel(RowArgs a) {
     for (int m = 0; m < 16; ++m) v[m] = a.field[rowoff + t + m * T];
   }
   if (flags & ROW_INV) fft_dev<N, 1>(v, sm, t, a.tw);
-  if ((flags & ROW_PHASOR) && (flags & ROW_FOLDED)) {
+  if ((flags & ROW_PHASOR) && (flags & ROW_FOLDED) && a.loss == 1.0f) {
+    // the arithmetic of the persistent forms: a lossless step multiplies by the bare phasor
+    const float* ph = a.phi + rowoff;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], phasor_turns(ph[t + m * T]));
+  } else if ((flags & ROW_PHASOR) && (flags & ROW_FOLDED)) {
     const float* ph = a.phi + rowoff;
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cscale(phasor_turns(ph[t + m * T]), a.loss));
