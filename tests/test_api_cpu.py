@@ -97,3 +97,18 @@ def test_step_values_resolve_to_screens_then_receiver():
     assert v.tolist() == [[0, 1, 2, 7], [10, 11, 12, 8]]
     r = resolve(("step_mean_r",), out, pupils, [], n)
     assert r[:, :3].tolist() == [[5.0] * 3] * 2 and r[:, 3].tolist() == [0.0, 0.0]
+
+
+def test_theory_vacuum_rejects_other_grids_before_touching_a_device():
+    """theory.vacuum.vacuum_propagation runs on the field's own frequency grid
+    (f_delta = 1 / (N delta)); other grids and non-square fields are refused."""
+    import numpy as np
+    import pytest
+    from pyatmosphere_gb300.theory.vacuum import vacuum_propagation
+    u = np.zeros((64, 64), np.complex64)
+    with pytest.raises(ValueError):
+        vacuum_propagation(u, 1e3, 2 * np.pi / 1e-6, 1e-3, f_delta=1.0)
+    with pytest.raises(ValueError):
+        vacuum_propagation(np.zeros((64, 32), np.complex64), 1e3, 2 * np.pi / 1e-6, 1e-3)
+    with pytest.raises(ValueError):
+        vacuum_propagation(u, 1e3, 2 * np.pi / 1e-6, 1e-3, f2=np.zeros((32, 32)))
