@@ -137,6 +137,9 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--raw-features", action="store_true", help="the 8 raw inputs only (no physics features)")
     ap.add_argument("--eval-only", default="", help="evaluate this saved model (no data generation or training)")
+    ap.add_argument("--save-data", default="", help="also write the generated training set (features, targets) here")
+    ap.add_argument("--load-data", default="", help="train on a training set written by --save-data instead of "
+                                                     "simulating one (--points and --realisations are taken from it)")
     a = ap.parse_args()
     box = Box()
     if a.eval_only:
@@ -155,7 +158,14 @@ def main():
         print(json.dumps(rep))
         return
     t0 = time.perf_counter()
-    P, X, Y, _ = Surrogate.generate(box, a.points, SimConfig(realisations=a.realisations), seed=a.seed)
+    if a.load_data:
+        z = np.load(a.load_data)
+        X, Y = z["X"], z["Y"]
+        a.points, a.realisations, a.seed = int(z["points"]), int(z["realisations"]), int(z["seed"])
+    else:
+        _, X, Y, _ = Surrogate.generate(box, a.points, SimConfig(realisations=a.realisations), seed=a.seed)
+        if a.save_data:
+            np.savez_compressed(a.save_data, X=X, Y=Y, points=a.points, realisations=a.realisations, seed=a.seed)
     if a.raw_features:
         X = X[:, :8]
     t_gen = time.perf_counter() - t0
@@ -179,7 +189,7 @@ def main():
     q_s, sim_q_s = speed(s, box)
     rep = {
         "points": a.points, "realisations_per_point": a.realisations, "train_points": n_tr,
-        "generation_s": t_gen, "training_s": t_train, "steps": a.steps, "loss_curve": losses,
+        "data": a.load_data or "simulated", "generation_s": t_gen, "training_s": t_train, "steps": a.steps, "loss_curve": losses,
         "val_kl": kl_val, "holdout_points": a.holdout, "eval_realisations": a.eval_realisations,
         "ks_mean": float(ks.mean()), "ks_median": float(np.median(ks)), "ks_p90": float(np.quantile(ks, 0.9)),
         "ks_frac_le_0.02": float((ks <= 0.02).mean()),
