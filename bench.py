@@ -488,7 +488,7 @@ def main():
                     help="row_variant,col_tile,col_variant set by hand instead of atm_autotune (e.g. 2,4,0)")
     ap.add_argument("--mixed-channels", type=int, default=16,
                     help="channels of the mixed-size workload leg (0: skip)")
-    ap.add_argument("--surrogate-points", type=int, default=8,
+    ap.add_argument("--surrogate-points", type=int, default=32,
                     help="held-out points of the surrogate check (0: skip the surrogate leg)")
     ap.add_argument("--gemm", choices=["auto", "tc", "tc256", "tc128", "tc-cpasync", "simt"], default="auto",
                     help="screen GEMM on tensor cores (tc / tc256: persistent TMA form with 128 x 256 tiles, the "
