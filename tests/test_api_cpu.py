@@ -112,3 +112,27 @@ def test_theory_vacuum_rejects_other_grids_before_touching_a_device():
         vacuum_propagation(np.zeros((64, 32), np.complex64), 1e3, 2 * np.pi / 1e-6, 1e-3)
     with pytest.raises(ValueError):
         vacuum_propagation(u, 1e3, 2 * np.pi / 1e-6, 1e-3, f2=np.zeros((32, 32)))
+
+
+def test_mixed_workload_sampler_follows_its_distribution():
+    """engine.uneven.sample_mixed: N from the size set with N delta = 3 m,
+    screen counts on the closed range, log-uniform L and Cn2 inside their
+    ranges, F0 either infinity or L; middle-of-slab screen positions."""
+    import math
+    import numpy as np
+    from pyatmosphere_gb300.engine.uneven import sample_mixed
+    chans = sample_mixed(400, np.random.default_rng(5))
+    assert {c.N for c in chans} == {512, 1024, 2048, 4096}
+    assert all(abs(c.N * c.delta - 3.0) < 1e-12 for c in chans)
+    counts = [c.n_screens for c in chans]
+    assert min(counts) == 3 and max(counts) == 20
+    assert all(1e3 <= c.length <= 1e5 and 1e-16 <= c.Cn2 <= 1e-14 and 0.02 <= c.w0 <= 0.2 for c in chans)
+    assert {c.wvl for c in chans} == {808e-9, 1550e-9}
+    assert {math.isinf(c.F0) for c in chans} == {True, False}
+    assert all(c.F0 == c.length for c in chans if not math.isinf(c.F0))
+    c = chans[0]
+    pos = c.positions()
+    np.testing.assert_allclose(np.diff(pos), c.length / c.n_screens)
+    assert pos[0] == pytest.approx(0.5 * c.length / c.n_screens)
+    b = c.base()
+    assert b[0] == pytest.approx(c.f_min, rel=1e-6) and b[-1] == pytest.approx(2 / c.l0, rel=1e-6)
