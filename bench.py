@@ -283,6 +283,7 @@ def run_gb300(args, rank, world, local_rank):
              "tc-cpasync": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_CPASYNC,
              "tc256": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_N256,
              "tc128": _lib.FLAG_TC_GEMM | _lib.FLAG_TC_N128}[args.gemm]
+    flags |= {"auto": 0, "tiled": _lib.FLAG_TILED, "rowmajor": _lib.FLAG_ROWMAJOR}[args.layout]
     plan = EnginePlan(w["N"], w["delta"], w["wvl"], w["w0"], w["F0"], pos, w["length"], f_base=base,
                       pupils=[(w["pupil_radius"],)], batch=B, device=dev, flags=flags, cheb_cut=args.cheb_cut)
     if args.variants:
@@ -451,6 +452,7 @@ def run_gb300(args, rank, world, local_rank):
             "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B, "gemm": args.gemm,
                        "l2": "inputs larger than L2 (field batch 8.6 GB per step)", "gemm_k": K,
                        "low_annuli": info["low_annuli"], "cheb_terms": info["cheb_terms"], "autotune": tuned,
+                       "field_layout": "tiled 4x4 blocks" if info.get("tiled") else "row-major",
                        "gemm_form": ["fp32 simt", "tcgen05 cp.async", "tcgen05 persistent tma 128x128",
                                      "tcgen05 persistent tma 128x256"][info["gemm_form"]]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -485,6 +487,8 @@ def main():
     ap.add_argument("--autotune", type=int, default=1, help="time the FFT-pass launch variants first (atm_autotune)")
     ap.add_argument("--cheb-cut", type=float, default=0.0,
                     help="annuli below cheb_cut / (N delta) go into the Chebyshev block (0: the engine default)")
+    ap.add_argument("--layout", choices=["auto", "tiled", "rowmajor"], default="auto",
+                    help="field layout between the FFT passes (tiled: 4 x 4 blocks of 128 bytes)")
     ap.add_argument("--variants", default="",
                     help="row_variant,col_tile,col_variant set by hand instead of atm_autotune (e.g. 2,4,0)")
     ap.add_argument("--mixed-channels", type=int, default=16,

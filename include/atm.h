@@ -41,6 +41,8 @@ extern "C" {
 #define ATM_ERR_UNSUPPORTED (-2) /* e.g. N not a power of two in [128, 4096] */
 #define ATM_ERR_CUDA (-3)        /* CUDA runtime error (message has details) */
 #define ATM_ERR_NOMEM (-4)       /* device allocation failed */
+#define ATM_ERR_TIMEOUT (-5)     /* a kernel's bounded wait ran out (atm_plan_check) */
+#define ATM_ERR_NONFINITE (-6)   /* NaN or infinite spectrum values were injected (atm_plan_check) */
 
 #define ATM_SOURCE_GAUSSIAN 0    /* GaussianSource (sources.py:21-23) */
 #define ATM_SOURCE_PLANE 1       /* PlaneSource (sources.py:16-18) */
@@ -57,6 +59,10 @@ extern "C" {
                                     and TMA-stored result blocks (the default form; the flag is kept) */
 #define ATM_FLAG_TC_N128 32      /* persistent TMA GEMM with 128 x 128 tiles, three stages and double-buffered
                                     accumulators instead of the default 128 x 256 form */
+#define ATM_FLAG_TILED 64        /* keep the plan's field between passes in the tiled layout (4 x 4 blocks of
+                                    128 bytes): the column pass then moves whole 128-byte lines; N in
+                                    {512, 1024, 2048}.  Inputs and outputs of every call stay row-major. */
+#define ATM_FLAG_ROWMAJOR 128    /* keep the plan's field row-major where the tiled layout would be the default */
 
 /* per-realisation doubles in measures_out (slot index).  With
  * ATM_FLAG_STEP_MEASURES, ATM_STEP_SLOTS more doubles per screen i follow the
@@ -118,16 +124,20 @@ typedef struct AtmPlanInfo {
   int32_t row_variant;        /* 0: persistent pipelined row pass, 1: one CTA per row block,
                                  2: persistent pipelined with one row per CTA,
                                  3: as 2 with rows loaded by bulk copies (TMA),
-                                 4: as 3 with twiddles formed from powers of two */
+                                 4: as 3 with twiddles formed from powers of two,
+                                 5: tiled layout, four rows per CTA with a named barrier per row,
+                                 6: as 5 with twiddles formed from powers of two */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile,
                                  2: persistent pipelined with twiddles formed from powers of two,
                                  3: persistent with tiles loaded by TMA (loads overlap the FFTs),
                                  4: as 3 with the FFT exchanges alternating between two buffers
-                                    (one barrier per exchange instead of two) */
+                                    (one barrier per exchange instead of two),
+                                 5: as 4 on the tiled layout (block columns of 4 columns) */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
                                  form with 128 x 128 tiles (ATM_FLAG_TC_N128), 3 the same with 128 x 256
                                  tiles and TMA-stored result blocks (the default) */
+  int32_t tiled;              /* 1: the plan's field is kept in the tiled layout between passes */
 } AtmPlanInfo;
 
 /* ABI version of the loaded library (ATM_ABI_VERSION). */
@@ -302,6 +312,25 @@ int atm_profile_end(AtmPlan* plan, double* ms_by_kind, int32_t* launches_by_kind
  * time in *ms; FLOPs = blocks * 256 * iters * 16.  No reference counterpart:
  * the roofline denominator for the FP32 screen GEMM. */
 int atm_fma_probe(int32_t blocks, int32_t iters, double* ms, void* stream);
+
+/* Waits for the plan's work on `stream` and reports what its kernels
+ * recorded since the last check: ATM_ERR_TIMEOUT if a bounded device wait ran
+ * out (a TMA-fed FFT pass or the tensor-core GEMM; the CTA drained its copies
+ * and MMAs, freed its TMEM and returned), ATM_ERR_NONFINITE if a spectrum
+ * value was NaN or infinite (the term was dropped).  Either way the runs since
+ * the last check wrote NaN measures (the canary for callers that do not
+ * check), and the call clears the record.  The reference has no counterpart:
+ * its only failure handling is the KeyboardInterrupt flush of
+ * Simulation.run (simulations/simulation.py:135-138). */
+int atm_plan_check(AtmPlan* plan, void* stream);
+
+/* Budget in ns (default 2e9) of the device waits for work in the FFT passes
+ * and the screen GEMM on the current device: a tile or operand stage that has
+ * not landed, a stage or accumulator not yet released.  The waits that drain
+ * copies and MMAs before a CTA leaves keep their 2 s bound.  A budget far
+ * below a kernel's latency makes the waits run out: the failure path that
+ * atm_plan_check reports.  No reference counterpart. */
+int atm_set_wait_budget(uint64_t ns);
 
 /* Allocation-free variant of atm_vacuum, for callers that cannot allocate
  * device memory where they propagate (their framework's caching allocator

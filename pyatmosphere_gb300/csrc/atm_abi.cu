@@ -138,6 +138,7 @@ struct AtmPlan {
   double delta = 0, wvl = 0, w0 = 0, F0 = 0, length = 0, losses_db = 0, kw = 0, sx = 0, sy = 0;
   int path_output_loss = 0, source_kind = 0, col_tile = 0;
   int row_variant = 0, col_variant = 0, tuned = 0;  // launch choices (atm_autotune)
+  bool tiled = false;  // field kept in the tiled layout between passes (ATM_FLAG_TILED)
   int P_L = 0, D = 2, P_H = 0, KH = 0, KC = 0;
   int rows = 1, n_parts = 0, n_meas = 0, n_out = 0;
   std::vector<double> positions, dz;      // dz[0..n]
@@ -161,6 +162,7 @@ struct AtmPlan {
   DevBuf s_int, s_edge;  // chunk sums of the low-frequency block
   DevBuf gy_t, hx_t;     // 1-D phases in turns, folded into the GEMM output (TMA form)
   DevBuf step_partials, step_center;  // per-step measures (ATM_FLAG_STEP_MEASURES)
+  DevBuf status;                      // device status word (atm::STATUS_*), read by atm_plan_check
   bool step_meas = false;
   int step_slot0 = 0;
   atm::TcPlan* tcp = nullptr;  // TMA descriptors of the screen GEMM (null: cp.async form)
@@ -427,7 +429,14 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
     const int kraw = pl->kc0 + (pl->P_L > 0 ? pl->D - 1 : 0);
     pl->Kp = std::max(64, (kraw + 63) / 64 * 64);
   }
-  pl->rows = atm::row_pass_rows(pl->N);
+  // tiled layout: opt-in by flag; the tiled passes write one measure partial per row
+  pl->tiled = atm::tiled_supported(pl->N) && (d->flags & ATM_FLAG_TILED) && !(d->flags & ATM_FLAG_ROWMAJOR);
+  if (pl->tiled) {
+    pl->row_variant = 5;
+    pl->col_variant = 5;
+    pl->col_tile = 4;
+  }
+  pl->rows = pl->tiled ? 1 : atm::row_pass_rows(pl->N);
   pl->n_parts = pl->N / pl->rows;
   pl->n_meas = 6 + pl->n_pupils;
   pl->n_out = ATM_OUT_PUPIL0 + pl->n_pupils + pl->n_tracked;
@@ -450,9 +459,14 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
       (rc = dev_alloc(pl->tracked_r, (size_t)pl->n_tracked * sizeof(double), v)) ||
       (rc = dev_alloc(pl->intensity, pl->n_tracked > 0 ? B * plane * sizeof(float) : 0, v)) ||
       (rc = dev_alloc(pl->step_partials, pl->step_meas ? (size_t)pl->n * B * pl->n_parts * 6 * sizeof(double) : 0, v)) ||
-      (rc = dev_alloc(pl->step_center, pl->step_meas ? (size_t)pl->n * B * sizeof(float) : 0, v))) {
+      (rc = dev_alloc(pl->step_center, pl->step_meas ? (size_t)pl->n * B * sizeof(float) : 0, v)) ||
+      (rc = dev_alloc(pl->status, sizeof(int), v))) {
     delete pl;
     return rc;
+  }
+  if (cudaMemset(pl->status.p, 0, sizeof(int)) != cudaSuccess) {
+    delete pl;
+    return fail(ATM_ERR_CUDA, "cudaMemset of the status word failed");
   }
   if (pl->use_tc) {
     const size_t th = B * N * (size_t)pl->Kp * sizeof(__half);
@@ -565,6 +579,7 @@ int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
   info->col_variant = pl->col_variant;
   info->tuned = pl->tuned;
   info->gemm_form = pl->n == 0 ? 0 : (!pl->use_tc ? 0 : (pl->tcp ? (pl->tc_n256 ? 3 : 2) : 1));
+  info->tiled = pl->tiled ? 1 : 0;
   return ATM_OK;
 }
 
@@ -608,6 +623,7 @@ atm::ScreenArgs screen_args(AtmPlan* pl, const float* rho, const float* theta, c
   s.KH = pl->KH;
   s.KC = pl->KC;
   s.hterms = (atm::HighTerm*)pl->ht.p;
+  s.status = (int*)pl->status.p;
   s.s_int = (float2*)pl->s_int.p;
   s.s_edge = (double2*)pl->s_edge.p;
   s.Py = (float2*)pl->Py.p;
@@ -651,7 +667,8 @@ int run_screen(AtmPlan* pl, atm::ScreenArgs s, int B, bool fold, cudaStream_t st
     Prof p(pl, ATM_KIND_SCREEN_GEMM, st);
     constexpr float kInv2Pi = 0.15915494309189533577f;  // phi_G in turns
     if (pl->tcp)
-      ATM_CUDA(atm::launch_tc_gemm_tma(pl->tcp, B, (float*)pl->phi.p, kInv2Pi, s.gy_t, s.hx_t, st));
+      ATM_CUDA(atm::launch_tc_gemm_tma(pl->tcp, B, (float*)pl->phi.p, kInv2Pi, s.gy_t, s.hx_t, (int*)pl->status.p,
+                                       st));
     else
       ATM_CUDA(atm::launch_tc_gemm(B, pl->N, pl->N, pl->Kp, (const __half*)pl->ta_hi.p, (const __half*)pl->ta_lo.p,
                                    (const __half*)pl->tb_hi.p, (const __half*)pl->tb_lo.p, (float*)pl->phi.p, kInv2Pi,
@@ -695,6 +712,8 @@ atm::RowArgs row_args(AtmPlan* pl, float* mean_intensity, void* field_out) {
   ra.delta64 = pl->delta;
   ra.out = (float2*)field_out;
   ra.variant = pl->row_variant;
+  ra.tiled = pl->tiled ? (atm::TILE_IN | atm::TILE_OUT) : 0;
+  ra.status = (int*)pl->status.p;
   return ra;
 }
 
@@ -708,6 +727,7 @@ int finish_measures(AtmPlan* pl, int batch, double* measures, cudaStream_t st) {
   fa.n_out = pl->n_out;
   fa.n_pupils = pl->n_pupils;
   fa.delta = pl->delta;
+  fa.status = (const int*)pl->status.p;
   {
     Prof p(pl, ATM_KIND_FINALIZE, st);
     ATM_CUDA(atm::launch_finalize(batch, fa, st));
@@ -723,6 +743,7 @@ int finish_measures(AtmPlan* pl, int batch, double* measures, cudaStream_t st) {
     ta.slot0 = ATM_OUT_PUPIL0 + pl->n_pupils;
     ta.N = pl->N;
     ta.delta = pl->delta;
+    ta.status = (const int*)pl->status.p;
     ATM_CUDA(atm::launch_tracked(batch, ta, st));
   }
   return ATM_OK;
@@ -755,6 +776,7 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
   ca.field = (float2*)pl->field.p;
   ca.tw = (const float2*)pl->tw.p;
   ca.variant = pl->col_variant;
+  ca.status = (int*)pl->status.p;
 
   bool measured = false;
   for (int i = 0; i < n; ++i) {
@@ -809,6 +831,7 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
     fa.n_out = pl->n_out;
     fa.n_pupils = 0;
     fa.delta = pl->delta;
+    fa.status = (const int*)pl->status.p;
     Prof p(pl, ATM_KIND_FINALIZE, st);
     ATM_CUDA(atm::launch_finalize(batch, fa, st));
   }
@@ -823,6 +846,7 @@ int atm_measures(AtmPlan* pl, const void* field, int32_t batch, double* measures
   cudaStream_t st = (cudaStream_t)stream;
   atm::RowArgs ra = row_args(pl, nullptr, nullptr);
   ra.field = (float2*)field;
+  ra.tiled = 0;  // the caller's field is row-major
   ra.flags = atm::ROW_MEAS;
   ra.loss = 1.f;
   {
@@ -897,7 +921,9 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   ra.loss = 1.f;
   double best_row = -1.0;
   int row_variant = 0;
-  for (int v = 0; v < 5; ++v) {
+  // a tiled plan chooses among the tiled forms only (the others do not know its layout)
+  const int v_lo = pl->tiled ? 5 : 0, v_hi = pl->tiled ? 7 : 5;
+  for (int v = v_lo; v < v_hi; ++v) {
     ra.variant = v;
     const double ms = time_it([&] { return atm::launch_row_pass(N, batch, ra, st); });
     if (ms >= 0 && (best_row < 0 || ms < best_row)) {
@@ -915,7 +941,8 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   int col_tile = pl->col_tile, col_variant = 0;
   for (int C : {2, 4, 8, 16}) {
     if (C * (N / 16) > 512 || C > N) continue;
-    for (int v = 0; v < 5; ++v) {
+    if (pl->tiled && C != 4) continue;
+    for (int v = pl->tiled ? 5 : 0; v < (pl->tiled ? 6 : 5); ++v) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
       if (ms >= 0 && (best_col < 0 || ms < best_col)) {
@@ -945,6 +972,15 @@ int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* s
 
 int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, int32_t col_variant) {
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (pl->tiled) {
+    // a tiled plan's field is only understood by the tiled forms
+    if (row_variant != 5 && row_variant != 6)
+      return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5 or 6", row_variant);
+    if (col_variant != 5 || col_tile != 4)
+      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5 with col_tile 4");
+    pl->row_variant = row_variant;
+    return ATM_OK;
+  }
   if (row_variant < 0 || row_variant > 4) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4", row_variant);
   if (col_variant < 0 || col_variant > 4) return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4", col_variant);
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
@@ -975,21 +1011,30 @@ int atm_vacuum(AtmPlan* pl, void* field, int32_t batch, double dz, void* stream)
   }
   // the source is pageable: cudaMemcpyAsync returns once it has been staged
   ATM_CUDA(cudaMemcpyAsync(pl->vac_h.p, tab.data(), tab.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+  // a tiled plan converts the caller's row-major field to the tiled layout in
+  // the first row pass and back in the last (the tensor copies want the field
+  // on a 128-byte boundary); otherwise the row-major forms run
+  const bool tiled = pl->tiled && ((uintptr_t)field & 127) == 0;
   atm::RowArgs ra{};
   ra.field = (float2*)field;
   ra.tw = (const float2*)pl->tw.p;
   ra.loss = 1.f;
   ra.delta = (float)pl->delta;
   ra.delta64 = pl->delta;
+  ra.variant = tiled ? pl->row_variant : 0;
+  ra.tiled = tiled ? atm::TILE_OUT : 0;
+  ra.status = (int*)pl->status.p;
   ra.flags = atm::ROW_FWD | atm::ROW_STORE;
   ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
   atm::ColArgs ca{};
   ca.field = (float2*)field;
   ca.tw = (const float2*)pl->tw.p;
-  ca.variant = pl->col_variant;
+  ca.variant = tiled ? 5 : (pl->tiled ? 4 : pl->col_variant);
+  ca.status = (int*)pl->status.p;
   ca.hy = (const float2*)pl->vac_h.p;
   ca.hx = (const float2*)pl->vac_h.p + N;
   ATM_CUDA(atm::launch_col_pass(N, batch, pl->col_tile, ca, st));
+  ra.tiled = tiled ? atm::TILE_IN : 0;
   ra.flags = atm::ROW_INV | atm::ROW_STORE;
   ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
   return ATM_OK;
@@ -1029,7 +1074,7 @@ int atm_fft_screen(AtmPlan* pl, const float* normals, const float* amp, const vo
   atm::ColArgs ca{};
   ca.field = (float2*)pl->field.p;
   ca.tw = (const float2*)pl->tw.p;
-  ca.variant = pl->col_variant;
+  ca.variant = pl->tiled ? 4 : pl->col_variant;  // this screen's workspace stays row-major
   ca.inv_only = 1;
   {
     Prof p(pl, ATM_KIND_COL_PASS, st);
@@ -1102,6 +1147,35 @@ int atm_fma_probe(int32_t blocks, int32_t iters, double* ms, void* stream) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   *ms = t;
+  return ATM_OK;
+}
+
+int atm_plan_check(AtmPlan* pl, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  ATM_CUDA(cudaStreamSynchronize(st));
+  int word = 0, pass_flag = 0, tc_flag = 0;
+  ATM_CUDA(cudaMemcpy(&word, pl->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+  ATM_CUDA(atm::pass_error_flag(&pass_flag, true));
+  ATM_CUDA(atm::tc_error_flag(&tc_flag, true));
+  if (word == 0 && !pass_flag && !tc_flag) return ATM_OK;
+  ATM_CUDA(cudaMemset(pl->status.p, 0, sizeof(int)));
+  if (word & atm::STATUS_NONFINITE)
+    return fail(ATM_ERR_NONFINITE, "a spectrum value (rho, theta or value) was NaN or infinite; the measures of "
+                                   "the runs since the last check are NaN");
+  return fail(ATM_ERR_TIMEOUT, "a device wait ran out (%s%s%s); the kernels recorded it, drained their copies and "
+                               "returned, and the measures of the runs since the last check are NaN",
+              (word & atm::STATUS_PASS_WAIT) || pass_flag ? "FFT pass" : "",
+              ((word & atm::STATUS_PASS_WAIT) || pass_flag) && ((word & atm::STATUS_GEMM_WAIT) || tc_flag) ? ", " : "",
+              (word & atm::STATUS_GEMM_WAIT) || tc_flag ? "screen GEMM" : "");
+}
+
+int atm_set_wait_budget(uint64_t ns) {
+  if (ns < 1 || ns > 60000000000ull) return fail(ATM_ERR_INVALID, "wait budget %llu ns not in [1, 6e10]",
+                                                 (unsigned long long)ns);
+  ATM_CUDA(atm::set_pass_wait_budget((unsigned long long)ns));
+  ATM_CUDA(atm::set_tc_wait_budget((unsigned long long)ns));
   return ATM_OK;
 }
 

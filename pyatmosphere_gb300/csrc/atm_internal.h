@@ -21,6 +21,14 @@ enum : int {
 };
 
 constexpr int kMaxPupils = 8;
+
+// bits of a plan's device status word (atm_plan_check reads and clears it;
+// while it is non-zero, finalize writes NaN measures)
+enum : int {
+  STATUS_PASS_WAIT = 1,   // an FFT pass gave up waiting for a staged tile or a free stage
+  STATUS_GEMM_WAIT = 2,   // the tensor-core screen GEMM gave up waiting
+  STATUS_NONFINITE = 4,   // a spectrum value (rho, theta or value) was NaN or infinite
+};
 // measure slots accumulated by the last row pass (before the delta^2 scale)
 enum : int {
   MS_I = 0, MS_IX, MS_IMY, MS_IX2, MS_IMXY, MS_IY2, MS_PUPIL0,
@@ -57,8 +65,23 @@ struct RowArgs {
   int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per row block,
                             // 2: persistent pipeline with one row per CTA (row blocks of several rows otherwise),
                             // 3: as 2 with the rows moved by bulk copies (TMA) from one thread,
-                            // 4: as 3 with twiddles formed from powers of two (fewer shared loads)
+                            // 4: as 3 with twiddles formed from powers of two (fewer shared loads),
+                            // 5: four rows (one block row of the tiled layout) per CTA, each row's warps
+                            //    synchronising on their own named barrier; 6: as 5 with product twiddles
+  int tiled;                // variants 5 / 6: TILE_IN = field read in the tiled layout, TILE_OUT = field
+                            // (not `out`) written in the tiled layout; row-major otherwise
+  int* status;              // plan status word (nullable): STATUS_PASS_WAIT on a wait that runs out
 };
+
+// Tiled field layout: 4 x 4 blocks of complex64 (128 bytes), block rows of
+// 4 N elements contiguous.  A column pass then moves whole 128-byte lines,
+// and a block row is contiguous for the row pass.
+enum : int { TILE_IN = 1, TILE_OUT = 2 };
+__host__ __device__ inline size_t tiled_index(int N, int y, int x) {
+  return (size_t)(y >> 2) * (size_t)(4 * N) + (size_t)(x >> 2) * 16 + (size_t)((y & 3) * 4 + (x & 3));
+}
+// N with a tiled form of the passes (4 rows of N/16 threads per CTA, three FFT stages)
+inline bool tiled_supported(int N) { return N == 512 || N == 1024 || N == 2048; }
 
 struct ColArgs {
   float2* field;            // [B][N][N]
@@ -68,7 +91,11 @@ struct ColArgs {
   int inv_only;             // 1: inverse column FFT only (no forward FFT, no H)
   int variant;              // 0: persistent cp.async pipeline when aligned, 1: one CTA per column tile,
                             // 2: persistent pipeline with twiddles from powers of two (fewer shared loads),
-                            // 3: persistent, tiles loaded by TMA (one thread) so loads overlap the FFTs
+                            // 3: persistent, tiles loaded by TMA (one thread) so loads overlap the FFTs,
+                            // 4: as 3 with alternating exchange buffers,
+                            // 5: as 4 on the tiled layout (one block column of 4 columns per item,
+                            //    whole 128-byte lines in and out)
+  int* status;              // plan status word (nullable): STATUS_PASS_WAIT on a wait that runs out
 };
 
 // FFT screen (phase_screens.py:42-67) without shifts: screen[y][x] =
@@ -122,6 +149,7 @@ struct ScreenArgs {
   float* hx_t;              // [B][N] x-only phase in turns reduced to [-1/2, 1/2] (nullable)
   float2* s_int;            // [B][chunks][(D-1)^2] FP32 chunk sums of the Chebyshev interior
   double2* s_edge;          // [B][chunks][2D-1] FP64 chunk sums of its edge row / column
+  int* status;              // plan status word (nullable): STATUS_NONFINITE on a NaN / infinite spectrum value
 };
 
 // GEMM: phi[s][y][x] = sum_k At[s][k][y] B[s][k][x], k < KH from At, then the
@@ -140,6 +168,7 @@ struct FinalArgs {
   double* out;              // [B][n_out]
   int n_parts, n_meas, n_out, n_pupils;
   double delta;
+  const int* status;        // plan status word (nullable): non-zero -> NaN measures
 };
 
 struct TrackedArgs {
@@ -148,6 +177,7 @@ struct TrackedArgs {
   const double* radii;      // [n_tracked]
   int n_tracked, n_out, slot0, N;
   double delta;
+  const int* status;        // plan status word (nullable): non-zero -> NaN
 };
 
 // kernel launchers (atm_kernels.cu); return cudaGetLastError()
@@ -186,9 +216,19 @@ void tc_plan_destroy(TcPlan* p);
 // tensor map (128-byte storage of a CUtensorMap) of a complex64 field [B][N][N]
 // in boxes of C columns x box_rows rows; false without an encoder or alignment
 bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int box_rows);
+// tensor maps of a tiled field [B][N][N] (128-byte blocks, 128-byte swizzle):
+// by_rows: 2-D, consecutive blocks of a block row (boxes of box_blocks blocks);
+// otherwise 3-D, one block column (boxes of box_blocks blocks down the column)
+bool encode_tiled_field(void* map, const float2* field, int N, int B, bool by_rows, int box_blocks);
 // fold_y [S][M] / fold_x [S][Nn] (nullable, turns): added to every output
 cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
-                               const float* fold_x, cudaStream_t st);
+                               const float* fold_x, int* status, cudaStream_t st);
+// budget (ns) of the waits for work in the pass kernels / the tensor-core GEMM
+// on the current device; the waits that drain copies keep their 2 s bound
+cudaError_t set_pass_wait_budget(unsigned long long ns);
+cudaError_t set_tc_wait_budget(unsigned long long ns);
+// reads (and with reset, clears) the device-wide error word of the pass kernels
+cudaError_t pass_error_flag(int* host_flag, bool reset);
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                            const __half* b_lo, float* out, float scale, cudaStream_t st);
 cudaError_t launch_screen_table_tc(int B, const ScreenArgs& a, cudaStream_t st);

@@ -89,6 +89,10 @@ __device__ __forceinline__ float2 phasor_turns(float t) {
 // bounded mbarrier waits of the TMA-fed passes (error word set on timeout)
 // ---------------------------------------------------------------------------
 __device__ int g_pass_error;
+// budget of the waits for work (a staged tile, a free stage); atm_set_wait_budget
+// changes it.  The waits that drain copies before a CTA leaves keep kDrainNs.
+__device__ unsigned long long g_pass_wait_ns = 2000000000ull;
+constexpr unsigned long long kDrainNs = 2000000000ull;
 
 __device__ __forceinline__ uint64_t pass_timer() {
   uint64_t t;
@@ -96,7 +100,7 @@ __device__ __forceinline__ uint64_t pass_timer() {
   return t;
 }
 
-__device__ __forceinline__ bool pass_mbar_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool pass_mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns = kDrainNs) {
   const uint64_t t0 = pass_timer();
   while (true) {
     uint32_t ok;
@@ -106,7 +110,7 @@ __device__ __forceinline__ bool pass_mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (pass_timer() - t0 > 2000000000ull) return false;
+    if (pass_timer() - t0 > limit_ns) return false;
   }
 }
 
@@ -361,10 +365,13 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
     if (next < n_items) prefetch(next, s ^ 1);
     if constexpr (BULK) {
       // item k of this CTA uses stage k & 1 for the (k >> 1)-th time
-      const bool ok = !load_field || pass_mbar_wait(bar0 + 8 * s, (uint32_t)((k >> 1) & 1));
+      const bool ok = !load_field || pass_mbar_wait(bar0 + 8 * s, (uint32_t)((k >> 1) & 1), g_pass_wait_ns);
       if (tid == 0 && ok) pending[s] = false;
       if (__syncthreads_or(!ok)) {
-        if (tid == 0) atomicExch(&g_pass_error, 1);
+        if (tid == 0) {
+          atomicExch(&g_pass_error, 1);
+          if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+        }
         break;
       }
     } else {
@@ -465,6 +472,327 @@ struct LaunchCache {
   }
 };
 
+// ---------------------------------------------------------------------------
+// tiled layout (4 x 4 blocks of complex64, 128 bytes; see tiled_index):
+// row pass over one block row (4 rows) per item
+// ---------------------------------------------------------------------------
+// named barrier of one group of `count` threads (ids 1..15; 0 is __syncthreads)
+__device__ __forceinline__ void group_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+}
+// AND of `pred` over one group; every thread of the group gets the result
+__device__ __forceinline__ bool group_all(int id, int count, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void mbar_arrive_cta(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+// FFT of one row held by one group of N/16 threads whose exchanges
+// synchronise on the group's own named barrier, so the rows of a CTA never
+// wait for each other
+template <int N, int DIR, int s = 0, int TWPAD = 0, int TWREC = 0>
+__device__ __forceinline__ void fft_dev_grp(float2 (&v)[16], float2* sm, int t, const float2* __restrict__ tw,
+                                            int bar) {
+  if constexpr (s == FftPlan<N>::S - 1) {
+    stage_last<N, DIR, TWPAD, TWREC>(v, t, tw);
+  } else {
+    stage_to_smem<N, s, DIR, TWPAD, TWREC>(v, sm, t, tw);
+    group_sync(bar, N / 16);
+    stage_from_smem<N, s + 1>(v, sm, t);
+    group_sync(bar, N / 16);
+    fft_dev_grp<N, DIR, s + 1, TWPAD, TWREC>(v, sm, t, tw, bar);
+  }
+}
+
+// float2 slot of element (yi, x) of a block row staged by a 128-byte-swizzled
+// tensor copy of consecutive blocks: block j = x / 4 is box row j, and its
+// 16-byte chunk c = 2 yi + (x / 2) % 2 lands at chunk c ^ (j % 8).  A warp
+// reading 32 consecutive x of one row then meets no bank conflict.
+__device__ __forceinline__ int rowblock_slot(int yi, int x) {
+  const int j = x >> 2;
+  return j * 16 + (((((yi << 1) | ((x >> 1) & 1)) ^ (j & 7))) << 1) + (x & 1);
+}
+// float2 slot of element (y, c) of a staged block column (4 columns x N rows):
+// block yb = y / 4 is box row yb, chunk 2 (y % 4) + c / 2 lands at chunk ^ (yb % 8)
+__device__ __forceinline__ int colblock_slot(int y, int c) {
+  const int yb = y >> 2;
+  return yb * 16 + ((((((y & 3) << 1) | (c >> 1)) ^ (yb & 7))) << 1) + (c & 1);
+}
+
+// measures of one row held by one group of N/16 threads: the arithmetic of
+// measure_row with one row per CTA (FP32 per thread and warp, FP64 across the
+// group's warps), one partial vector per row: partials[r][y][n_meas]
+template <int N>
+__device__ __forceinline__ void measure_row_grp(const RowArgs& a, double* partials, float* center, int n_meas,
+                                                int n_pupils, bool full, const float2 (&v)[16], int t, int y, int r,
+                                                int bar, float (*red)[6 + kMaxPupils]) {
+  constexpr int T = N / 16;
+  constexpr int NWG = T >= 32 ? T / 32 : 1;
+  constexpr int MM = 6 + kMaxPupils;
+  const float d = (float)a.delta;
+  float s0 = 0.f, s1 = 0.f, s3 = 0.f;
+  float sp[kMaxPupils];
+  int2 iv[kMaxPupils];
+#pragma unroll
+  for (int p = 0; p < kMaxPupils; ++p) {
+    sp[p] = 0.f;
+    iv[p] = p < n_pupils ? a.pupil_rows[p * N + y] : make_int2(1, 0);
+  }
+  const size_t plane = (size_t)N * N;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    const int x = t + m * T;
+    const float I = v[m].x * v[m].x + v[m].y * v[m].y;
+    const float xc = (float)(x - N / 2) * d;
+    s0 += I;
+    s1 += I * xc;
+    s3 += I * xc * xc;
+#pragma unroll
+    for (int p = 0; p < kMaxPupils; ++p) {
+      if (p >= n_pupils) break;
+      if (x >= iv[p].x && x <= iv[p].y) sp[p] += I;
+    }
+    if (full) {
+      if (a.mean_I) atomicAdd(a.mean_I + (size_t)y * N + x, I);
+      if (a.intensity) a.intensity[(size_t)r * plane + (size_t)y * N + x] = I;
+    }
+    if (y == N / 2 && x == N / 2) center[r] = I;
+  }
+  const float yc = (float)(y - N / 2) * d;
+  float val[MM];
+  val[MS_I] = s0;
+  val[MS_IX] = s1;
+  val[MS_IMY] = -yc * s0;
+  val[MS_IX2] = s3;
+  val[MS_IMXY] = -yc * s1;
+  val[MS_IY2] = yc * yc * s0;
+#pragma unroll
+  for (int p = 0; p < kMaxPupils; ++p) val[MS_PUPIL0 + p] = sp[p];
+  const int lane = threadIdx.x & 31, w = t >> 5;
+#pragma unroll
+  for (int k = 0; k < MM; ++k) {
+    if (k >= n_meas) break;
+    float x = val[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if (lane == 0) red[w][k] = x;
+  }
+  group_sync(bar, T);
+  if (t < n_meas) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < NWG; ++i) s += (double)red[i][t];
+    partials[((size_t)r * N + y) * n_meas + t] = s;
+  }
+  group_sync(bar, T);  // red[] is reused by the group's next row
+}
+
+template <int N>
+struct RowTiled {
+  static constexpr int T = N / 16;
+  static constexpr int NT = 4 * T;
+  static constexpr size_t STAGE = (size_t)4 * N * sizeof(float2);          // one block row, a multiple of 1024
+  static constexpr size_t EXCH = (size_t)Padded<N>::value * sizeof(float2);  // one row's FFT exchange area
+  static constexpr size_t SMEM = 1024 + 2 * STAGE + 4 * EXCH + EXCH;         // + twiddles + alignment slack
+  static constexpr int BOX = (N / 4 < 256) ? N / 4 : 256;                     // blocks per tensor copy
+};
+
+// One item = one block row (realisation r, rows 4 yb .. 4 yb + 3).  Thread 0
+// moves the next item's block row into the other stage (tiled input: 128-byte
+// swizzled tensor copies of its N / 4 consecutive blocks; row-major input:
+// one bulk copy per row) once every warp has released that stage's previous
+// contents on an `empty` mbarrier.  Each row's N / 16 threads then run
+// alone: they read their row from the stage, release it, and transform it
+// in their own exchange area with their own named barrier.  Bounded waits:
+// on timeout the group records an error and leaves; thread 0 drains its
+// copies in flight first.
+template <int N, int TWREC>
+__global__ void __launch_bounds__(4 * (N / 16), 2048 / N)
+row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int n_items) {
+  using Cfg = RowTiled<N>;
+  constexpr int T = Cfg::T;
+  constexpr int NT = Cfg::NT;
+  constexpr int NRB = N / 4;  // block rows per realisation = blocks per block row
+  constexpr int NWG = T >= 32 ? T / 32 : 1;
+  constexpr int MM = 6 + kMaxPupils;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
+  __shared__ float red[4][NWG][MM];
+  const int tid = threadIdx.x, rl = tid / T, t = tid - rl * T;
+  const int bar = 1 + rl;
+  unsigned char* sbase = smem_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u);
+  auto stage = [&](int s) { return reinterpret_cast<float2*>(sbase + s * Cfg::STAGE); };
+  float2* exch = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + rl * Cfg::EXCH);
+  float2* tws = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + 4 * Cfg::EXCH);
+  load_twiddles<N>(tws, a.tw);
+  const int flags = a.flags;
+  const bool load_field = !(flags & ROW_GEN);
+  const bool load_phi = (flags & ROW_PHASOR) != 0;
+  const bool in_tiled = (a.tiled & TILE_IN) != 0;
+  float2* dst = (a.store_out && a.out) ? a.out : a.field;
+  const bool out_tiled = (a.tiled & TILE_OUT) && dst == a.field;
+  const unsigned long long wait_ns = g_pass_wait_ns;
+  const uint32_t fb0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
+  const uint32_t eb0 = (uint32_t)__cvta_generic_to_shared(&empty_bar[0]);
+  if (tid == 0) {
+    for (int q = 0; q < 2; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fb0 + 8 * q) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(eb0 + 8 * q), "r"(NT / 32) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  int fills[2] = {0, 0};             // thread 0: copies issued into each stage
+  bool pending[2] = {false, false};  // thread 0: issued and not yet waited for
+  bool producer_ok = true;
+  auto prefetch = [&](int item, int s) -> bool {
+    // the stage's previous contents have been read by every warp
+    if (fills[s] > 0 && !pass_mbar_wait(eb0 + 8 * s, (uint32_t)((fills[s] - 1) & 1), wait_ns)) return false;
+    const int r = item / NRB, yb = item - r * NRB;
+    const uint32_t fb = fb0 + 8 * s;
+    const uint32_t d0 = (uint32_t)__cvta_generic_to_shared(stage(s));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::STAGE)
+                 : "memory");
+    if (in_tiled) {
+#pragma unroll 1
+      for (int b = 0; b < NRB / Cfg::BOX; ++b)
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4}], [%5];\n" ::"r"(d0 + (uint32_t)(b * Cfg::BOX * 128)),
+            "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(0), "r"(yb * NRB + b * Cfg::BOX), "r"(r), "r"(fb)
+            : "memory");
+    } else {
+      const float2* src = a.field + (size_t)r * N * N + (size_t)yb * 4 * N;
+#pragma unroll 1
+      for (int q = 0; q < 4; ++q)
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                d0 + (uint32_t)(q * N * sizeof(float2))),
+            "l"(src + (size_t)q * N), "r"((uint32_t)(N * sizeof(float2))), "r"(fb)
+            : "memory");
+    }
+    ++fills[s];
+    pending[s] = true;
+    return true;
+  };
+
+  int item = blockIdx.x, s = 0, k = 0;
+  if (tid == 0 && load_field && item < n_items) producer_ok = prefetch(item, 0);
+  for (; item < n_items; item += gridDim.x, s ^= 1, ++k) {
+    const int next = item + gridDim.x;
+    if (tid == 0 && load_field && producer_ok && next < n_items) producer_ok = prefetch(next, s ^ 1);
+    bool ok = tid != 0 || producer_ok;
+    if (load_field) {
+      // item k of this CTA uses stage k & 1 for the (k >> 1)-th time
+      const bool landed = pass_mbar_wait(fb0 + 8 * s, (uint32_t)((k >> 1) & 1), wait_ns);
+      if (tid == 0 && landed) pending[s] = false;
+      ok = ok && landed;
+    }
+    if (!group_all(bar, T, ok)) {
+      if (t == 0) {
+        atomicExch(&g_pass_error, 1);
+        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      }
+      break;
+    }
+    const int r = item / NRB, yb = item - r * NRB;
+    const int y = yb * 4 + rl;
+    const size_t rowoff = (size_t)r * N * N + (size_t)y * N;
+    float2 v[16];
+    if (!load_field) {
+      const float2 gy = a.ay[y];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(gy, a.ax[t + m * T]);
+    } else if (in_tiled) {
+      const float2* sm = stage(s);
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = sm[rowblock_slot(rl, t + m * T)];
+    } else {
+      const float2* sm = stage(s) + rl * N;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = sm[t + m * T];
+    }
+    float ph[16];
+    if (load_phi) {
+      const float* src = a.phi + rowoff;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) ph[m] = src[t + m * T];
+    }
+    if (load_field) {
+      // this warp's reads of the stage are done: it may be refilled (by the async proxy)
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      __syncwarp();
+      if ((tid & 31) == 0) mbar_arrive_cta(eb0 + 8 * s);
+    }
+    if (flags & ROW_INV) fft_dev_grp<N, 1, 0, 1, TWREC>(v, exch, t, tws, bar);
+    if (load_phi && (flags & ROW_FOLDED) && a.loss == 1.0f) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], phasor_turns(ph[m]));
+    } else if (load_phi && (flags & ROW_FOLDED)) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cscale(phasor_turns(ph[m]), a.loss));
+    } else if (load_phi) {
+      const float2 py = cscale(a.Py[(size_t)r * N + y], a.loss);
+      const float2* px = a.Px + (size_t)r * N;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int x = t + m * T;
+        v[m] = cmul(v[m], cmul(cmul(py, px[x]), phasor_turns(ph[m])));
+      }
+    } else if (a.loss != 1.0f) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cscale(v[m], a.loss);
+    }
+    if (flags & ROW_STEP)
+      measure_row_grp<N>(a, a.step_partials, a.step_center, 6, 0, false, v, t, y, r, bar, red[rl]);
+    if (flags & ROW_FWD) fft_dev_grp<N, -1, 0, 1, TWREC>(v, exch, t, tws, bar);
+    if (flags & ROW_STORE) {
+      if (out_tiled) {
+        float2* d = dst + (size_t)r * N * N + (size_t)yb * 4 * N + rl * 4;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+          const int x = t + m * T;
+          d[(x >> 2) * 16 + (x & 3)] = v[m];
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) dst[rowoff + t + m * T] = v[m];
+      }
+    }
+    if (flags & ROW_MEAS)
+      measure_row_grp<N>(a, a.partials, a.center, a.n_meas, a.n_pupils, true, v, t, y, r, bar, red[rl]);
+  }
+  // no copy may land after the CTA leaves: wait (bounded) for any still pending
+  if (tid == 0)
+    for (int q = 0; q < 2; ++q)
+      if (pending[q]) pass_mbar_wait(fb0 + 8 * q, (uint32_t)((fills[q] - 1) & 1));
+}
+
+template <int N, int TWREC>
+static cudaError_t row_tiled_launch(int B, const RowArgs& a, cudaStream_t st) {
+  alignas(128) CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const bool in_tiled = (a.tiled & TILE_IN) && !(a.flags & ROW_GEN);
+  if (in_tiled && !encode_tiled_field(&map, a.field, N, B, true, RowTiled<N>::BOX)) return cudaErrorNotSupported;
+  static LaunchCache cache;
+  const int threads = RowTiled<N>::NT;
+  const size_t smem = RowTiled<N>::SMEM;
+  int grid_max = 0;
+  cudaError_t e = cache.get(row_pass_tiled_kernel<N, TWREC>, threads, smem, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_items = B * (N / 4);
+  const int grid = std::max(1, std::min(n_items, grid_max));
+  row_pass_tiled_kernel<N, TWREC><<<grid, threads, smem, st>>>(map, a, n_items);
+  return cudaGetLastError();
+}
+
 template <int N, int ROWS, int BULK = 0, int TWREC = 0>
 static cudaError_t row_pipe_launch(int B, const RowArgs& a, cudaStream_t st) {
   static LaunchCache cache;
@@ -501,6 +829,14 @@ template <int N>
 static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
+  if constexpr (N == 512 || N == 1024 || N == 2048) {
+    if (a.variant == 5 || a.variant == 6) {
+      // the tiled forms: the only forms that read or write the tiled layout
+      if (!field_ok || !phi_ok || (a.store_out && a.out && !aligned16(a.out))) return cudaErrorInvalidValue;
+      return a.variant == 5 ? row_tiled_launch<N, 0>(B, a, st) : row_tiled_launch<N, 1>(B, a, st);
+    }
+  }
+  if (a.tiled) return cudaErrorInvalidValue;  // no other form knows the tiled layout
   // measure partials are laid out per block of RowRows<N> rows: one-row forms fall back there
   const bool meas = (a.flags & (ROW_MEAS | ROW_STEP)) != 0;
   const int variant = meas && a.variant == 2 ? 0 : a.variant;
@@ -717,10 +1053,13 @@ col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_
     const int next = item + gridDim.x;
     if (tid == 0 && next < n_items) prefetch(next, s ^ 1);
     // item k of this CTA uses stage k & 1 for the (k >> 1)-th time
-    const bool ok = pass_mbar_wait(bar0 + 8 * s, (uint32_t)((k >> 1) & 1));
+    const bool ok = pass_mbar_wait(bar0 + 8 * s, (uint32_t)((k >> 1) & 1), g_pass_wait_ns);
     if (tid == 0 && ok) pending[s] = false;
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicExch(&g_pass_error, 1);
+      if (tid == 0) {
+        atomicExch(&g_pass_error, 1);
+        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      }
       break;
     }
     const int r = item / NCT, x = (item - r * NCT) * C + c;
@@ -774,6 +1113,129 @@ static cudaError_t col_tma_launch(int B, const ColArgs& a, cudaStream_t st) {
   const int n_items = B * (N / C);
   const int grid = std::max(1, std::min(n_items, grid_max));
   col_pass_tma_kernel<N, C, DBX><<<grid, threads, smem, st>>>(map, a, n_items);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// column pass on the tiled layout: one item = one block column (4 columns x
+// N rows) of one realisation, N / 4 blocks of 128 bytes down the column,
+// moved by 128-byte-swizzled tensor copies; each warp stores two whole
+// blocks (8 rows x 4 columns) per store instruction.  FFT exchanges alternate
+// between the staged tile and a third buffer (one barrier per exchange).
+// Every wait is bounded (an error word, then a drain of the copies in flight).
+// ---------------------------------------------------------------------------
+template <int N>
+struct ColTiled {
+  static constexpr int C = 4;
+  static constexpr int S = ColStride<N, 4>::value;
+  static constexpr size_t TILE = (size_t)N * 4 * sizeof(float2);
+  static constexpr size_t EXCH = (size_t)4 * S * sizeof(float2);
+  static constexpr size_t STAGE = ((TILE > EXCH ? TILE : EXCH) + 1023) / 1024 * 1024;
+  static constexpr size_t TW = (size_t)Padded<N>::value * sizeof(float2);
+  static constexpr size_t SMEM = 1024 + 2 * STAGE + EXCH + TW;
+  static constexpr int BOX = (N / 4 < 256) ? N / 4 : 256;  // blocks per tensor copy
+};
+
+template <int N>
+__global__ void __launch_bounds__(4 * (N / 16))
+col_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
+  using Cfg = ColTiled<N>;
+  constexpr int T = N / 16;
+  constexpr int S = Cfg::S;
+  constexpr int NCT = N / 4;  // block columns per realisation
+  static_assert(FftPlan<N>::S == 3, "alternating exchanges need three stages");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[2];
+  const int tid = threadIdx.x;
+  const int c = tid & 3, t = tid >> 2;
+  unsigned char* sbase = smem_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u);
+  auto buf = [&](int s) { return reinterpret_cast<float2*>(sbase + s * Cfg::STAGE); };
+  float2* xbuf = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE);
+  float2* tws = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + Cfg::EXCH);
+  load_twiddles<N>(tws, a.tw);
+  const unsigned long long wait_ns = g_pass_wait_ns;
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  bool pending[2] = {false, false};  // thread 0: copies issued and not yet waited for
+  auto prefetch = [&](int item, int s) {
+    const int r = item / NCT, xb = item - r * NCT;
+    const uint32_t bar = bar0 + 8 * s;
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(buf(s));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"((uint32_t)Cfg::TILE)
+                 : "memory");
+#pragma unroll 1
+    for (int b = 0; b < NCT / Cfg::BOX; ++b)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+          "[%5];\n" ::"r"(dst + (uint32_t)(b * Cfg::BOX * 128)),
+          "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(0), "r"(xb), "r"(r * NCT + b * Cfg::BOX), "r"(bar)
+          : "memory");
+    pending[s] = true;
+  };
+  int item = blockIdx.x, s = 0, k = 0;
+  if (tid == 0 && item < n_items) prefetch(item, 0);
+  for (; item < n_items; item += gridDim.x, s ^= 1, ++k) {
+    const int next = item + gridDim.x;
+    if (tid == 0 && next < n_items) prefetch(next, s ^ 1);
+    // item k of this CTA uses stage k & 1 for the (k >> 1)-th time
+    const bool ok = pass_mbar_wait(bar0 + 8 * s, (uint32_t)((k >> 1) & 1), wait_ns);
+    if (tid == 0 && ok) pending[s] = false;
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicExch(&g_pass_error, 1);
+        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      }
+      break;
+    }
+    const int r = item / NCT, xb = item - r * NCT;
+    float2* tile = buf(s);
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = tile[colblock_slot(t + m * T, c)];
+    __syncthreads();  // the exchanges below overwrite the staged tile
+    float2* sm = tile + c * S;
+    float2* sm2 = xbuf + c * S;
+    if (!a.inv_only) {
+      fft_dev_db<N, -1, 0, 1>(v, sm, sm2, t, tws);
+      const float2 hx = a.hx[xb * 4 + c];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(__ldg(a.hy + t + m * T), hx));
+    }
+    fft_dev_db<N, 1, 0, 1>(v, sm, sm2, t, tws);
+    float2* f = a.field + (size_t)r * N * N + (size_t)xb * 16 + c;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int y = t + m * T;
+      f[(size_t)(y >> 2) * (4 * N) + (y & 3) * 4] = v[m];
+    }
+    // stage s is refilled by TMA (the async proxy) after the next barrier
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+  }
+  // no copy may land after the CTA leaves: wait (bounded) for any still pending
+  if (tid == 0)
+    for (int q = 0; q < 2; ++q)
+      if (pending[q]) pass_mbar_wait(bar0 + 8 * q, (uint32_t)(((k + (q != s)) >> 1) & 1));
+}
+
+template <int N>
+static cudaError_t col_tiled_launch(int B, const ColArgs& a, cudaStream_t st) {
+  alignas(128) CUtensorMap map;
+  if (!encode_tiled_field(&map, a.field, N, B, false, ColTiled<N>::BOX)) return cudaErrorNotSupported;
+  static LaunchCache cache;
+  const int threads = 4 * (N / 16);
+  const size_t smem = ColTiled<N>::SMEM;
+  int grid_max = 0;
+  cudaError_t e = cache.get(col_pass_tiled_kernel<N>, threads, smem, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_items = B * (N / 4);
+  const int grid = std::max(1, std::min(n_items, grid_max));
+  col_pass_tiled_kernel<N><<<grid, threads, smem, st>>>(map, a, n_items);
   return cudaGetLastError();
 }
 
@@ -853,6 +1315,16 @@ static cudaError_t col_dispatch(int C, int B, const ColArgs& a, cudaStream_t st)
 }
 
 cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t st) {
+  if (a.variant == 5) {
+    // the tiled layout: tiles are block columns (4 columns); C does not apply
+    if (!aligned16(a.field)) return cudaErrorInvalidValue;
+    switch (N) {
+      case 512: return col_tiled_launch<512>(B, a, st);
+      case 1024: return col_tiled_launch<1024>(B, a, st);
+      case 2048: return col_tiled_launch<2048>(B, a, st);
+    }
+    return cudaErrorInvalidValue;
+  }
   if (C <= 0) C = col_tile_default(N);
   switch (N) {
     case 128: return col_dispatch<128>(C, B, a, st);
@@ -921,8 +1393,12 @@ __global__ void __launch_bounds__(kPrepThreads) screen_terms_kernel(ScreenArgs a
     if (q >= nh) return;
     HighTerm h;
     h.pad_ = make_float2(0.f, 0.f);
-    if (q < a.P_H) {
-      const int p = P_L + q;
+    const int pq = P_L + q;
+    const bool finite = q >= a.P_H || (isfinite(rho[pq]) && isfinite(theta[pq]) && isfinite(value[pq].x) &&
+                                       isfinite(value[pq].y));
+    if (!finite && a.status) atomicOr(a.status, STATUS_NONFINITE);
+    if (q < a.P_H && finite) {
+      const int p = pq;
       double s, c;
       sincos((double)theta[p], &s, &c);
       const double rh = (double)rho[p];
@@ -951,20 +1427,26 @@ __global__ void __launch_bounds__(kPrepThreads) screen_terms_kernel(ScreenArgs a
   float2* vf = reinterpret_cast<float2*>(Jxf + kPrepChunk * D);
   if (tid < np) {
     const int p = p0 + tid;
-    double s, cs;
-    sincos((double)theta[p], &s, &cs);
-    const double rh = (double)rho[p];
-    const double fx = rh * cs, fy = rh * s;
     const float2 v = value[p];
-    const double xh = 0.5 * (N - 1) * delta;
-    const double xc = -0.5 * delta + a.sx, yc = -0.5 * delta + a.sy;
-    double ps, pc;
-    sincospi(2.0 * (fx * xc + fy * yc), &ps, &pc);
-    LowTerm lt;
-    lt.vr = (double)v.x * pc - (double)v.y * ps;
-    lt.vi = (double)v.x * ps + (double)v.y * pc;
-    lt.ax = two_pi * fx * xh;
-    lt.ay = two_pi * fy * xh;
+    LowTerm lt{0.0, 0.0, 0.0, 0.0};
+    if (isfinite(rho[p]) && isfinite(theta[p]) && isfinite(v.x) && isfinite(v.y)) {
+      double s, cs;
+      sincos((double)theta[p], &s, &cs);
+      const double rh = (double)rho[p];
+      const double fx = rh * cs, fy = rh * s;
+      const double xh = 0.5 * (N - 1) * delta;
+      const double xc = -0.5 * delta + a.sx, yc = -0.5 * delta + a.sy;
+      double ps, pc;
+      sincospi(2.0 * (fx * xc + fy * yc), &ps, &pc);
+      lt.vr = (double)v.x * pc - (double)v.y * ps;
+      lt.vi = (double)v.x * ps + (double)v.y * pc;
+      // an annulus radius far outside the low block would only lengthen the
+      // Bessel recurrence (its start order grows with the argument): keep it bounded
+      lt.ax = fmin(fmax(two_pi * fx * xh, -4096.0), 4096.0);
+      lt.ay = fmin(fmax(two_pi * fy * xh, -4096.0), 4096.0);
+    } else if (a.status) {
+      atomicOr(a.status, STATUS_NONFINITE);
+    }
     low[tid] = lt;
   }
   __syncthreads();
@@ -1437,7 +1919,12 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalArgs a) {
     tot[tid] = s;
   }
   __syncthreads();
-  if (tid == 0) {
+  if (tid == 0 && a.status && *a.status != 0) {
+    // a wait ran out or a spectrum value was not finite in this plan since its
+    // last atm_plan_check: the measures of the run are not trustworthy
+    double* o = a.out + (size_t)r * a.n_out;
+    for (int k = 0; k < MO_PUPIL0 + a.n_pupils; ++k) o[k] = __longlong_as_double(0x7ff8000000000000ll);
+  } else if (tid == 0) {
     const double d2 = a.delta * a.delta;
     double* o = a.out + (size_t)r * a.n_out;
     const double mx = tot[MS_IX] * d2, my = tot[MS_IMY] * d2;
@@ -1497,7 +1984,8 @@ __global__ void __launch_bounds__(256) tracked_kernel(TrackedArgs a) {
   if (tid == 0) {
     double s = 0.0;
     for (int i = 0; i < 8; ++i) s += red[i];
-    o[a.slot0 + p] = s * d * d;
+    const bool failed = a.status && *a.status != 0;  // the plan's status canary, as in finalize
+    o[a.slot0 + p] = failed ? __longlong_as_double(0x7ff8000000000000ll) : s * d * d;
   }
 }
 
@@ -1598,6 +2086,17 @@ cudaError_t launch_structure_function(const float* phi, int B, int N, double* ou
   const size_t smem = (size_t)N * sizeof(float);
   structure_function_kernel<<<grid, kSfThreads, smem, st>>>(phi, N, out);
   return cudaGetLastError();
+}
+
+cudaError_t set_pass_wait_budget(unsigned long long ns) {
+  return cudaMemcpyToSymbol(g_pass_wait_ns, &ns, sizeof(ns));
+}
+
+cudaError_t pass_error_flag(int* host_flag, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(host_flag, g_pass_error, sizeof(int));
+  if (e != cudaSuccess || !reset) return e;
+  const int z = 0;
+  return cudaMemcpyToSymbol(g_pass_error, &z, sizeof(int));
 }
 
 __device__ float g_fma_sink[256];

@@ -57,6 +57,9 @@ constexpr int THREADS = 128;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s
 
 __device__ int g_tc_error;
+// budget of the persistent form's waits for work (operands, an accumulator,
+// a free stage); atm_set_wait_budget changes it.  Drains keep kTimeoutNs.
+__device__ unsigned long long g_tc_wait_ns = kTimeoutNs;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -346,6 +349,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 // a timeout sets the flag itself
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
   const uint64_t t0 = globaltimer();
+  const unsigned long long limit = g_tc_wait_ns;
   for (uint32_t spin = 1;; ++spin) {
     uint32_t ok;
     asm volatile(
@@ -356,7 +360,7 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity
     if (ok) return true;
     if ((spin & 15) == 0) {
       if (*abort_flag) return false;
-      if (globaltimer() - t0 > kTimeoutNs) {
+      if (globaltimer() - t0 > limit) {
         *abort_flag = 1;
         return false;
       }
@@ -376,7 +380,7 @@ template <int TNT, int STG, int NACC, int EPI = 0>
 __global__ void __launch_bounds__(P_THREADS, 1)
     tc_gemm_tma_kernel(const __grid_constant__ TmaOperands ops, const __grid_constant__ CUtensorMap outmap,
                        float* __restrict__ out, int S, int M, int Nn, int Kp, float scale,
-                       const float* __restrict__ fold_y, const float* __restrict__ fold_x) {
+                       const float* __restrict__ fold_y, const float* __restrict__ fold_x, int* status) {
   using Cfg = TmaCfg<TNT, STG, NACC, EPI>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STG], empty_bar[STG], accf_bar[NACC], acce_bar[NACC], drain_bar;
@@ -595,7 +599,10 @@ __global__ void __launch_bounds__(P_THREADS, 1)
 
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_error, 1);
+  if (threadIdx.x == 0 && *abort_flag) {
+    atomicExch(&g_tc_error, 1);
+    if (status) atomicOr(status, STATUS_GEMM_WAIT);
+  }
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem) : "memory");
@@ -668,6 +675,31 @@ bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int
             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// tiled field [B][N][N] (4 x 4 blocks of complex64 = 32 FP32 = 128 bytes):
+//   by_rows: 2-D {32, B N^2 / 16}, boxes of box_blocks consecutive blocks (a block row is contiguous);
+//   else:    3-D {32, N / 4, B N / 4}, boxes of box_blocks blocks of one block column.
+// 128-byte swizzle: the 16-byte chunk c of box row j lands at chunk c ^ (j & 7), so the passes read
+// a row or a column of the staged blocks without shared-memory bank conflicts.
+bool encode_tiled_field(void* map, const float2* field, int N, int B, bool by_rows, int box_blocks) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !map || ((uintptr_t)field & 127) != 0 || N < 16 || box_blocks < 1 || box_blocks > 256) return false;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if (by_rows) {
+    const cuuint64_t dims[2] = {32, (cuuint64_t)B * N * N / 16};
+    const cuuint64_t strides[1] = {128};
+    const cuuint32_t box[2] = {32, (cuuint32_t)box_blocks};
+    return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(field), dims,
+              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  }
+  const cuuint64_t dims[3] = {32, (cuuint64_t)N / 4, (cuuint64_t)B * N / 4};
+  const cuuint64_t strides[2] = {128, (cuuint64_t)N * 32};
+  const cuuint32_t box[3] = {32, 1, (cuuint32_t)box_blocks};
+  return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(field), dims,
+            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 struct TcPlan {
   TmaOperands ops;
   int S, M, Nn, Kp;
@@ -711,7 +743,7 @@ static bool encode_output(EncodeTiledFn fn, CUtensorMap* map, float* out, int S,
 
 template <int TNT, int STG, int NACC, int EPI>
 static cudaError_t launch_tma_form(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
-                                   const float* fold_x, cudaStream_t st) {
+                                   const float* fold_x, int* status, cudaStream_t st) {
   using Cfg = TmaCfg<TNT, STG, NACC, EPI>;
   alignas(64) CUtensorMap outmap{};
   if (EPI) {
@@ -735,17 +767,19 @@ static cudaError_t launch_tma_form(const TcPlan* p, int S, float* out, float sca
   const int n_tiles = S * (p->M / TM) * (p->Nn / TNT);
   const int grid = std::min(n_tiles, sms[dev]);
   tc_gemm_tma_kernel<TNT, STG, NACC, EPI><<<grid, P_THREADS, Cfg::SMEM, st>>>(p->ops, outmap, out, S, p->M, p->Nn,
-                                                                               p->Kp, scale, fold_y, fold_x);
+                                                                               p->Kp, scale, fold_y, fold_x, status);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
-                               const float* fold_x, cudaStream_t st) {
+                               const float* fold_x, int* status, cudaStream_t st) {
   if (!p || S < 1 || S > p->S || !out || (!fold_y) != (!fold_x)) return cudaErrorInvalidValue;
   if (((uintptr_t)fold_x & 15) != 0) return cudaErrorMisalignedAddress;
-  if (p->tn == 128) return launch_tma_form<128, 3, 2, 0>(p, S, out, scale, fold_y, fold_x, st);
-  return launch_tma_form<256, 2, 1, 1>(p, S, out, scale, fold_y, fold_x, st);
+  if (p->tn == 128) return launch_tma_form<128, 3, 2, 0>(p, S, out, scale, fold_y, fold_x, status, st);
+  return launch_tma_form<256, 2, 1, 1>(p, S, out, scale, fold_y, fold_x, status, st);
 }
+
+cudaError_t set_tc_wait_budget(unsigned long long ns) { return cudaMemcpyToSymbol(g_tc_wait_ns, &ns, sizeof(ns)); }
 
 cudaError_t launch_tc_gemm(int S, int M, int Nn, int Kp, const __half* a_hi, const __half* a_lo, const __half* b_hi,
                            const __half* b_lo, float* out, float scale, cudaStream_t st) {
@@ -820,7 +854,7 @@ extern "C" int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32
     if (!tp) e = cudaErrorNotSupported;
   }
   if (e == cudaSuccess)
-    e = variant != 1 ? atm::launch_tc_gemm_tma(tp, S, out, scale, nullptr, nullptr, st)
+    e = variant != 1 ? atm::launch_tc_gemm_tma(tp, S, out, scale, nullptr, nullptr, nullptr, st)
                      : atm::launch_tc_gemm(S, M, N, Kp, ah, al, bh, bl, out, scale, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   int flag = 0;

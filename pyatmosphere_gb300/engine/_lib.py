@@ -23,6 +23,10 @@ FLAG_TC_CPASYNC = 4
 FLAG_STEP_MEASURES = 8
 FLAG_TC_N256 = 16
 FLAG_TC_N128 = 32
+FLAG_TILED = 64
+FLAG_ROWMAJOR = 128
+ERR_TIMEOUT = -5
+ERR_NONFINITE = -6
 STEP_SLOTS = 8
 SOURCE_GAUSSIAN = 0
 SOURCE_PLANE = 1
@@ -87,6 +91,7 @@ class AtmPlanInfo(ctypes.Structure):
         ("col_variant", ctypes.c_int32),
         ("tuned", ctypes.c_int32),
         ("gemm_form", ctypes.c_int32),
+        ("tiled", ctypes.c_int32),
     ]
 
 
@@ -144,6 +149,8 @@ SIGNATURES = {
                                         ctypes.c_int32, ctypes.c_void_p]),
     "atm_vacuum_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+    "atm_plan_check": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_set_wait_budget": (ctypes.c_int, [ctypes.c_uint64]),
 }
 
 KIND_NAMES = ["screen_prep", "screen_table", "screen_gemm", "row_pass", "col_pass", "finalize", "tracked",
@@ -154,7 +161,11 @@ _lib = None
 
 
 class EngineError(RuntimeError):
-    pass
+    """A libatm call failed; ``code`` is its ATM_ERR_* status."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
 
 
 def load(path: str = LIB_PATH):
@@ -181,7 +192,7 @@ def load(path: str = LIB_PATH):
 def check(rc: int):
     if rc != 0:
         msg = load().atm_last_error().decode(errors="replace")
-        raise EngineError(f"libatm error {rc}: {msg}")
+        raise EngineError(f"libatm error {rc}: {msg}", rc)
 
 
 def load_selftest(path: str = SELFTEST_PATH):

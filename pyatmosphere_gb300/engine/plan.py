@@ -145,6 +145,14 @@ class EnginePlan:
             check(self.lib.atm_draw_spectra(self._handle, int(seed), int(first), _tptr(sqrt_psd), batch, _tptr(rho),
                                             _tptr(theta), _tptr(value), _stream(self.device)))
 
+    def check(self):
+        """Waits for the plan's work on the current stream and raises
+        EngineError (code ERR_TIMEOUT or ERR_NONFINITE) if its kernels recorded
+        a wait that ran out or non-finite spectra since the last check
+        (atm_plan_check); the measures of those runs are NaN."""
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_plan_check(self._handle, _stream(self.device)))
+
     # ------------------------------------------------------------------
     def close(self):
         h = getattr(self, "_handle", None)
@@ -239,6 +247,15 @@ class EnginePlan:
         with torch.cuda.device(self.device):
             check(self.lib.atm_profile_end(self._handle, ms, cnt, n))
         return {k: {"ms": ms[i], "launches": cnt[i]} for i, k in enumerate(_lib.KIND_NAMES)}
+
+
+def set_wait_budget(ns: int, device=None):
+    """Budget (ns) of the engine's device waits for work on `device`
+    (atm_set_wait_budget; default 2e9)."""
+    lib = load()
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else torch.device(device).index or 0)
+    with torch.cuda.device(dev):
+        check(lib.atm_set_wait_budget(int(ns)))
 
 
 def structure_function(phi: torch.Tensor) -> torch.Tensor:
