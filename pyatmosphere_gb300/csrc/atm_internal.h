@@ -217,7 +217,7 @@ void tc_plan_destroy(TcPlan* p);
 // in boxes of C columns x box_rows rows; false without an encoder or alignment
 bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int box_rows);
 // tensor maps of a tiled field [B][N][N] (128-byte blocks, 128-byte swizzle):
-// by_rows: 2-D, consecutive blocks of a block row (boxes of box_blocks blocks);
+// by_rows: 3-D {32, N^2/16, B}, consecutive blocks of a block row (boxes of box_blocks blocks);
 // otherwise 3-D, one block column (boxes of box_blocks blocks down the column)
 bool encode_tiled_field(void* map, const float2* field, int N, int B, bool by_rows, int box_blocks);
 // fold_y [S][M] / fold_x [S][Nn] (nullable, turns): added to every output

@@ -676,7 +676,7 @@ bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int
 }
 
 // tiled field [B][N][N] (4 x 4 blocks of complex64 = 32 FP32 = 128 bytes):
-//   by_rows: 2-D {32, B N^2 / 16}, boxes of box_blocks consecutive blocks (a block row is contiguous);
+//   by_rows: 3-D {32, N^2 / 16, B}, boxes of box_blocks consecutive blocks (a block row is contiguous);
 //   else:    3-D {32, N / 4, B N / 4}, boxes of box_blocks blocks of one block column.
 // 128-byte swizzle: the 16-byte chunk c of box row j lands at chunk c ^ (j & 7), so the passes read
 // a row or a column of the staged blocks without shared-memory bank conflicts.
@@ -685,10 +685,11 @@ bool encode_tiled_field(void* map, const float2* field, int N, int B, bool by_ro
   if (!fn || !map || ((uintptr_t)field & 127) != 0 || N < 16 || box_blocks < 1 || box_blocks > 256) return false;
   const cuuint32_t estr[3] = {1, 1, 1};
   if (by_rows) {
-    const cuuint64_t dims[2] = {32, (cuuint64_t)B * N * N / 16};
-    const cuuint64_t strides[1] = {128};
-    const cuuint32_t box[2] = {32, (cuuint32_t)box_blocks};
-    return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(field), dims,
+    // {block float, block index within a realisation, realisation}: coordinates stay below 2^31 for any batch
+    const cuuint64_t dims[3] = {32, (cuuint64_t)N * N / 16, (cuuint64_t)B};
+    const cuuint64_t strides[2] = {128, (cuuint64_t)N * N * sizeof(float2)};
+    const cuuint32_t box[3] = {32, (cuuint32_t)box_blocks, 1};
+    return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(field), dims,
               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   }
