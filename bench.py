@@ -169,6 +169,66 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
+# the reference's GPU algorithm restated on torch: a measurement baseline
+# ---------------------------------------------------------------------------
+def reference_algorithm_on_torch(dev, host_spectra, n_real):
+    """Realisations/s of the reference's own GPU algorithm (its cupy backend,
+    gpu.py:4-20) restated on torch, one realisation at a time: the shifted
+    2-D FFTs of utils.py:42-50 (cuFFT through torch.fft), the transfer function
+    of theory/vacuum.py:5-7, the complex64 screen GEMM of
+    phase_screens.py:125-126 (cuBLAS through torch's matmul), the exp(-i phi)
+    multiply of pathes.py:72-73 and the pupil and measures of pupils.py:8-13 and
+    measures.py:1-38, each measure a separate reduction read back to the host.
+    A timing baseline only: nothing of the engine runs here."""
+    import torch
+    w = WORKLOAD
+    N, d, wvl, L, n = w["N"], w["delta"], w["wvl"], w["length"], w["count"]
+    k = 2 * math.pi / wvl
+    ax = (torch.arange(N, device=dev, dtype=torch.float32) - N // 2) * d
+    x, y = ax.reshape(1, N), ax.reshape(N, 1)
+    r2 = x * x + y * y
+    fa = (torch.arange(N, device=dev, dtype=torch.float32) - N // 2) / (N * d)
+    f2 = fa.reshape(1, N) ** 2 + fa.reshape(N, 1) ** 2
+    pupil = (r2 <= w["pupil_radius"] ** 2)
+    pos = positions(L, n)
+    steps = [pos[0]] + [pos[i] - pos[i - 1] for i in range(1, n)] + [L - pos[-1]]
+    u0 = (math.sqrt(2 / math.pi) / w["w0"] * torch.exp(-r2 / w["w0"] ** 2)).to(torch.complex64)
+
+    def vac(u, dz):
+        U = torch.fft.fftshift(torch.fft.fft2(torch.fft.fftshift(u))) * d * d
+        h = torch.exp(torch.tensor(1j * k * dz, dtype=torch.complex64, device=dev)) * \
+            torch.exp(-1j * (math.pi * dz * wvl) * f2)
+        # (N df)^2 with df = 1 / (N delta)
+        return (torch.fft.ifftshift(torch.fft.ifft2(torch.fft.ifftshift(U * h))) / (d * d)).to(torch.complex64)
+
+    rho, theta, value = (torch.from_numpy(a).to(dev) for a in host_spectra)
+
+    def one(r):
+        u = u0
+        for i in range(n):
+            u = vac(u, steps[i])
+            fx = (rho[r, i] * torch.cos(theta[r, i])).reshape(1, -1)
+            fy = (rho[r, i] * torch.sin(theta[r, i])).reshape(-1, 1)
+            a = value[r, i].reshape(1, -1) * torch.exp(2j * math.pi * (y @ fy.T))
+            b = torch.exp(2j * math.pi * (fx.T @ x))
+            u = torch.exp(-1j * (a @ b).real) * u
+        u = vac(u, steps[n])
+        I = u.real ** 2 + u.imag ** 2
+        out = [float((I * pupil).sum() * d * d)]
+        for wgt in (x, -y, x * x, -x * y, y * y):
+            out.append(float((I * wgt).sum() * d * d))
+        return out
+
+    one(0)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for r in range(n_real):
+        one(r % rho.shape[0])
+    torch.cuda.synchronize()
+    return n_real / (time.perf_counter() - t)
+
+
+# ---------------------------------------------------------------------------
 # GB300 engine
 # ---------------------------------------------------------------------------
 def surrogate_leg(args, dev):
@@ -311,21 +371,39 @@ def run_gb300(args, rank, world, local_rank):
         plan.run(*devin[s], out=out[s])
     torch.cuda.synchronize()
 
-    # ---- device-resident timed region, kernels bracketed by CUDA events ----
+    # ---- device-resident timed region: one captured CUDA graph per step (each
+    # step's whole launch sequence, its spectra already in HBM), replayed; the
+    # engine's event pair around every kernel is captured with it ----
     launches = plan.info["launches_per_run"] * args.steps
     plan.profile_begin(launches + 8)
     stream = torch.cuda.current_stream(dev)
+    graphs = []
+    if args.graph:
+        cap = torch.cuda.Stream(device=dev)
+        cap.wait_stream(stream)
+        for s in range(args.warmup, n_steps):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=cap):
+                plan.run(*devin[s], out=out[s])
+            graphs.append(g)
+        stream.wait_stream(cap)
+        torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clocks:
         barrier()
         torch.cuda.synchronize()
         e0.record(stream)
-        for s in range(args.warmup, n_steps):
-            plan.run(*devin[s], out=out[s])
+        if graphs:
+            for g in graphs:
+                g.replay()
+        else:
+            for s in range(args.warmup, n_steps):
+                plan.run(*devin[s], out=out[s])
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
     prof = plan.profile_end()
+    plan.check()
     ms = e0.elapsed_time(e1)
     t_max = torch.tensor([ms], dtype=torch.float64, device=dev)
     if world > 1:
@@ -373,6 +451,9 @@ def run_gb300(args, rank, world, local_rank):
         torch.cuda.synchronize()
         plain = args.plain / (e4.elapsed_time(e5) * 1e-3)
         p1.close()
+    torch_ref = None
+    if args.torch_reference > 0 and rank == 0:
+        torch_ref = reference_algorithm_on_torch(dev, [a[:16] for a in host[args.warmup]], args.torch_reference)
 
     # ---- roofline of the dominant kernel, measured in the timed region ----
     N, n = w["N"], w["count"]
@@ -444,28 +525,42 @@ def run_gb300(args, rank, world, local_rank):
                          "the reference path in its own precision (OpenBLAS threads = cores; numpy FFT single-threaded)"}
 
     if rank == 0:
+        def r3(v):
+            return None if v is None else float(f"{v:.4g}")
+
+        # standard keys first; the measured extras last, compact, so that the
+        # headline ratios sit at the end of the line
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32 (complex64 field, FP64 phase arguments and accumulators)",
+            "vs_baseline": None, "dtype": "fp32 (c64 field; fp64 phase args, accumulators)",
             "data": "synthetic (seeded spectra, reference formulas)",
-            "config": {"workload": WORKLOAD_NAME, "batch": B, "realisations_per_step": B, "gemm": args.gemm,
-                       "l2": "inputs larger than L2 (field batch 8.6 GB per step)", "gemm_k": K,
-                       "low_annuli": info["low_annuli"], "cheb_terms": info["cheb_terms"], "autotune": tuned,
-                       "field_layout": "tiled 4x4 blocks" if info.get("tiled") else "row-major",
-                       "gemm_form": ["fp32 simt", "tcgen05 cp.async", "tcgen05 persistent tma 128x128",
-                                     "tcgen05 persistent tma 128x256"][info["gemm_form"]]},
+            "config": {"workload": "2048^2 advanced channel, 50 km, 5 SS screens x 1024", "batch": B,
+                       "realisations_per_step": B, "timed_as": "cuda graph replay" if graphs else "direct launches",
+                       "l2": "inputs > L2 (8.6 GB field batch)", "gemm_k": K,
+                       "layout": "tiled" if info.get("tiled") else "row-major", "autotune": tuned,
+                       "gemm": ["simt", "tc cp.async", "tc tma 128x128", "tc tma 128x256"][info["gemm_form"]]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "plain": {"value": plain, "unit": UNIT, "realisations": args.plain,
-                      "batched_over_plain": (value / world / plain) if plain else None},
             "gpu_launches": sum(v["launches"] for v in prof.values()),
             "roofline": roof(dom),
-            "roofline_hbm": roof(hbm_dom),
-            "kernels": kernels,
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
-            "surrogate": sur,
-            "mixed": mixed,
+            "roofline_hbm": roof(hbm_dom),
+            "kernels": {k: {"ms": r3(e["avg_ms"]), "n": e["launches"], "share": r3(e["share"]),
+                            **({"frac": r3(e["frac"]), "bound": e["bound"]} if "frac" in e else {})}
+                        for k, e in kernels.items()},
+            "mixed": None if mixed is None else {k: mixed[k] for k in ("channels", "realisations_per_channel",
+                                                                      "seconds", "channels_per_s",
+                                                                      "realisations_per_s", "one_graph")
+                                                 if k in mixed},
+            "surrogate": None if sur is None else {k: r3(sur[k]) if isinstance(sur[k], float) else sur[k]
+                                                   for k in ("queries_per_s", "e2e_queries_per_s",
+                                                             "frac_ks_le_0.02", "ks_binned_median",
+                                                             "answered_frac", "heldout_points")
+                                                   if k in sur},
+            "plain": {"value": r3(plain), "batched_over_plain": r3(value / world / plain) if plain else None,
+                      "torch_reference_algorithm": r3(torch_ref),
+                      "batched_over_torch_reference": r3(value / world / torch_ref) if torch_ref else None},
         }
         print(json.dumps(line), flush=True)
     if plan is not None:
@@ -487,6 +582,9 @@ def main():
     ap.add_argument("--autotune", type=int, default=1, help="time the FFT-pass launch variants first (atm_autotune)")
     ap.add_argument("--cheb-cut", type=float, default=0.0,
                     help="annuli below cheb_cut / (N delta) go into the Chebyshev block (0: the engine default)")
+    ap.add_argument("--graph", type=int, default=1, help="time the batched steps as captured CUDA graphs (0: direct)")
+    ap.add_argument("--torch-reference", type=int, default=16,
+                    help="realisations of the reference's GPU algorithm restated on torch (0: skip)")
     ap.add_argument("--layout", choices=["auto", "tiled", "rowmajor"], default="auto",
                     help="field layout between the FFT passes (tiled: 4 x 4 blocks of 128 bytes)")
     ap.add_argument("--variants", default="",

@@ -132,7 +132,10 @@ typedef struct AtmPlanInfo {
                                  3: persistent with tiles loaded by TMA (loads overlap the FFTs),
                                  4: as 3 with the FFT exchanges alternating between two buffers
                                     (one barrier per exchange instead of two),
-                                 5: as 4 on the tiled layout (block columns of 4 columns) */
+                                 5: as 4 on the tiled layout (block columns of 4 columns),
+                                 6: tiled layout, each column of a block column transformed by its own
+                                    warps with their own named barrier; a producer warp loads and stores
+                                    the block columns with TMA */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
                                  form with 128 x 128 tiles (ATM_FLAG_TC_N128), 3 the same with 128 x 256

@@ -433,7 +433,7 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   pl->tiled = atm::tiled_supported(pl->N) && (d->flags & ATM_FLAG_TILED) && !(d->flags & ATM_FLAG_ROWMAJOR);
   if (pl->tiled) {
     pl->row_variant = 5;
-    pl->col_variant = 5;
+    pl->col_variant = 6;
     pl->col_tile = 4;
   }
   pl->rows = pl->tiled ? 1 : atm::row_pass_rows(pl->N);
@@ -942,7 +942,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   for (int C : {2, 4, 8, 16}) {
     if (C * (N / 16) > 512 || C > N) continue;
     if (pl->tiled && C != 4) continue;
-    for (int v = pl->tiled ? 5 : 0; v < (pl->tiled ? 6 : 5); ++v) {
+    for (int v = pl->tiled ? 5 : 0; v < (pl->tiled ? 7 : 5); ++v) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
       if (ms >= 0 && (best_col < 0 || ms < best_col)) {
@@ -976,9 +976,10 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
     // a tiled plan's field is only understood by the tiled forms
     if (row_variant != 5 && row_variant != 6)
       return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5 or 6", row_variant);
-    if (col_variant != 5 || col_tile != 4)
-      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5 with col_tile 4");
+    if ((col_variant != 5 && col_variant != 6) || col_tile != 4)
+      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5 or 6 with col_tile 4");
     pl->row_variant = row_variant;
+    pl->col_variant = col_variant;
     return ATM_OK;
   }
   if (row_variant < 0 || row_variant > 4) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4", row_variant);

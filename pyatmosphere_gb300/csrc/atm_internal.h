@@ -94,7 +94,9 @@ struct ColArgs {
                             // 3: persistent, tiles loaded by TMA (one thread) so loads overlap the FFTs,
                             // 4: as 3 with alternating exchange buffers,
                             // 5: as 4 on the tiled layout (one block column of 4 columns per item,
-                            //    whole 128-byte lines in and out)
+                            //    whole 128-byte lines in and out),
+                            // 6: tiled layout with one independent thread group per column and a TMA
+                            //    producer / store warp
   int* status;              // plan status word (nullable): STATUS_PASS_WAIT on a wait that runs out
 };
 

@@ -597,39 +597,37 @@ __device__ __forceinline__ void measure_row_grp(const RowArgs& a, double* partia
 template <int N>
 struct RowTiled {
   static constexpr int T = N / 16;
-  static constexpr int NT = 4 * T;
+  static constexpr int NTG = 4 * T;                                           // row-group threads
+  static constexpr int NT = NTG + 32;                                         // + the producer warp
   static constexpr size_t STAGE = (size_t)4 * N * sizeof(float2);          // one block row, a multiple of 1024
   static constexpr size_t EXCH = (size_t)Padded<N>::value * sizeof(float2);  // one row's FFT exchange area
   static constexpr size_t SMEM = 1024 + 2 * STAGE + 4 * EXCH + EXCH;         // + twiddles + alignment slack
   static constexpr int BOX = (N / 4 < 256) ? N / 4 : 256;                     // blocks per tensor copy
 };
 
-// One item = one block row (realisation r, rows 4 yb .. 4 yb + 3).  Thread 0
-// moves the next item's block row into the other stage (tiled input: 128-byte
+// One item = one block row (realisation r, rows 4 yb .. 4 yb + 3).  A
+// producer warp moves item k into stage k % 2 (tiled input: 128-byte
 // swizzled tensor copies of its N / 4 consecutive blocks; row-major input:
-// one bulk copy per row) once every warp has released that stage's previous
-// contents on an `empty` mbarrier.  Each row's N / 16 threads then run
-// alone: they read their row from the stage, release it, and transform it
+// one bulk copy per row) once every row-group warp has released the stage's
+// previous contents on an `empty` mbarrier.  Each row's N / 16 threads then
+// run alone: they read their row from the stage, release it, and transform it
 // in their own exchange area with their own named barrier.  Bounded waits:
-// on timeout the group records an error and leaves; thread 0 drains its
-// copies in flight first.
+// on timeout a group (or the producer) records an error and leaves; the
+// producer drains its copies in flight first.
 template <int N, int TWREC>
-__global__ void __launch_bounds__(4 * (N / 16), 2048 / N)
+__global__ void __launch_bounds__(RowTiled<N>::NT, 2048 / N)
 row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int n_items) {
   using Cfg = RowTiled<N>;
   constexpr int T = Cfg::T;
-  constexpr int NT = Cfg::NT;
   constexpr int NRB = N / 4;  // block rows per realisation = blocks per block row
   constexpr int NWG = T >= 32 ? T / 32 : 1;
   constexpr int MM = 6 + kMaxPupils;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
   __shared__ float red[4][NWG][MM];
-  const int tid = threadIdx.x, rl = tid / T, t = tid - rl * T;
-  const int bar = 1 + rl;
+  const int tid = threadIdx.x;
   unsigned char* sbase = smem_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u);
   auto stage = [&](int s) { return reinterpret_cast<float2*>(sbase + s * Cfg::STAGE); };
-  float2* exch = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + rl * Cfg::EXCH);
   float2* tws = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + 4 * Cfg::EXCH);
   load_twiddles<N>(tws, a.tw);
   const int flags = a.flags;
@@ -644,63 +642,77 @@ row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int 
   if (tid == 0) {
     for (int q = 0; q < 2; ++q) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fb0 + 8 * q) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(eb0 + 8 * q), "r"(NT / 32) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(eb0 + 8 * q), "r"(Cfg::NTG / 32) : "memory");
     }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
-  int fills[2] = {0, 0};             // thread 0: copies issued into each stage
-  bool pending[2] = {false, false};  // thread 0: issued and not yet waited for
-  bool producer_ok = true;
-  auto prefetch = [&](int item, int s) -> bool {
-    // the stage's previous contents have been read by every warp
-    if (fills[s] > 0 && !pass_mbar_wait(eb0 + 8 * s, (uint32_t)((fills[s] - 1) & 1), wait_ns)) return false;
-    const int r = item / NRB, yb = item - r * NRB;
-    const uint32_t fb = fb0 + 8 * s;
-    const uint32_t d0 = (uint32_t)__cvta_generic_to_shared(stage(s));
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::STAGE)
-                 : "memory");
-    if (in_tiled) {
-#pragma unroll 1
-      for (int b = 0; b < NRB / Cfg::BOX; ++b)
-        asm volatile(
-            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
-            "%4}], [%5];\n" ::"r"(d0 + (uint32_t)(b * Cfg::BOX * 128)),
-            "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(0), "r"(yb * NRB + b * Cfg::BOX), "r"(r), "r"(fb)
-            : "memory");
-    } else {
-      const float2* src = a.field + (size_t)r * N * N + (size_t)yb * 4 * N;
-#pragma unroll 1
-      for (int q = 0; q < 4; ++q)
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                d0 + (uint32_t)(q * N * sizeof(float2))),
-            "l"(src + (size_t)q * N), "r"((uint32_t)(N * sizeof(float2))), "r"(fb)
-            : "memory");
-    }
-    ++fills[s];
-    pending[s] = true;
-    return true;
-  };
 
-  int item = blockIdx.x, s = 0, k = 0;
-  if (tid == 0 && load_field && item < n_items) producer_ok = prefetch(item, 0);
-  for (; item < n_items; item += gridDim.x, s ^= 1, ++k) {
-    const int next = item + gridDim.x;
-    if (tid == 0 && load_field && producer_ok && next < n_items) producer_ok = prefetch(next, s ^ 1);
-    bool ok = tid != 0 || producer_ok;
+  if (tid >= Cfg::NTG) {
+    // ---- producer warp: lane 0 moves the block rows in ----
+    if (tid != Cfg::NTG || !load_field) return;
+    int fills[2] = {0, 0};
+    bool ok = true;
+    int k = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++k) {
+      const int s = k & 1;
+      // every row-group warp has read item k - 2 out of stage s
+      if (k >= 2 && !pass_mbar_wait(eb0 + 8 * s, (uint32_t)(((k - 2) >> 1) & 1), wait_ns)) {
+        ok = false;
+        break;
+      }
+      const int r = item / NRB, yb = item - r * NRB;
+      const uint32_t fb = fb0 + 8 * s;
+      const uint32_t d0 = (uint32_t)__cvta_generic_to_shared(stage(s));
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::STAGE)
+                   : "memory");
+      if (in_tiled) {
+#pragma unroll 1
+        for (int b = 0; b < NRB / Cfg::BOX; ++b)
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+              "%4}], [%5];\n" ::"r"(d0 + (uint32_t)(b * Cfg::BOX * 128)),
+              "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(0), "r"(yb * NRB + b * Cfg::BOX), "r"(r), "r"(fb)
+              : "memory");
+      } else {
+        const float2* src = a.field + (size_t)r * N * N + (size_t)yb * 4 * N;
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q)
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                  d0 + (uint32_t)(q * N * sizeof(float2))),
+              "l"(src + (size_t)q * N), "r"((uint32_t)(N * sizeof(float2))), "r"(fb)
+              : "memory");
+      }
+      ++fills[s];
+    }
+    if (!ok) {
+      atomicExch(&g_pass_error, 1);
+      if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+    }
+    // no copy may land after the CTA leaves: wait (bounded) for the last fill of each stage
+    for (int q = 0; q < 2; ++q)
+      if (fills[q] > 0) pass_mbar_wait(fb0 + 8 * q, (uint32_t)((fills[q] - 1) & 1));
+    return;
+  }
+
+  // ---- row groups: group rl transforms row rl of each block row ----
+  const int rl = tid / T, t = tid - rl * T;
+  const int bar = 1 + rl;
+  float2* exch = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + rl * Cfg::EXCH);
+  int k = 0;
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++k) {
+    const int s = k & 1;
     if (load_field) {
       // item k of this CTA uses stage k & 1 for the (k >> 1)-th time
       const bool landed = pass_mbar_wait(fb0 + 8 * s, (uint32_t)((k >> 1) & 1), wait_ns);
-      if (tid == 0 && landed) pending[s] = false;
-      ok = ok && landed;
-    }
-    if (!group_all(bar, T, ok)) {
-      if (t == 0) {
-        atomicExch(&g_pass_error, 1);
-        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      if (!group_all(bar, T, landed)) {
+        if (t == 0) {
+          atomicExch(&g_pass_error, 1);
+          if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+        }
+        break;
       }
-      break;
     }
     const int r = item / NRB, yb = item - r * NRB;
     const int y = yb * 4 + rl;
@@ -769,10 +781,6 @@ row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int 
     if (flags & ROW_MEAS)
       measure_row_grp<N>(a, a.partials, a.center, a.n_meas, a.n_pupils, true, v, t, y, r, bar, red[rl]);
   }
-  // no copy may land after the CTA leaves: wait (bounded) for any still pending
-  if (tid == 0)
-    for (int q = 0; q < 2; ++q)
-      if (pending[q]) pass_mbar_wait(fb0 + 8 * q, (uint32_t)((fills[q] - 1) & 1));
 }
 
 template <int N, int TWREC>
@@ -1239,6 +1247,174 @@ static cudaError_t col_tiled_launch(int B, const ColArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// column pass on the tiled layout with independent column groups.  Each of
+// the four columns of a block column is transformed by its own group of N/16
+// threads that synchronise on their own named barrier, so the groups drift
+// apart and one group's shared-memory exchanges overlap another's
+// arithmetic (with one barrier for all sixteen warps they all exchange at
+// once and then all compute).  A producer warp moves the block columns with
+// TMA: the groups write their outputs back into the stage they read from,
+// and once all have (the `done` mbarrier) the producer stores the stage with
+// tensor stores, waits until the stores have read it, and loads item k + 2
+// into it.  Bounded waits everywhere: on timeout a group or the producer
+// records an error and leaves; the producer first drains its copies.
+// ---------------------------------------------------------------------------
+template <int N>
+struct ColGroups {
+  static constexpr int T = N / 16;
+  static constexpr int NTG = 4 * T;                                           // group threads
+  static constexpr int NT = NTG + 32;                                         // + the producer warp
+  static constexpr size_t TILE = (size_t)N * 4 * sizeof(float2);              // one block column
+  static constexpr size_t EXCH = (size_t)Padded<N>::value * sizeof(float2);  // one column's exchange area
+  static constexpr size_t SMEM = 1024 + 2 * TILE + 4 * EXCH + EXCH;           // + twiddles + alignment slack
+  static constexpr int BOX = (N / 4 < 256) ? N / 4 : 256;                     // blocks per tensor copy
+};
+
+__device__ __forceinline__ void tma_store_col(const CUtensorMap* map, uint32_t src, int x, int y, int z) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];\n" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z), "r"(src)
+               : "memory");
+}
+
+template <int N>
+__global__ void __launch_bounds__(ColGroups<N>::NT, 1)
+col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
+  using Cfg = ColGroups<N>;
+  constexpr int T = Cfg::T;
+  constexpr int NCT = N / 4;  // block columns per realisation
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[2], done_bar[2];
+  const int tid = threadIdx.x;
+  unsigned char* sbase = smem_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u);
+  auto stage = [&](int s) { return reinterpret_cast<float2*>(sbase + s * Cfg::TILE); };
+  float2* tws = reinterpret_cast<float2*>(sbase + 2 * Cfg::TILE + 4 * Cfg::EXCH);
+  load_twiddles<N>(tws, a.tw);
+  const unsigned long long wait_ns = g_pass_wait_ns;
+  const uint32_t fb0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
+  const uint32_t db0 = (uint32_t)__cvta_generic_to_shared(&done_bar[0]);
+  if (tid == 0) {
+    for (int q = 0; q < 2; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fb0 + 8 * q) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(db0 + 8 * q), "r"(Cfg::NTG) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+
+  if (tid >= Cfg::NTG) {
+    // ---- producer warp: lane 0 loads and stores the block columns ----
+    if (tid != Cfg::NTG) return;
+    auto store_item = [&](int item, int s) {
+      const int r = item / NCT, xb = item - r * NCT;
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      const uint32_t src = (uint32_t)__cvta_generic_to_shared(stage(s));
+#pragma unroll 1
+      for (int b = 0; b < NCT / Cfg::BOX; ++b)
+        tma_store_col(&tiles, src + (uint32_t)(b * Cfg::BOX * 128), 0, xb, r * NCT + b * Cfg::BOX);
+      asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+    };
+    int fills[2] = {0, 0};
+    bool ok = true;
+    int k = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++k) {
+      const int s = k & 1;
+      if (k >= 2) {
+        // the groups have written item k - 2's outputs into stage s: store them and
+        // wait until the stores have read the stage before it is refilled
+        if (!pass_mbar_wait(db0 + 8 * s, (uint32_t)(((k - 2) >> 1) & 1), wait_ns)) {
+          ok = false;
+          break;
+        }
+        store_item(item - 2 * gridDim.x, s);
+        asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+      }
+      const int r = item / NCT, xb = item - r * NCT;
+      const uint32_t fb = fb0 + 8 * s;
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(stage(s));
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::TILE)
+                   : "memory");
+#pragma unroll 1
+      for (int b = 0; b < NCT / Cfg::BOX; ++b)
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4}], [%5];\n" ::"r"(dst + (uint32_t)(b * Cfg::BOX * 128)),
+            "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(0), "r"(xb), "r"(r * NCT + b * Cfg::BOX), "r"(fb)
+            : "memory");
+      ++fills[s];
+    }
+    // the outputs of the last two items
+    for (int j = (k >= 2 ? k - 2 : 0); ok && j < k; ++j) {
+      const int s = j & 1;
+      if (!pass_mbar_wait(db0 + 8 * s, (uint32_t)((j >> 1) & 1), wait_ns)) {
+        ok = false;
+        break;
+      }
+      store_item(blockIdx.x + j * gridDim.x, s);
+    }
+    if (!ok) {
+      atomicExch(&g_pass_error, 1);
+      if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      // no load may land after the CTA leaves: wait (bounded) for the last fill of each stage
+      for (int q = 0; q < 2; ++q)
+        if (fills[q] > 0) pass_mbar_wait(fb0 + 8 * q, (uint32_t)((fills[q] - 1) & 1));
+    }
+    asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");  // the stores have read shared memory
+    return;
+  }
+
+  // ---- column groups: group g transforms column g of each block column ----
+  const int g = tid / T, t = tid - g * T;
+  const int bar = 1 + g;
+  float2* exch = reinterpret_cast<float2*>(sbase + 2 * Cfg::TILE + g * Cfg::EXCH);
+  int k = 0;
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++k) {
+    const int s = k & 1;
+    const bool landed = pass_mbar_wait(fb0 + 8 * s, (uint32_t)((k >> 1) & 1), wait_ns);
+    if (!group_all(bar, T, landed)) {
+      if (t == 0) {
+        atomicExch(&g_pass_error, 1);
+        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      }
+      break;
+    }
+    const int xb = item % NCT;
+    float2* tile = stage(s);
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = tile[colblock_slot(t + m * T, g)];
+    if (!a.inv_only) {
+      fft_dev_grp<N, -1, 0, 1>(v, exch, t, tws, bar);
+      const float2 hx = a.hx[xb * 4 + g];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(__ldg(a.hy + t + m * T), hx));
+    }
+    fft_dev_grp<N, 1, 0, 1>(v, exch, t, tws, bar);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) tile[colblock_slot(t + m * T, g)] = v[m];
+    // this thread's outputs are in the stage: visible to the tensor store (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    mbar_arrive_cta(db0 + 8 * s);
+  }
+}
+
+template <int N>
+static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
+  alignas(128) CUtensorMap map;
+  if (!encode_tiled_field(&map, a.field, N, B, false, ColGroups<N>::BOX)) return cudaErrorNotSupported;
+  static LaunchCache cache;
+  const int threads = ColGroups<N>::NT;
+  const size_t smem = ColGroups<N>::SMEM;
+  int grid_max = 0;
+  cudaError_t e = cache.get(col_pass_groups_kernel<N>, threads, smem, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_items = B * (N / 4);
+  const int grid = std::max(1, std::min(n_items, grid_max));
+  col_pass_groups_kernel<N><<<grid, threads, smem, st>>>(map, a, n_items);
+  return cudaGetLastError();
+}
+
 template <int N, int C, int TWREC>
 static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
   static LaunchCache cache;
@@ -1315,13 +1491,14 @@ static cudaError_t col_dispatch(int C, int B, const ColArgs& a, cudaStream_t st)
 }
 
 cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t st) {
-  if (a.variant == 5) {
+  if (a.variant == 5 || a.variant == 6) {
     // the tiled layout: tiles are block columns (4 columns); C does not apply
     if (!aligned16(a.field)) return cudaErrorInvalidValue;
+    const bool groups = a.variant == 6;
     switch (N) {
-      case 512: return col_tiled_launch<512>(B, a, st);
-      case 1024: return col_tiled_launch<1024>(B, a, st);
-      case 2048: return col_tiled_launch<2048>(B, a, st);
+      case 512: return groups ? col_groups_launch<512>(B, a, st) : col_tiled_launch<512>(B, a, st);
+      case 1024: return groups ? col_groups_launch<1024>(B, a, st) : col_tiled_launch<1024>(B, a, st);
+      case 2048: return groups ? col_groups_launch<2048>(B, a, st) : col_tiled_launch<2048>(B, a, st);
     }
     return cudaErrorInvalidValue;
   }

@@ -1,13 +1,15 @@
-"""Maps a Channel object graph to engine plans and spectra.
+"""Maps a channel object graph onto engine plans and spectra.
 
-A plan is built per (geometry, batch, pupils, screen shift, loss mode) and
-cached on the channel.  Spectra are taken from each screen's
-``_get_spectrum`` (numpy global RNG in the reference's draw order, or an
-injected spectrum) and stacked as [batch][n_screens][P].
+The channel may be this package's Channel or the reference package's own
+(channels.py:17-29): both expose the same attributes, which is all this
+module reads -- grid.resolution / delta, source.wvl / w0 / F0,
+path.length / losses_db / positions / phase_screens, and per screen
+f_grid.base and _get_spectrum.  A plan is built per (geometry, batch,
+pupils, screen shift, loss mode) and cached on the channel.  Spectra come
+from each screen's ``_get_spectrum`` (numpy's global generator in the
+reference's draw order, or an injected spectrum), stacked [batch][n][P].
 """
 from __future__ import annotations
-
-from typing import List, Sequence, Tuple
 
 import numpy as np
 
@@ -15,42 +17,61 @@ from .. import gpu
 from . import _lib
 
 
-def _path_geometry(channel):
-    from ..pathes import PhaseScreensPath, VacuumPath
-    path = channel.path
-    if isinstance(path, PhaseScreensPath):
-        screens = path.phase_screens
-        from ..phase_screens import SSPhaseScreen
-        if not all(isinstance(s, SSPhaseScreen) for s in screens):
-            raise NotImplementedError("the batched engine path needs SSPhaseScreen screens")
-        bases = [np.asarray(s.f_grid.base, np.float32) for s in screens]
-        if any(b.shape != bases[0].shape or not np.array_equal(b, bases[0]) for b in bases):
-            raise NotImplementedError("all screens of a path must share one RandLogPolarGrid")
-        return list(map(float, path.positions)), float(path.length), float(path.losses_db or 0.0), bases[0]
-    if isinstance(path, VacuumPath):
+def grid_size(grid) -> int:
+    """N of a square grid (RectGrid.resolution is an int or a pair)."""
+    res = grid.resolution
+    nx, ny = (res, res) if np.ndim(res) == 0 else (res[0], res[1])
+    if int(nx) != int(ny):
+        raise NotImplementedError(f"the engine propagates square grids only, not {nx} x {ny}")
+    return int(nx)
+
+
+def source_kind(source):
+    """('gaussian' | 'plane', wvl, w0, F0) of a GaussianSource / PlaneSource."""
+    name = type(source).__name__
+    if name == "GaussianSource":
+        return "gaussian", float(source.wvl), float(source.w0), float(source.F0)
+    if name == "PlaneSource":
+        return "plane", float(source.wvl), 0.0, float("inf")
+    raise NotImplementedError(f"unsupported source type {name}")
+
+
+def path_geometry(path):
+    """(screen positions, length, losses_db, annulus radii or None) of a
+    VacuumPath or a path of sparse-spectrum screens sharing one spectral grid."""
+    screens = getattr(path, "phase_screens", None)
+    if screens is None:
+        if type(path).__name__ != "VacuumPath":
+            raise NotImplementedError(f"unsupported path type {type(path).__name__}")
         return [], float(path.length), float(path.losses_db or 0.0), None
-    raise NotImplementedError(f"unsupported path type {type(path).__name__}")
+    if not all(type(s).__name__ == "SSPhaseScreen" for s in screens):
+        raise NotImplementedError("the fused engine path takes SSPhaseScreen screens")
+    bases = [np.asarray(s.f_grid.base, np.float32) for s in screens]
+    if any(not np.array_equal(b, bases[0]) for b in bases):
+        raise NotImplementedError("all screens of a path must share one RandLogPolarGrid")
+    return [float(p) for p in path.positions], float(path.length), float(path.losses_db or 0.0), bases[0]
 
 
-def _source(channel):
-    from ..sources import GaussianSource, PlaneSource
-    s = channel.source
-    if isinstance(s, GaussianSource):
-        return "gaussian", float(s.wvl), float(s.w0), float(s.F0)
-    if isinstance(s, PlaneSource):
-        return "plane", float(s.wvl), 0.0, float("inf")
-    raise NotImplementedError(f"unsupported source type {type(s).__name__}")
+def fusable(channel) -> bool:
+    """Whether the fused engine call (atm_run) serves the channel."""
+    try:
+        source_kind(channel.source)
+        path_geometry(channel.path)
+        grid_size(channel.grid)
+    except NotImplementedError:
+        return False
+    return True
 
 
-def get_plan(channel, batch: int = 1, pupils: Sequence[tuple] = (), tracked: Sequence[float] = (),
-             shift=(0.0, 0.0), path_output_loss: bool = False, length=None, step_measures: bool = False):
+def get_plan(channel, batch: int = 1, pupils=(), tracked=(), shift=(0.0, 0.0), path_output_loss: bool = False,
+             length=None, step_measures: bool = False):
     from .plan import EnginePlan
     gpu.require_engine()
-    positions, L, losses, base = _path_geometry(channel)
+    positions, L, losses, base = path_geometry(channel.path)
     if length is not None:
         L = float(length)
-    kind, wvl, w0, F0 = _source(channel)
-    N, delta = channel.grid.N, float(channel.grid.delta)
+    kind, wvl, w0, F0 = source_kind(channel.source)
+    N, delta = grid_size(channel.grid), float(channel.grid.delta)
     key = (N, delta, kind, wvl, w0, F0, tuple(positions), L, losses,
            None if base is None else base.tobytes(), int(batch), tuple(map(tuple, pupils)), tuple(tracked),
            (float(shift[0]), float(shift[1])), bool(path_output_loss), gpu.config.get("cheb_cut", 0.0),
@@ -71,8 +92,8 @@ def get_plan(channel, batch: int = 1, pupils: Sequence[tuple] = (), tracked: Seq
 
 
 def draw_channel_spectra(channel, realisations: int, wind: bool = False, clear: bool = True):
-    """Spectra of `realisations` consecutive realisations, drawn like the
-    reference's Simulation.iter does (cache_clear, then each screen's
+    """Spectra of `realisations` consecutive realisations, drawn as the
+    per-realisation loop draws them (cache_clear, then each screen's
     _get_spectrum in path order).  Returns numpy (rho, theta, value)."""
     screens = channel.path.phase_screens
     n, P = len(screens), screens[0].f_grid.points

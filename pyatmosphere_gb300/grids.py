@@ -1,9 +1,17 @@
-"""Grids (the reference's grids.py:7-119).
+"""Sample grids of a channel: the spatial grid of the field and the random
+log-polar grid of the sparse screen spectrum (the reference's
+grids.py:7-119 offers the same classes and methods).
 
-``RectGrid`` coordinates are float32 like the reference's, returned as torch
-tensors on the engine's device.  ``RandLogPolarGrid`` draws from numpy's
-global RNG in the reference's order, so ``np.random.seed(s)`` reproduces the
-reference's spectra.
+RectGrid puts sample j of an axis of n points at (j - n // 2) * delta, the
+x axis along the columns (resolution[0] points) and the y axis down the rows
+(resolution[1] points).  Coordinates are float32 products of the index and
+delta, the values the reference's float32 aranges produce, returned as torch
+tensors on the engine device.
+
+RandLogPolarGrid draws its annulus radii and angles from numpy's global
+generator, one uniform for all radii and one uniform per angle, in the order
+the reference draws them, so that ``np.random.seed(s)`` gives the reference's
+spectra.
 """
 from __future__ import annotations
 
@@ -17,8 +25,15 @@ __all__ = ["Grid", "RectGrid", "RandLogPolarGrid"]
 
 
 class Grid:
+    """Base of the grids: the array module their outputs belong to."""
+
     def get_array_module(self):
         return gpu.get_xp()
+
+
+def _centred(n: int) -> np.ndarray:
+    """Sample indices of an n-point axis, relative to its origin sample n // 2."""
+    return np.arange(n, dtype=np.int64) - n // 2
 
 
 @dataclass
@@ -27,83 +42,81 @@ class RectGrid(Grid):
     delta: float
 
     def __post_init__(self):
-        if isinstance(self.resolution, (int, np.integer)):
-            self.resolution = (int(self.resolution), int(self.resolution))
+        if np.ndim(self.resolution) == 0:
+            n = int(self.resolution)
+            self.resolution = (n, n)
         else:
-            self.resolution = tuple(self.resolution)
+            self.resolution = tuple(int(n) for n in self.resolution)
 
-    @property
-    def size(self):
-        return np.array(self.resolution) * self.delta
-
-    @property
-    def extent(self):
-        return np.array([self._left_bound, self._right_bound, self._top_bound, self._bottom_bound]) * self.delta
-
+    # ---- geometry in metres and samples ----------------------------------
     @property
     def shape(self):
         return self.resolution
 
     @property
+    def size(self):
+        return np.asarray(self.resolution, dtype=float) * self.delta
+
+    @property
     def origin_index(self):
-        return (self.resolution[0] // 2, self.resolution[1] // 2)
+        return tuple(n // 2 for n in self.resolution)
 
     @property
-    def _left_bound(self):
-        return -self.resolution[0] // 2 + bool(self.resolution[0] % 2)
+    def extent(self):
+        """(first x, last x + delta, first y, last y + delta): the extent
+        matplotlib's imshow takes."""
+        edges = []
+        for n in self.resolution:
+            idx = _centred(n)
+            edges += [idx[0], idx[-1] + 1]
+        return np.asarray(edges, dtype=float) * self.delta
 
-    @property
-    def _right_bound(self):
-        return self.resolution[0] // 2 + bool(self.resolution[0] % 2)
-
-    @property
-    def _top_bound(self):
-        return -self.resolution[1] // 2 + bool(self.resolution[1] % 2)
-
-    @property
-    def _bottom_bound(self):
-        return self.resolution[1] // 2 + bool(self.resolution[1] % 2)
-
-    def _axis(self, lo, hi):
+    # ---- coordinate arrays (torch, engine device) ------------------------
+    def _coordinates(self, n: int):
         import torch
-        return torch.arange(lo, hi, dtype=torch.float32, device=gpu.device()) * np.float32(self.delta)
-
-    def get_NxNy(self):
-        import torch
-        d = gpu.device()
-        return (torch.arange(self._top_bound, self._bottom_bound, device=d).reshape(-1, 1),
-                torch.arange(self._left_bound, self._right_bound, device=d).reshape(1, -1))
-
-    def get_N2(self):
-        Nx, Ny = self.get_NxNy()
-        return Nx ** 2 + Ny ** 2
+        idx = torch.from_numpy(_centred(n).astype(np.float32)).to(gpu.device())
+        return idx * self.delta  # one float32 product per sample
 
     def get_x(self):
-        return self._axis(self._left_bound, self._right_bound).reshape((1, -1))
+        return self._coordinates(self.resolution[0]).reshape(1, -1)
 
     def get_y(self):
-        return self._axis(self._top_bound, self._bottom_bound).reshape((-1, 1))
+        return self._coordinates(self.resolution[1]).reshape(-1, 1)
 
     def get_xy(self):
         return self.get_x(), self.get_y()
 
     def get_rho2(self):
         x, y = self.get_xy()
-        return x ** 2 + y ** 2
+        return x * x + y * y
 
     def get_rho(self):
         return self.get_rho2().sqrt()
 
-    def get_f_grid(self):
-        return RectGrid(resolution=int(np.min(self.resolution)),
-                        delta=1 / (np.min(self.resolution) * self.delta))
+    def get_NxNy(self):
+        """Integer sample indices: a column of y indices and a row of x indices."""
+        import torch
+        d = gpu.device()
+        iy = torch.from_numpy(_centred(self.resolution[1])).to(d).reshape(-1, 1)
+        ix = torch.from_numpy(_centred(self.resolution[0])).to(d).reshape(1, -1)
+        return iy, ix
 
-    # engine helpers ------------------------------------------------------
+    def get_N2(self):
+        iy, ix = self.get_NxNy()
+        return iy * iy + ix * ix
+
+    def get_f_grid(self):
+        """The reciprocal grid of the FFT: the smaller resolution n, step 1 / (n delta)."""
+        n = int(min(self.resolution))
+        return RectGrid(resolution=n, delta=1 / (n * self.delta))
+
+    # ---- engine helper -----------------------------------------------------
     @property
     def N(self) -> int:
-        if self.resolution[0] != self.resolution[1]:
-            raise ValueError("the engine needs a square grid")
-        return int(self.resolution[0])
+        nx, ny = self.resolution
+        if nx != ny:
+            raise ValueError(f"the engine propagates square grids only, not {nx} x {ny}")
+        return int(nx)
 
 
 @dataclass
@@ -114,13 +127,18 @@ class RandLogPolarGrid(Grid):
 
     @property
     def base(self):
-        return np.exp(np.linspace(np.log(self.f_min), np.log(self.f_max), self.points, dtype=np.float32))
+        """Outer radii [1/m] of the `points` annuli, log-spaced from f_min to
+        f_max, float32."""
+        log_lo, log_hi = np.log(self.f_min), np.log(self.f_max)
+        return np.exp(np.linspace(log_lo, log_hi, self.points, dtype=np.float32))
 
     def rho_from(self, u):
-        """Annulus radii for one uniform draw u (grids.py:98-103)."""
-        f = self.base
-        f_prev = np.insert(f, 0, 0)[:-1]
-        return np.sqrt(f_prev ** 2 + np.asarray(u, np.float32) * (f ** 2 - f_prev ** 2))
+        """Annulus radii for one uniform u in [0, 1): radius i sits at the
+        fraction u of annulus i's area, in float32."""
+        outer = self.base
+        inner = np.concatenate([np.zeros(1, np.float32), outer[:-1]])
+        inner2, outer2 = inner ** 2, outer ** 2
+        return np.sqrt(inner2 + np.asarray(u, np.float32) * (outer2 - inner2))
 
     def get_rho(self):
         return self.rho_from(np.random.random(size=(1,)).astype(np.float32))
@@ -128,11 +146,16 @@ class RandLogPolarGrid(Grid):
     def get_theta(self):
         return 2 * np.pi * np.random.random(size=(self.points,)).astype(np.float32)
 
+    @staticmethod
+    def _components(rho, theta):
+        return rho * np.cos(theta), rho * np.sin(theta)
+
     def get_x(self, rho, theta):
-        return rho * np.cos(theta)
+        return self._components(rho, theta)[0]
 
     def get_y(self, rho, theta):
-        return rho * np.sin(theta)
+        return self._components(rho, theta)[1]
 
     def get_xy(self, rho, theta):
-        return (rho * np.cos(theta)).reshape((1, -1)), (rho * np.sin(theta)).reshape((-1, 1))
+        fx, fy = self._components(rho, theta)
+        return fx.reshape(1, -1), fy.reshape(-1, 1)

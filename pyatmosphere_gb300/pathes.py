@@ -1,9 +1,17 @@
-"""Propagation paths (the reference's pathes.py:10-95) on the GB300 engine.
+"""Propagation paths on the GB300 engine (the reference's pathes.py:10-95
+offers the same classes).
 
-``Channel.run`` sends whole channels to the fused engine (``atm_run``).  The
-path objects themselves also work step by step on any input field
-(``output`` / ``generator``): each vacuum step is ``atm_vacuum`` and each
-screen's phasor comes from ``atm_screen``.
+A path of length L with screens at z_0 < ... < z_{n-1} is the chain of
+segments
+
+    vacuum z_0, screen 0, vacuum z_1 - z_0, screen 1, ..., vacuum L - z_{n-1}
+
+where a screen multiplies the field by exp(-i phi) and by the attenuation of
+the path's share of its losses over the vacuum step before it.  Whole
+channels of Gaussian / plane sources and sparse-spectrum screens go to the
+fused engine (``Channel.run`` -> ``atm_run``); these classes also run the
+chain segment by segment on any field: a vacuum segment is ``atm_vacuum``
+and each screen's phasor comes from ``atm_screen``.
 """
 from __future__ import annotations
 
@@ -16,26 +24,49 @@ from . import gpu
 
 __all__ = ["AbstractPath", "VacuumPath", "PhaseScreensPath", "IdenticalPhaseScreensPath"]
 
+# where each screen of IdenticalPhaseScreensPath sits in its slab, as a
+# fraction of the slab thickness
+_SLAB_OFFSET = {"before": 0.0, "middle": 0.5, "after": 1.0}
+
+
+def attenuate(field, losses_db):
+    """The field after a loss of `losses_db` decibels (unchanged at 0)."""
+    if not losses_db:
+        return field
+    return field * 10 ** (-losses_db / 20)
+
 
 def _vacuum_plan(channel):
+    """A plan (cached on the channel) that only runs atm_vacuum steps."""
     from .engine.plan import EnginePlan
-    N, delta = channel.grid.N, float(channel.grid.delta)
-    key = ("vacuum", N, delta, float(channel.source.wvl), str(gpu.device()))
-    cache = channel.__dict__.setdefault("_atm_plans", {})
-    if key not in cache:
-        cache[key] = EnginePlan(N, delta, float(channel.source.wvl), 1.0, float("inf"), [], 1.0, batch=1,
-                                device=gpu.device())
-    return cache[key]
+    N, delta, wvl = channel.grid.N, float(channel.grid.delta), float(channel.source.wvl)
+    plans = channel.__dict__.setdefault("_atm_plans", {})
+    key = ("vacuum-steps", N, delta, wvl, str(gpu.device()))
+    if key not in plans:
+        plans[key] = EnginePlan(N, delta, wvl, 1.0, float("inf"), [], 1.0, batch=1, device=gpu.device())
+    return plans[key]
 
 
-def _as_field(channel, input):
+def _as_field(channel, value):
+    """A fresh complex64 [N, N] engine tensor holding `value` (a field, or a
+    scalar such as PlaneSource's output broadcast over the grid)."""
     import torch
     N = channel.grid.N
-    if not isinstance(input, torch.Tensor):
-        input = torch.as_tensor(np.broadcast_to(np.asarray(input), (N, N)).copy())
-    if input.dim() == 0 or input.shape != (N, N):
-        input = input.expand(N, N)
-    return input.to(gpu.device(), torch.complex64).contiguous().clone()
+    t = value if isinstance(value, torch.Tensor) else torch.as_tensor(np.asarray(value))
+    t = t.to(gpu.device(), torch.complex64)
+    return t.expand(N, N).clone() if t.shape != (N, N) else t.clone()
+
+
+def _finish(generator):
+    """Exhausts a segment generator and returns its return value."""
+    box = []
+
+    def keep():
+        box.append((yield from generator))
+
+    for _ in keep():
+        pass
+    return box[0]
 
 
 class AbstractPath(ABC):
@@ -45,11 +76,12 @@ class AbstractPath(ABC):
 
     @abstractmethod
     def lossless_output(self, input, *args, **kwargs):
-        pass
+        """The field at the end of the path, before the path's losses."""
 
     def append_losses(self, input, losses_db=None):
-        losses_db = losses_db or self.losses_db
-        return input * 10 ** (-losses_db / 20) if losses_db else input
+        """A segment's own loss; a segment without one (None or 0) takes the
+        whole path's."""
+        return attenuate(input, losses_db if losses_db else self.losses_db)
 
     def output(self, input, *args, **kwargs):
         return self.append_losses(self.lossless_output(input, *args, **kwargs))
@@ -57,62 +89,61 @@ class AbstractPath(ABC):
 
 class VacuumPath(AbstractPath):
     def lossless_output(self, input, length=None):
-        length = length if length is not None else self.length
-        if length > 0:
-            field = _as_field(self.channel, input)
-            return _vacuum_plan(self.channel).vacuum(field, float(length))
-        return input
+        step = self.length if length is None else length
+        if not step > 0:
+            return input  # a zero-length segment leaves the field as it is
+        return _vacuum_plan(self.channel).vacuum(_as_field(self.channel, input), float(step))
 
 
 class PhaseScreensPath(AbstractPath):
     def __init__(self, length, phase_screens, positions, losses_db=0):
-        self.positions = positions
-        self.phase_screens = phase_screens
         super().__init__(length, losses_db)
+        self.phase_screens = phase_screens
+        self.positions = positions
 
     def init_phase_screens(self):
-        for phase_screen in self.phase_screens:
-            phase_screen.channel = self.channel
+        for screen in self.phase_screens:
+            screen.channel = self.channel
+
+    def segments(self):
+        """[(vacuum length before screen i, screen i)], then the length of the
+        last vacuum segment."""
+        z = [0.0] + [float(p) for p in self.positions]
+        steps = [(z[i + 1] - z[i], screen) for i, screen in enumerate(self.phase_screens)]
+        return steps, self.length - z[-1]
 
     def lossless_output(self, input, *args, **kwargs):
-        generator = self.generator(input, *args, **kwargs)
-        try:
-            while True:
-                next(generator)
-        except StopIteration as e:
-            return e.value
+        return _finish(self.generator(input, *args, **kwargs))
 
     def generator(self, input, *args, **kwargs):
-        vacuum_path = VacuumPath(length=None)
-        vacuum_path.channel = self.channel
+        """Yields (field just after screen i, screen i) for every screen and
+        returns the field at the end of the path."""
+        import torch
         self.init_phase_screens()
-        for i, phase_screen in enumerate(self.phase_screens):
-            vacuum_path.length = self.positions[i] - self.positions[i - 1] if i > 0 else self.positions[0]
-            import torch
-            if hasattr(phase_screen, "generate_with_phasor"):
-                screen, phasor = phase_screen.generate_with_phasor(*args, **kwargs)
+        vacuum = VacuumPath(length=None)
+        vacuum.channel = self.channel
+        steps, last = self.segments()
+        field = input
+        for dz, screen in steps:
+            if hasattr(screen, "generate_with_phasor"):
+                phi, phasor = screen.generate_with_phasor(*args, **kwargs)
             else:
-                screen = phase_screen.generate(*args, **kwargs)
-                phasor = torch.polar(torch.ones_like(screen), -screen)  # exp(-i phi), complex64
-            part_losses_db = self.losses_db * vacuum_path.length / self.length
-            field = _as_field(self.channel, vacuum_path.output(input))
-            input = self.append_losses(phasor * field, losses_db=part_losses_db)
-            yield input, screen
-        return vacuum_path.output(input, length=self.length - self.positions[-1])
+                phi = screen.generate(*args, **kwargs)
+                phasor = torch.polar(torch.ones_like(phi), -phi)
+            arrived = _as_field(self.channel, vacuum.output(field, length=dz))
+            field = self.append_losses(phasor * arrived, losses_db=self.losses_db * dz / self.length)
+            yield field, phi
+        return vacuum.output(field, length=last)
 
 
 class IdenticalPhaseScreensPath(PhaseScreensPath):
     def __init__(self, length, count, phase_screen, position_in_slab="middle", losses_db=0):
-        thickness = length / count
-        if position_in_slab == "before":
-            positions = np.arange(count) * thickness
-        elif position_in_slab == "middle":
-            positions = (np.arange(count) + 1 / 2) * thickness
-        elif position_in_slab == "after":
-            positions = (np.arange(count) + 1) * thickness
-        else:
-            raise ValueError("Available values for position_in_slab: 'before', 'middle' and 'after'")
-        phase_screen.thickness = thickness
-        phase_screens = [copy.copy(phase_screen) for _ in range(count)]
-        self.phase_screen = phase_screens[0]
-        super().__init__(length=length, phase_screens=phase_screens, positions=positions, losses_db=losses_db)
+        if position_in_slab not in _SLAB_OFFSET:
+            raise ValueError(f"position_in_slab must be one of {', '.join(_SLAB_OFFSET)}; got {position_in_slab!r}")
+        slab = length / count
+        phase_screen.thickness = slab
+        # one shallow copy per slab: the copies share the model and spectral grid
+        screens = [copy.copy(phase_screen) for _ in range(count)]
+        self.phase_screen = screens[0]
+        super().__init__(length=length, phase_screens=screens,
+                         positions=(np.arange(count) + _SLAB_OFFSET[position_in_slab]) * slab, losses_db=losses_db)

@@ -2,8 +2,6 @@
 each one's value sits in ``atm_run``'s per-realisation output."""
 from __future__ import annotations
 
-import functools
-
 from .. import measures as M
 from ..engine import _lib
 
@@ -14,7 +12,7 @@ _MOMENT = {M.mean_x: _lib.OUT_MEAN_X, M.mean_y: _lib.OUT_MEAN_Y, M.mean_x2: _lib
 def classify(channel, mtype, ops):
     """Returns a key describing the value, or None if not fusable."""
     from .beam import BeamResult
-    from .pdt import PDTResult, TrackedPDTResult
+    from .pdt import PDTResult, PupilStop, TrackedPDTResult
     if mtype == "atmosphere":
         if len(ops) == 1:
             op = ops[0]
@@ -29,18 +27,17 @@ def classify(channel, mtype, ops):
             if getattr(op, "__func__", None) is BeamResult.mean_x2_r:
                 return ("slot", _lib.OUT_MEAN_X2_R)
             return None
-        if len(ops) == 2 and ops[1] is M.eta and isinstance(ops[0], functools.partial):
-            owner = getattr(ops[0].func, "__self__", None)
-            if isinstance(owner, PDTResult) and getattr(ops[0].func, "__func__", None) is PDTResult.append_pupil \
-                    and not isinstance(owner, TrackedPDTResult):
+        if len(ops) == 2 and ops[1] is M.eta and isinstance(ops[0], PupilStop):
+            owner = ops[0].result
+            if isinstance(owner, PDTResult) and not isinstance(owner, TrackedPDTResult):
                 sx, sy = owner.pupil_shift
-                return ("pupil", (float(ops[0].args[0].radius), float(sx), float(sy)))
+                return ("pupil", (float(ops[0].pupil.radius), float(sx), float(sy)))
             return None
-        if len(ops) == 3 and ops[2] is M.eta and isinstance(ops[1], functools.partial):
+        if len(ops) == 3 and ops[2] is M.eta and isinstance(ops[1], PupilStop):
             owner = getattr(ops[0], "__self__", None)
-            if isinstance(owner, TrackedPDTResult) and \
+            if isinstance(owner, TrackedPDTResult) and owner is ops[1].result and \
                     getattr(ops[0], "__func__", None) is TrackedPDTResult.set_pupil_position:
-                return ("tracked", (float(ops[1].args[0].radius),))
+                return ("tracked", (float(ops[1].pupil.radius),))
         return None
     if mtype == "pupil" and len(ops) == 1 and ops[0] is M.eta and channel.pupil is not None:
         return ("pupil", (float(channel.pupil.radius), 0.0, 0.0))
@@ -96,3 +93,64 @@ def resolve(kind, out, pupils, tracked, n_screens=0):
     if kind[0] == "tracked":
         return out[:, _lib.OUT_PUPIL0 + len(pupils) + tracked.index(kind[1][0])]
     raise KeyError(kind)
+
+
+def run_batched(plans, batch: int) -> int:
+    """One batch of realisations of every channel through the fused engine.
+
+    plans: {channel: [(measure, kind from classify, time tuple or None)]}.
+    Spectra are drawn realisation by realisation, channel by channel, screen
+    by screen (the per-realisation loop's order); one draw serves every time
+    value of a realisation (the wind cache), and the screens move by (0, t)
+    for time value t.  Appends each measure's values and returns the number
+    of realisations run."""
+    import numpy as np
+    from ..engine.runner import draw_channel_spectra, get_plan, to_device
+    live = [m for ms in plans.values() for m, _, _ in ms if not m.is_done]
+    wanted = [m.max_size - len(m) for m in live if m.max_size is not None]
+    R = max(1, min(batch, max(wanted) if wanted else batch))
+    chans = list(plans)
+    for c in chans:
+        c.path.init_phase_screens()
+    draws = {c: [] for c in chans}
+    for _ in range(R):
+        for c in chans:
+            draws[c].append(draw_channel_spectra(c, 1, wind=True, clear=True))
+    for c, entries in plans.items():
+        spectra = [np.concatenate([d[k] for d in draws[c]]) for k in range(3)]
+        pupils = sorted({k[1] for _, k, _ in entries if k[0] == "pupil"})
+        tracked = sorted({k[1][0] for _, k, _ in entries if k[0] == "tracked"})
+        steps = any(k[0].startswith("step") for _, k, _ in entries)
+        plan = get_plan(c, batch=batch, pupils=pupils, tracked=tracked, path_output_loss=False,
+                        step_measures=steps)
+        dev = to_device(*spectra)
+        shifts = sorted({float(t or 0) for _, _, T in entries for t in (T or (0,))})
+        want_sf = any(k[0] == "screen_sf" for _, k, _ in entries)
+        outs, sfs = {}, {}
+        try:
+            for t in shifts:
+                plan.set_shift((0.0, t))
+                outs[t] = plan.run(*dev).cpu().numpy()
+                if want_sf:
+                    import torch
+                    from ..engine.plan import structure_function
+                    phi = torch.empty((R, plan.N, plan.N), dtype=torch.float32, device=plan.device)
+                    plan.screen(*dev, 0, phi_out=phi)
+                    sfs[t] = structure_function(phi).cpu().numpy()
+            plan.check()
+        finally:
+            plan.set_shift((0.0, 0.0))
+
+        def values(kind, t):
+            return sfs[t] if kind[0] == "screen_sf" else resolve(kind, outs[t], pupils, tracked, plan.n_screens)
+
+        for m, kind, T in entries:
+            per_t = [values(kind, float(t or 0)) for t in (T or (0,))]
+            for r in range(R):
+                if m.is_done:
+                    break
+                row = per_t[0][r] if T is None else [v[r] for v in per_t]
+                val = np.asarray(row, dtype=float).tolist()
+                m.data.append(val)
+                m.iteration_data = val
+    return R

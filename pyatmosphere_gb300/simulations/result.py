@@ -1,10 +1,16 @@
-"""Result base class (simulations/result.py:5-43).  The CSV format is the
-reference's (one column per measure, header = measure names, values
-'{:.3e}', shorter columns padded with empty cells) written without pandas."""
+"""Result: a named set of measures with CSV persistence (the reference's
+simulations/result.py:5-43 offers the same base class).
+
+The CSV file has the reference's layout -- one column per measure, the
+measure names as the header, values written with '{:.3e}', shorter columns
+padded with empty cells -- written and read with the csv module instead of
+pandas.  A result whose save_path exists when it is built resumes from it.
+"""
 from __future__ import annotations
 
 import csv
 import math
+import os
 
 import numpy as np
 
@@ -15,28 +21,29 @@ class Result:
     def __init__(self, channel, measures, max_size=None, save_path: str = ""):
         self.channel = channel
         self.measures = measures
-        self.set_max_size(max_size)
         self.save_path = save_path
-        if self.save_path:
-            try:
-                self.load_output()
-                print(f"Loaded measures from {self.save_path}")
-            except FileNotFoundError:
-                pass
+        self.set_max_size(max_size)
+        if save_path and os.path.exists(save_path):
+            self.load_output()
+            rows = max((len(m) for m in self.measures), default=0)
+            print(f"{type(self).__name__}: resumed {rows} realisations from {save_path}")
 
     def set_max_size(self, max_size):
-        for measures in self.measures:
-            measures.max_size = max_size
+        """Realisations each measure collects before it is done (None: no limit)."""
+        for m in self.measures:
+            m.max_size = max_size
 
     def print_output(self):
-        print(f"Len of the first measures: {len(self.measures[0])}")
+        counts = ", ".join(f"{m.name or i}: {len(m)}" for i, m in enumerate(self.measures))
+        print(f"{type(self).__name__} realisations per measure -- {counts}")
 
     def plot_output(self):
         self.print_output()
 
-    def _format(self, v):
+    # ---- CSV ------------------------------------------------------------------
+    def _cell(self, v):
         if isinstance(v, (list, tuple, np.ndarray)):
-            return str(list(np.asarray(v).tolist()))
+            return str(np.asarray(v).tolist())
         if v is None or (isinstance(v, float) and math.isnan(v)):
             return ""
         return self.save_float_format(v)
@@ -44,24 +51,19 @@ class Result:
     def save_output(self):
         if not self.save_path:
             return
-        cols = [m.data for m in self.measures]
-        n = max((len(c) for c in cols), default=0)
+        columns = [m.data for m in self.measures]
+        depth = max((len(c) for c in columns), default=0)
         with open(self.save_path, "w", newline="") as f:
-            w = csv.writer(f)
-            w.writerow([m.name for m in self.measures])
-            for i in range(n):
-                w.writerow([self._format(c[i]) if i < len(c) else "" for c in cols])
+            out = csv.writer(f)
+            out.writerow([m.name for m in self.measures])
+            out.writerows([[self._cell(c[i]) if i < len(c) else "" for c in columns] for i in range(depth)])
 
-    @staticmethod
-    def _parse(cell):
-        return float(cell) if cell.strip() != "" else float("nan")
-
-    def _read_columns(self):
+    def csv_columns(self):
+        """The saved file's cells, one list per measure (header dropped)."""
         with open(self.save_path, newline="") as f:
-            rows = list(csv.reader(f))
-        body = rows[1:]
-        return [[r[j] if j < len(r) else "" for r in body] for j in range(len(self.measures))]
+            body = list(csv.reader(f))[1:]
+        return [[row[j] if j < len(row) else "" for row in body] for j in range(len(self.measures))]
 
     def load_output(self):
-        for measures, col in zip(self.measures, self._read_columns()):
-            measures.data = [self._parse(c) for c in col]
+        for m, cells in zip(self.measures, self.csv_columns()):
+            m.data = [float(c) if c.strip() else float("nan") for c in cells]

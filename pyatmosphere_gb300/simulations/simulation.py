@@ -1,18 +1,31 @@
-"""Monte-Carlo driver (simulations/simulation.py:7-152).
+"""Monte-Carlo driver on the GB300 engine (the reference's
+simulations/simulation.py:7-152 offers the same class and methods).
 
-``Simulation.iter`` keeps the reference's per-realisation semantics
-(channel -> time -> measure type -> operation chain).  ``Simulation.run``
-first tries the batched engine path: when every measure of every channel is
-one the engine computes in its fused reductions (Beam moments, mean_x2_r,
-eta through fixed or centroid-tracked CirclePupils, total eta, and the same
-quantities after every screen for "propagation" measures such as SIResult
-and BeamPropagationResult), it runs ``gpu.config['batch']`` realisations per
-engine call, once per time shift of the wind measures, and appends their
-scalars; otherwise it falls back to ``iter`` (engine propagation, one
-realisation at a time).  Spectra are drawn from numpy's global RNG in the
-same order as the reference (realisation by realisation, channel by
-channel, screen by screen), so a seeded run reproduces the reference's
-realisations.
+Measures are grouped by (channel, time list, measure type, operation
+chain); a group's chain runs once per value it is offered and its result
+goes to every measure of the group.  Per realisation, a channel offers, in
+this order and once per time value t of the group (screens shifted by
+(0, t), one spectrum draw serving every t):
+
+    "propagation" i   the field just after screen i   (and "phase_screen":
+                      the first screen, when i = 0)
+    "atmosphere"      the receiver field
+    "propagation" -1  the receiver field
+    "pupil"           the receiver field behind the channel's pupil
+
+Groups see the values in the order they were added, so a chain that reads
+another measure's value of this realisation (BeamResult.mean_x2_r,
+TrackedPDTResult.set_pupil_position) finds it.
+
+``run`` first tries the batched engine path: when every measure is one the
+engine's fused reductions produce (beam moments, mean_x2_r, eta through fixed
+or centroid-tracked circular pupils, total eta, the per-screen values of
+"propagation" measures, the first screen's structure function), it runs
+``gpu.config['batch']`` realisations per engine call, once per time value,
+with spectra drawn from numpy's global generator in the per-realisation
+order (realisation, channel, screen).  Otherwise it runs ``iter`` (engine
+propagation, one realisation at a time).  Either way a seeded run gives the
+reference's realisations.
 """
 from __future__ import annotations
 
@@ -23,91 +36,118 @@ from .measure import Measure
 from .result import Result
 
 
+def _blank(measure):
+    """Empty per-realisation value of a measure: one slot per time value and,
+    for "propagation" measures, one per screen plus the receiver."""
+    steps = len(measure.channel.path.positions) + 1 if measure.measure_type == "propagation" else None
+
+    def one():
+        return [None] * steps if steps else None
+
+    return [one() for _ in measure.time] if measure.time else one()
+
+
+def _store(measure, value, time_id, step):
+    if measure.time is None and step is None:
+        measure.iteration_data = value
+        return
+    slot = measure.iteration_data
+    if measure.time is not None:
+        if step is None:
+            slot[time_id] = value
+            return
+        slot = slot[time_id]
+    slot[step] = value
+
+
+def _copy(value):
+    return value.clone() if hasattr(value, "clone") else value.copy() if hasattr(value, "copy") else value
+
+
 class Simulation:
     def __init__(self, results_list: Sequence[Result] = None, measures_list: Sequence[Measure] = None):
-        self.measures = {}
-        if measures_list:
-            for measures in measures_list:
-                self.add_measures(measures)
-        self.results_list = results_list or []
+        self._groups: dict = {}  # (channel, time, measure_type, operations) -> [Measure]
+        for m in measures_list or ():
+            self.add_measures(m)
+        self.results_list = list(results_list or ())
         for result in self.results_list:
-            for measures in result.measures:
-                self.add_measures(measures)
+            for m in result.measures:
+                self.add_measures(m)
 
     def add_measures(self, measures):
-        """channel - time - measure_type - operations"""
-        d = self.measures.setdefault(measures.channel, {})
-        d = d.setdefault(measures.time, {})
-        d = d.setdefault(measures.measure_type, {})
-        d.setdefault(measures.operations, []).append(measures)
+        key = (measures.channel, measures.time, measures.measure_type, measures.operations)
+        self._groups.setdefault(key, []).append(measures)
 
-    def init_measures_iteration_data(self):
-        for measures in self.flattened_measures():
-            empty = None
-            if measures.time:
-                if measures.measure_type == "propagation":
-                    empty = [[None for _ in range(len(measures.channel.path.positions) + 1)] for _ in measures.time]
-                else:
-                    empty = [None for _ in measures.time]
-            elif measures.measure_type == "propagation":
-                empty = [None for _ in range(len(measures.channel.path.positions) + 1)]
-            measures.iteration_data = empty
-
-    def process_operations(self, output, operations_measures, time_id, propagation_id=None):
-        for operations, measures_list in operations_measures.items():
-            if self.is_measures_done(measures_list):
-                continue
-            measures = measures_list[0]
-            out = output.clone() if hasattr(output, "clone") else output.copy()
-            for operation in operations:
-                out = operation(measures.channel, output=out)
-            for measures in measures_list:
-                if measures.is_done:
-                    continue
-                if measures.time is not None:
-                    if propagation_id is not None:
-                        measures.iteration_data[time_id][propagation_id] = out
-                    else:
-                        measures.iteration_data[time_id] = out
-                else:
-                    if propagation_id is not None:
-                        measures.iteration_data[propagation_id] = out
-                    else:
-                        measures.iteration_data = out
-
-    def iter(self):
-        self.init_measures_iteration_data()
-        for channel, channel_measures in self.measures.items():
-            for ps in channel.path.phase_screens:
-                ps.cache_clear()
-            for time, time_measures in channel_measures.items():
-                time = time or [None]
-                for time_id, time_value in enumerate(time):
-                    for propagation_id, (propagation_result, phase_screen) in enumerate(
-                            channel.generator(pupil=False, shift=(0, time_value or 0), store_output=True, wind=True)):
-                        self.process_operations(propagation_result, time_measures.get("propagation", {}), time_id,
-                                                propagation_id)
-                        if propagation_id == 0:
-                            self.process_operations(phase_screen, time_measures.get("phase_screen", {}), time_id)
-                    self.process_operations(channel.output, time_measures.get("atmosphere", {}), time_id)
-                    self.process_operations(channel.output, time_measures.get("propagation", {}), time_id, -1)
-                    if channel.pupil:
-                        self.process_operations(channel.pupil.output(channel.output), time_measures.get("pupil", {}),
-                                                time_id)
-        for measures in self.flattened_measures():
-            if not measures.is_done:
-                measures.data.append(measures.iteration_data)
+    @property
+    def measures(self):
+        """The groups as nested dicts: channel -> time -> measure type -> operations -> [Measure]."""
+        tree = {}
+        for (channel, time, mtype, ops), ms in self._groups.items():
+            tree.setdefault(channel, {}).setdefault(time, {}).setdefault(mtype, {})[ops] = ms
+        return tree
 
     def flattened_measures(self, measures=None):
-        measures = measures if measures is not None else self.measures
-        if isinstance(measures, dict):
-            for values in measures.values():
-                yield from self.flattened_measures(values)
+        if measures is None:
+            for ms in self._groups.values():
+                yield from ms
+        elif isinstance(measures, dict):
+            for v in measures.values():
+                yield from self.flattened_measures(v)
         else:
             yield from measures
 
     def is_measures_done(self, measures=None):
         return all(m.is_done for m in self.flattened_measures(measures))
+
+    # ------------------------------------------------------------------
+    # one realisation at a time
+    # ------------------------------------------------------------------
+    @staticmethod
+    def _offers(channel, time_value):
+        """(measure type, step, value) in the order one realisation offers them."""
+        walk = channel.generator(pupil=False, shift=(0, time_value or 0), store_output=True, wind=True)
+        for i, (field, screen) in enumerate(walk):
+            yield "propagation", i, field
+            if i == 0:
+                yield "phase_screen", None, screen
+        yield "atmosphere", None, channel.output
+        yield "propagation", -1, channel.output
+        if channel.pupil:
+            yield "pupil", None, channel.pupil.output(channel.output)
+
+    def process_operations(self, output, operations_measures, time_id, propagation_id=None):
+        """Runs each group's chain on `output` and stores the result in its
+        measures (operations_measures: {operations: [Measure]})."""
+        for ops, group in operations_measures.items():
+            if self.is_measures_done(group):
+                continue
+            value = _copy(output)
+            for op in ops:
+                value = op(group[0].channel, output=value)
+            for m in group:
+                if not m.is_done:
+                    _store(m, value, time_id, propagation_id)
+
+    def iter(self):
+        for m in self.flattened_measures():
+            m.iteration_data = _blank(m)
+        channels = list(dict.fromkeys(key[0] for key in self._groups))
+        for channel in channels:
+            for screen in getattr(channel.path, "phase_screens", ()):
+                screen.cache_clear()  # a new spectrum per realisation
+            times = list(dict.fromkeys(key[1] for key in self._groups if key[0] is channel))
+            for time in times:
+                by_type = {}
+                for (c, t, mtype, ops), group in self._groups.items():
+                    if c is channel and t == time:
+                        by_type.setdefault(mtype, {})[ops] = group
+                for time_id, t in enumerate(time or [None]):
+                    for mtype, step, value in self._offers(channel, t):
+                        if mtype in by_type:
+                            self.process_operations(value, by_type[mtype], time_id, step)
+        for m in self.flattened_measures():
+            if not m.is_done:
+                m.data.append(m.iteration_data)
 
     # ------------------------------------------------------------------
     # batched engine path
@@ -117,109 +157,53 @@ class Simulation:
         some measure is outside what the engine fuses."""
         from .fused import classify
         plans = {}
-        for channel, by_time in self.measures.items():
+        for (channel, time, mtype, ops), group in self._groups.items():
             if not getattr(channel, "_fused_ok", lambda: False)():
                 return None
-            entries = []
-            for time, by_type in by_time.items():
-                for mtype, by_ops in by_type.items():
-                    for ops, ms in by_ops.items():
-                        kind = classify(channel, mtype, ops)
-                        if kind is None:
-                            return None
-                        entries += [(m, kind, time) for m in ms]
-            plans[channel] = entries
+            kind = classify(channel, mtype, ops)
+            if kind is None:
+                return None
+            plans.setdefault(channel, []).extend((m, kind, time) for m in group)
         return plans
 
     def _batched_iter(self, plans):
-        import numpy as np
-        from ..engine.runner import draw_channel_spectra, get_plan, to_device
-        from .fused import resolve
-        batch = int(gpu.config.get("batch", 256))
-        live = [m for ms in plans.values() for m, _, _ in ms if not m.is_done]
-        sized = [m.max_size - len(m) for m in live if m.max_size is not None]
-        R = max(1, min(batch, max(sized) if sized else batch))
-        chans = list(plans)
-        for c in chans:
-            c.path.init_phase_screens()
-        # reference RNG order: realisation, then channel, then screen; one
-        # spectrum per realisation serves every time shift (wind cache)
-        per = {c: [] for c in chans}
-        for _ in range(R):
-            for c in chans:
-                per[c].append(draw_channel_spectra(c, 1, wind=True, clear=True))
-        for c, entries in plans.items():
-            spectra = [np.concatenate([p[k] for p in per[c]]) for k in range(3)]
-            pupils = sorted({k[1] for _, k, _ in entries if k[0] == "pupil"})
-            tracked = sorted({k[1][0] for _, k, _ in entries if k[0] == "tracked"})
-            steps = any(k[0].startswith("step") for _, k, _ in entries)
-            plan = get_plan(c, batch=batch, pupils=pupils, tracked=tracked, path_output_loss=False,
-                            step_measures=steps)
-            dev = to_device(*spectra)
-            # screens move by (0, t) for each time value (Simulation.iter's shift=(0, time))
-            shifts = sorted({float(t or 0) for _, _, T in entries for t in (T or (0,))})
-            outs, sfs = {}, {}
-            want_sf = any(k[0] == "screen_sf" for _, k, _ in entries)
-            try:
-                for t in shifts:
-                    plan.set_shift((0.0, t))
-                    outs[t] = plan.run(*dev).cpu().numpy()
-                    if want_sf:
-                        import torch
-                        from ..engine.plan import structure_function
-                        phi = torch.empty((R, plan.N, plan.N), dtype=torch.float32, device=plan.device)
-                        plan.screen(*dev, 0, phi_out=phi)
-                        sfs[t] = structure_function(phi).cpu().numpy()
-            finally:
-                plan.set_shift((0.0, 0.0))
-            n = plan.n_screens
-            def values(kind, t):
-                if kind[0] == "screen_sf":
-                    return sfs[t]
-                return resolve(kind, outs[t], pupils, tracked, n)
+        from .fused import run_batched
+        return run_batched(plans, int(gpu.config.get("batch", 256)))
 
-            for m, kind, T in entries:
-                if T is None:
-                    vals = values(kind, 0.0)
-                    rows = [vals[r] for r in range(R)]
-                else:
-                    vs = [values(kind, float(t or 0)) for t in T]
-                    rows = [[v[r] for v in vs] for r in range(R)]
-                for r in range(R):
-                    if m.is_done:
-                        break
-                    val = np.asarray(rows[r], dtype=float).tolist()
-                    m.data.append(val)
-                    m.iteration_data = val
-        return R
-
+    # ------------------------------------------------------------------
     def run(self, *args, plot_step: int = None, save_step: int = None, **kwargs):
+        """Realisations until every measure has max_size values; an interrupt
+        (Ctrl-C) stops early, keeping what was measured, and the final
+        process_output saves it."""
+        done = 0
         try:
-            iteration = 0
-            plans = self._batch_plan()
+            batched = self._batch_plan()
             while not self.is_measures_done():
-                if plans is not None:
-                    n = self._batched_iter(plans)
+                if batched is not None:
+                    n = self._batched_iter(batched)
                 else:
                     self.iter()
                     n = 1
-                for it in range(iteration + 1, iteration + n + 1):
+                for it in range(done + 1, done + n + 1):
                     self.process_output(it, plot_step=plot_step, save_step=save_step)
-                iteration += n
+                done += n
         except KeyboardInterrupt:
             pass
         finally:
             self.process_output(0, plot_step=plot_step, save_step=save_step)
 
     def process_output(self, iteration, plot_step, save_step):
-        if plot_step and iteration % plot_step == 0:
+        """Plots every plot_step-th and saves every save_step-th iteration
+        (iteration 0: the end of the run)."""
+        if plot_step and not iteration % plot_step:
             for result in self.results_list:
                 result.plot_output()
             try:
-                from IPython import display
-                display.clear_output(wait=True)
-            except ModuleNotFoundError:
-                pass
-        if save_step and iteration % save_step == 0:
+                from IPython.display import clear_output
+            except ImportError:
+                clear_output = None
+            if clear_output is not None:
+                clear_output(wait=True)
+        if save_step and not iteration % save_step:
             for result in self.results_list:
                 result.save_output()

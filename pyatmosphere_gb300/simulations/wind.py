@@ -12,7 +12,7 @@ from .result import Result
 
 class WindResult(Result):
     def load_output(self):
-        for measures, col in zip(self.measures, self._read_columns()):
+        for measures, col in zip(self.measures, self.csv_columns()):
             measures.data = [[float(v) for v in c[1:-1].split(", ")] for c in col if c.strip()]
 
 

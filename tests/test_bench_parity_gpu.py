@@ -1,0 +1,144 @@
+"""Parity on exactly what bench.py times, and the paired PDT check.
+
+Config 2, the bench's workload (2048^2, delta 1.5 mm, 808 nm, w0 0.12 m,
+50 km, 5 SS screens x 1024 annuli, MVK Cn2 5e-16, pupil 0.2 m), with the
+bench's seeded host spectra (seed 2024, realisations 0..255) and its plan:
+B = 256, default flags (tensor-core TMA GEMM with the 1-D phase fold).  The
+launch forms that atm_autotune can pick are pinned with set_variants, one
+parametrised case each: the row-major forms (row 4, column tile 4, column 3
+or 4) and the tiled forms (row 5 or 6, column 5 or 6).  For each:
+  * 16 realisations against the complex128 oracle: field rel-L2 <= 1e-4 each
+    (field_out of a B = 16 plan with the same forms), eta and the second
+    moments to 1e-5 relative, the centroids and mean_xy to 1e-5 of their
+    natural scale (sqrt(mean_x2 eta), sqrt(mean_x2 mean_y2));
+  * B = 1, B = 16 and B = 256 give the same bits for the same realisations.
+References: phase_screens.py:108-136, pathes.py:61-75, measures.py:1-38.
+
+Config 1 (512^2, delta 2 mm, w0 0.09 m, 10 km, 5 screens, Cn2 1e-15,
+pupil 0.12 m): 200 realisations through the engine and through the oracle in
+FP64 and in the reference's own precision (which reproduces the reference's
+outputs), paired by their injected spectra.  The two-sample KS statistic of
+the per-realisation transmittance (PDTResult, simulations/pdt.py:11-26) and of
+the centroids must be <= 0.01."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import atm_oracle as o
+from oracle.parallel import simulate_parallel
+
+pytestmark = pytest.mark.gpu
+
+BENCH_SEED = 2024
+FORMS = [("row-major", 0, (4, 4, 4)), ("row-major", 0, (4, 4, 3)), ("tiled", 64, (5, 4, 6)),
+         ("tiled", 64, (6, 4, 6)), ("tiled", 64, (6, 4, 5))]
+
+
+def _bench_spec():
+    import bench
+    w = bench.WORKLOAD
+    return o.ChannelSpec(N=w["N"], delta=w["delta"], wvl=w["wvl"], w0=w["w0"], F0=w["F0"], length=w["length"],
+                         count=w["count"], Cn2=w["Cn2"], l0=w["l0"], L0=w["L0"], points=w["points"],
+                         f_min=w["f_min"], f_max=w["f_max"], pupil_radius=w["pupil_radius"])
+
+
+@pytest.fixture(scope="module")
+def bench_case():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    import bench
+    from pyatmosphere_gb300.engine.spectra import draw_spectra
+    base, psd = bench.base_and_psd()
+    spec = _bench_spec()
+    rho, theta, value = draw_spectra(BENCH_SEED, range(256), spec.count, base, psd)
+    meas, fields = simulate_parallel(spec, rho[:16], theta[:16], value[:16], prec="fp64", return_fields=True)
+    return dict(spec=spec, base=base, pos=bench.positions(spec.length, spec.count), spectra=(rho, theta, value),
+                oracle=meas, fields=fields)
+
+
+def _plan(case, B, flags, variants):
+    from pyatmosphere_gb300.engine import EnginePlan
+    s = case["spec"]
+    p = EnginePlan(s.N, s.delta, s.wvl, s.w0, s.F0, case["pos"], s.length, f_base=case["base"],
+                   pupils=[(s.pupil_radius,)], batch=B, flags=flags)
+    p.set_variants(*variants)
+    assert p.info["gemm_form"] == 3, "the bench's GEMM: persistent TMA tensor-core form"
+    return p
+
+
+@pytest.mark.parametrize("name,flags,variants", FORMS, ids=[f"{f[0]}-{f[2]}" for f in FORMS])
+def test_bench_plan_matches_fp64_oracle_and_is_batch_independent(bench_case, name, flags, variants):
+    import torch
+    rho, theta, value = bench_case["spectra"]
+    dev = [torch.from_numpy(a).cuda() for a in (rho, theta, value)]
+    N = bench_case["spec"].N
+    # B = 256: the bench's own launch
+    p256 = _plan(bench_case, 256, flags, variants)
+    m256 = p256.run(*dev).cpu().numpy()
+    p256.check()
+    p256.close()
+    # B = 16 with the final fields
+    p16 = _plan(bench_case, 16, flags, variants)
+    f16 = torch.empty((16, N, N), dtype=torch.complex64, device="cuda")
+    m16 = p16.run(*[t[:16].contiguous() for t in dev], field_out=f16).cpu().numpy()
+    p16.check()
+    p16.close()
+    f16 = f16.cpu().numpy()
+    # B = 1
+    p1 = _plan(bench_case, 1, flags, variants)
+    m1 = p1.run(*[t[:1].contiguous() for t in dev]).cpu().numpy()
+    p1.close()
+    np.testing.assert_array_equal(m16, m256[:16])
+    np.testing.assert_array_equal(m1, m256[:1])
+
+    worst = {"field": 0.0}
+    for b in range(16):
+        ref = bench_case["oracle"][b]
+        err = o.rel_l2(f16[b], bench_case["fields"][b])
+        worst["field"] = max(worst["field"], err)
+        assert err <= 1e-4, f"realisation {b}: field rel-L2 {err:.3e}"
+        got = dict(eta_total=m16[b, 0], mean_x=m16[b, 1], mean_y=m16[b, 2], mean_x2=m16[b, 3], mean_xy=m16[b, 4],
+                   mean_y2=m16[b, 5], eta_0=m16[b, 8])
+        scale = {"mean_x": math.sqrt(ref["mean_x2"] * ref["eta_total"]),
+                 "mean_y": math.sqrt(ref["mean_y2"] * ref["eta_total"]),
+                 "mean_xy": math.sqrt(ref["mean_x2"] * ref["mean_y2"])}
+        for k, v in got.items():
+            err = abs(v - ref[k]) / (scale[k] if k in scale else abs(ref[k]))
+            worst[k] = max(worst.get(k, 0.0), err)
+            assert err <= 1e-5, f"realisation {b}: {k} {v!r} vs {ref[k]!r} ({err:.2e})"
+    print(f"\n{name} {variants}: worst over 16 realisations " + ", ".join(f"{k} {v:.2e}" for k, v in worst.items()))
+
+
+def _ks(a, b):
+    a, b = np.sort(a), np.sort(b)
+    x = np.concatenate([a, b])
+    return float(np.max(np.abs(np.searchsorted(a, x, side="right") / len(a) -
+                               np.searchsorted(b, x, side="right") / len(b))))
+
+
+def test_config1_paired_pdt_ks():
+    import torch
+    from pyatmosphere_gb300.engine import EnginePlan
+    from pyatmosphere_gb300.engine.spectra import draw_spectra
+    assert torch.cuda.is_available()
+    spec = o.ChannelSpec()  # config 1: 512^2, delta 2 mm, w0 0.09, 10 km, 5 screens, Cn2 1e-15, pupil 0.12 m
+    R = 200
+    base = o.logpolar_base(spec.points, spec.f_min, spec.f_max)
+    psd = o.annulus_psd(base, spec.k, spec.thickness, spec.Cn2, spec.l0, spec.L0, use_scipy=False)
+    rho, theta, value = draw_spectra(2021, range(R), spec.count, base, psd)
+    plan = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, o.screen_positions(spec.length, spec.count),
+                      spec.length, f_base=base, pupils=[(spec.pupil_radius,)], batch=R)
+    eng = plan.run(*[torch.from_numpy(a).cuda() for a in (rho, theta, value)]).cpu().numpy()
+    plan.check()
+    plan.close()
+    report = {}
+    for prec in ("fp64", "ref"):
+        ref = simulate_parallel(spec, rho, theta, value, prec=prec)
+        for k, slot in (("eta_0", 8), ("mean_x", 1), ("mean_y", 2)):
+            r = np.array([m[k] for m in ref])
+            ks = _ks(eng[:, slot], r)
+            report[f"{prec}:{k}"] = (ks, float(np.abs(eng[:, slot] - r).max()))
+            assert ks <= 0.01, f"paired KS of {k} vs the {prec} oracle: {ks}"
+    print("\nconfig 1, 200 paired realisations (KS, max |diff|): " +
+          ", ".join(f"{k} ({v[0]:.3f}, {v[1]:.1e})" for k, v in report.items()))

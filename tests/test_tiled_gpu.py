@@ -62,13 +62,13 @@ def test_tiled_run_equals_row_major(torch_cuda, N):
     tl.close()
 
 
-@pytest.mark.parametrize("row_variant", [5, 6])
-def test_tiled_run_matches_oracle(torch_cuda, row_variant):
+@pytest.mark.parametrize("row_variant,col_variant", [(5, 5), (6, 5), (5, 6), (6, 6)])
+def test_tiled_run_matches_oracle(torch_cuda, row_variant, col_variant):
     torch = torch_cuda
     spec = o.ChannelSpec(N=512, delta=2e-3, w0=0.09, length=10e3, count=5, points=1024, Cn2=1e-15,
                          pupil_radius=0.12)
     _, tl, base = _plans(spec, 2)
-    tl.set_variants(row_variant, 4, 5)
+    tl.set_variants(row_variant, 4, col_variant)
     rho, theta, value = _spectra(spec, base, 3, 2)
     dev = [torch.from_numpy(a).cuda() for a in (rho, theta, value)]
     field = torch.empty((2, 512, 512), dtype=torch.complex64, device="cuda")
@@ -96,7 +96,8 @@ def test_tiled_vacuum_and_measures(torch_cuda, N):
     rm.vacuum(a, 987.0)
     tl.vacuum(b, 987.0)
     assert torch.equal(a, b)
-    np.testing.assert_allclose(tl.measures(b).cpu().numpy(), rm.measures(a).cpu().numpy(), rtol=1e-12, atol=1e-18)
+    # different kernels reduce the moments (their FP32 per-thread sums may contract differently)
+    np.testing.assert_allclose(tl.measures(b).cpu().numpy(), rm.measures(a).cpu().numpy(), rtol=1e-6, atol=1e-15)
     tl.check()
 
 
@@ -116,7 +117,7 @@ def test_tiled_step_measures_and_tracked(torch_cuda):
     tl = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length,
                     flags=_lib.FLAG_STEP_MEASURES | _lib.FLAG_TILED, **kw)
     dev = [torch.from_numpy(a).cuda() for a in _spectra(spec, base, 5, R)]
-    np.testing.assert_array_equal(tl.run(*dev).cpu().numpy(), rm.run(*dev).cpu().numpy())
+    np.testing.assert_allclose(tl.run(*dev).cpu().numpy(), rm.run(*dev).cpu().numpy(), rtol=1e-6, atol=1e-15)
     tl.check()
 
 
@@ -124,5 +125,5 @@ def test_tiled_autotune_keeps_tiled_forms(torch_cuda):
     spec = o.ChannelSpec(N=2048, delta=1.5e-3, count=2, points=256, length=10e3)
     _, tl, _ = _plans(spec, 2)
     choice = tl.autotune(repeats=1)
-    assert choice["row_variant"] in (5, 6) and choice["col_variant"] == 5 and choice["col_tile"] == 4
+    assert choice["row_variant"] in (5, 6) and choice["col_variant"] in (5, 6) and choice["col_tile"] == 4
     assert tl.info["tiled"] == 1
