@@ -40,9 +40,10 @@ WORKLOAD_NAME = ("advanced channel: 2048^2 grid, delta 1.5 mm, 808 nm, w0 0.12 m
                  "5 SS screens x 1024 annuli, MVK Cn2 5e-16, pupil 0.2 m")
 
 
-# DRAM bytes (read + write) per launch and realisation, from one ncu capture
-# of a 16-realisation run of this workload (profiles/traffic_2048_b16.md),
-# averaged over the launches of one run; traffic grows with the realisations.
+# DRAM bytes (read + write) per launch and realisation of the row-major
+# forms, from one ncu capture of a 16-realisation run of this workload,
+# averaged over the launches of one run (traffic grows with the
+# realisations); a fixed figure, not measured by this script.
 TRAFFIC_PER_REALISATION = {"row_pass": 66.98e6, "col_pass": 63.49e6, "screen_gemm": 25.98e6,
                            "screen_table": 8.24e6}
 
@@ -402,7 +403,27 @@ def run_gb300(args, rank, world, local_rank):
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-    prof = plan.profile_end()
+    kernels_timed = "cuda events inside the timed region" + (" (external event nodes of the graphs)" if graphs else "")
+    try:
+        prof = plan.profile_end()
+    except _lib.EngineError:
+        prof = None
+    plan.check()
+    # the same steps as direct launches: their time beside the graphs', and the
+    # per-kernel events if the graph replays could not record them
+    plan.profile_begin(launches + 8)
+    e6, e7 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e6.record(stream)
+    for s in range(args.warmup, n_steps):
+        plan.run(*devin[s], out=out[s])
+    e7.record(stream)
+    torch.cuda.synchronize()
+    direct_prof = plan.profile_end()
+    direct_ms = e6.elapsed_time(e7) / args.steps
+    if prof is None:
+        prof = direct_prof
+        kernels_timed = "cuda events in a direct-launch pass of the same steps right after the graph-timed region"
     plan.check()
     ms = e0.elapsed_time(e1)
     t_max = torch.tensor([ms], dtype=torch.float64, device=dev)
@@ -465,8 +486,9 @@ def run_gb300(args, rank, world, local_rank):
         "col_pass": ("hbm", 16.0 * N * N * B, "GB/s"),
         # n+1 row launches move 8 (write) + 4 (phi) + (n-1)(16 + 4) + 8 (read) bytes per pixel
         "row_pass": ("hbm", (12.0 + 20.0 * (n - 1) + 8.0) / (n + 1) * N * N * B, "GB/s"),
-        # high-frequency columns of A and B: FP16 hi + lo (tensor cores) or FP32 (SIMT)
-        "screen_table": ("hbm", (4 * 2.0 if tc else 2 * 4.0) * 2 * (w["points"] - plan.info["low_annuli"]) * N * B, "GB/s"),
+        # the high-frequency columns of A and B (FP16 hi + lo) are written once and the GEMM reads
+        # them back while they are still in L2: the DRAM bytes of the capture, not the table size
+        "screen_table": ("hbm", TRAFFIC_PER_REALISATION["screen_table"] * B, "GB/s"),
     }
     peaks = {}
     try:
@@ -501,7 +523,8 @@ def run_gb300(args, rank, world, local_rank):
         e = kernels[k]
         t = TRAFFIC_PER_REALISATION.get(k)
         return {"kernel": k, "bound": e["bound"], "achieved": e["achieved"], "peak": e["peak"], "unit": e["unit"],
-                "frac": e["frac"], "traffic": t * B if t else None, "traffic_unit": "bytes per launch",
+                "frac": e["frac"], "traffic": t * B if t else None,
+                "traffic_unit": "bytes per launch (ncu capture at B = 16, scaled per realisation)",
                 "peak_source": e["peak_source"]}
 
     info = dict(plan.info)
@@ -537,6 +560,7 @@ def run_gb300(args, rank, world, local_rank):
             "data": "synthetic (seeded spectra, reference formulas)",
             "config": {"workload": "2048^2 advanced channel, 50 km, 5 SS screens x 1024", "batch": B,
                        "realisations_per_step": B, "timed_as": "cuda graph replay" if graphs else "direct launches",
+                       "direct_ms_per_step": round(direct_ms, 3), "kernels_timed": kernels_timed,
                        "l2": "inputs > L2 (8.6 GB field batch)", "gemm_k": K,
                        "layout": "tiled" if info.get("tiled") else "row-major", "autotune": tuned,
                        "gemm": ["simt", "tc cp.async", "tc tma 128x128", "tc tma 128x256"][info["gemm_form"]]},

@@ -347,8 +347,9 @@ int atm_set_wait_budget(uint64_t ns);
  * loads the library, so N must be a power of two in [128, 4096] (larger N:
  * ATM_ERR_UNSUPPORTED).  The first call on a device looks up that array's
  * address (cudaGetSymbolAddress, once per device); make it before capturing
- * any stream.  All calls share the array: calls whose GPU work overlaps
- * (unordered streams) race on it. */
+ * any stream, and do not reset the device while the library is loaded (the
+ * address is kept for the life of the process).  All calls share the array:
+ * calls whose GPU work overlaps (unordered streams) race on it. */
 int atm_vacuum_noalloc(void* field, int32_t N, int32_t batch, double delta, double wvl, double dz,
                        void* stream);
 

@@ -587,21 +587,30 @@ int atm_plan_info(const AtmPlan* pl, AtmPlanInfo* info) {
 
 namespace {
 
-// brackets one launch with an event pair when the plan is profiling
+// brackets one launch with an event pair when the plan is profiling.  While
+// the stream is being captured into a CUDA graph the pair is recorded as
+// external event nodes, so that every replay of the graph records it.
 struct Prof {
   AtmPlan* pl;
   int kind;
   cudaStream_t st;
   int slot = -1;
+  static void record(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusActive)
+      cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else
+      cudaEventRecord(e, s);
+  }
   Prof(AtmPlan* p, int k, cudaStream_t s) : pl(p), kind(k), st(s) {
     if (pl->profiling && pl->ev_used < pl->ev_cap) {
       slot = pl->ev_used++;
       pl->ev_kind[slot] = kind;
-      cudaEventRecord(pl->ev[2 * slot], st);
+      record(pl->ev[2 * slot], st);
     }
   }
   ~Prof() {
-    if (slot >= 0) cudaEventRecord(pl->ev[2 * slot + 1], st);
+    if (slot >= 0) record(pl->ev[2 * slot + 1], st);
   }
 };
 

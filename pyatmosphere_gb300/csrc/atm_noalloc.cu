@@ -17,7 +17,10 @@
 //     process exits.
 //   * The first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before capturing any stream on the device.
+//     that first call before capturing any stream on the device.  The address
+//     is kept for the life of the process: do not reset the device
+//     (cudaDeviceReset) while the library is loaded, since the array may be
+//     placed elsewhere in the new context.
 //   * All calls share the one array.  Each call rewrites every table entry it
 //     reads before reading it, so nothing carries over between calls, but
 //     calls whose GPU work overlaps (different streams, no ordering) race on

