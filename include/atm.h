@@ -126,7 +126,9 @@ typedef struct AtmPlanInfo {
                                  3: as 2 with rows loaded by bulk copies (TMA),
                                  4: as 3 with twiddles formed from powers of two,
                                  5: tiled layout, four rows per CTA with a named barrier per row,
-                                 6: as 5 with twiddles formed from powers of two */
+                                 6: as 5 with twiddles formed from powers of two,
+                                 7: as 4 with each thread's twiddle bases held in registers,
+                                 8: as 6 with each thread's twiddle bases held in registers */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile,
                                  2: persistent pipelined with twiddles formed from powers of two,
                                  3: persistent with tiles loaded by TMA (loads overlap the FFTs),
@@ -135,7 +137,10 @@ typedef struct AtmPlanInfo {
                                  5: as 4 on the tiled layout (block columns of 4 columns),
                                  6: tiled layout, each column of a block column transformed by its own
                                     warps with their own named barrier; a producer warp loads and stores
-                                    the block columns with TMA */
+                                    the block columns with TMA,
+                                 7: as 4 with each thread's twiddle bases held in registers (the
+                                    product-twiddle arithmetic of 2),
+                                 8: as 6 with each thread's twiddle bases held in registers */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
                                  form with 128 x 128 tiles (ATM_FLAG_TC_N128), 3 the same with 128 x 256
@@ -265,11 +270,12 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
 
 /* Times the launch variants of the FFT passes on this plan's own workspace
  * (`batch` realisations, `repeats` timed launches each after one warm-up)
- * and keeps the fastest: row-pass variant (five forms), column tile
- * (2..16 columns, at most 512 threads per CTA) and column-pass variant
- * (four forms).  Every form but row variant 4 and column variant 2 computes
- * the same bits; those two form most twiddles as products of table values
- * and so round differently (FP32 round-off, well inside the 1e-4 field bound).  Overwrites the
+ * and keeps the fastest: row-pass variant (0..4 and 7; a tiled plan: 5, 6, 8),
+ * column tile (2..16 columns, at most 512 threads per CTA; a tiled plan: 4)
+ * and column-pass variant (0..4 and 7; a tiled plan: 5, 6, 8).  The forms
+ * that build twiddles as products of powers of two (row 4, 6, 7, 8; column
+ * 2, 7, 8) round differently from the table forms (FP32 round-off, well
+ * inside the 1e-4 field bound); the results are otherwise the same.  Overwrites the
  * plan's field / screen workspace (zeroes) and blocks until the timing
  * launches finish, so it is called outside CUDA-graph capture, before the
  * runs it tunes.  The reference has no tuner: cupy picks cuFFT plans inside
@@ -284,10 +290,12 @@ int atm_autotune(AtmPlan* plan, int32_t batch, int32_t repeats, void* stream);
  * calculate_structure_function (simulations/structure_function.py:11-12). */
 int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* sf_out, void* stream);
 
-/* Sets the launch choices atm_autotune makes (row-pass variant 0..4, column
- * tile 2/4/8/16 with at most 512 threads per CTA, column-pass variant 0..4)
- * by hand.  Results do not change, except for FP32 round-off with row
- * variant 4 and column variant 2.  No reference counterpart. */
+/* Sets the launch choices atm_autotune makes by hand: row-pass variant 0..4
+ * or 7, column tile 2/4/8/16 with at most 512 threads per CTA, column-pass
+ * variant 0..4 or 7; a tiled plan (ATM_FLAG_TILED) takes row 5, 6 or 8,
+ * column tile 4 and column 5, 6 or 8.  Results do not change, except for
+ * FP32 round-off between the table-twiddle and product-twiddle forms.  No
+ * reference counterpart. */
 int atm_plan_set_variants(AtmPlan* plan, int32_t row_variant, int32_t col_tile, int32_t col_variant);
 
 /* Launch categories reported by atm_profile_end. */

@@ -432,8 +432,8 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   // tiled layout: opt-in by flag; the tiled passes write one measure partial per row
   pl->tiled = atm::tiled_supported(pl->N) && (d->flags & ATM_FLAG_TILED) && !(d->flags & ATM_FLAG_ROWMAJOR);
   if (pl->tiled) {
-    pl->row_variant = 5;
-    pl->col_variant = 6;
+    pl->row_variant = 8;
+    pl->col_variant = 8;
     pl->col_tile = 4;
   }
   pl->rows = pl->tiled ? 1 : atm::row_pass_rows(pl->N);
@@ -931,8 +931,8 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   double best_row = -1.0;
   int row_variant = 0;
   // a tiled plan chooses among the tiled forms only (the others do not know its layout)
-  const int v_lo = pl->tiled ? 5 : 0, v_hi = pl->tiled ? 7 : 5;
-  for (int v = v_lo; v < v_hi; ++v) {
+  const std::vector<int> row_forms = pl->tiled ? std::vector<int>{5, 6, 8} : std::vector<int>{0, 1, 2, 3, 4, 7};
+  for (int v : row_forms) {
     ra.variant = v;
     const double ms = time_it([&] { return atm::launch_row_pass(N, batch, ra, st); });
     if (ms >= 0 && (best_row < 0 || ms < best_row)) {
@@ -951,7 +951,8 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   for (int C : {2, 4, 8, 16}) {
     if (C * (N / 16) > 512 || C > N) continue;
     if (pl->tiled && C != 4) continue;
-    for (int v = pl->tiled ? 5 : 0; v < (pl->tiled ? 7 : 5); ++v) {
+    const std::vector<int> col_forms = pl->tiled ? std::vector<int>{5, 6, 8} : std::vector<int>{0, 1, 2, 3, 4, 7};
+    for (int v : col_forms) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
       if (ms >= 0 && (best_col < 0 || ms < best_col)) {
@@ -983,16 +984,18 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
   if (pl->tiled) {
     // a tiled plan's field is only understood by the tiled forms
-    if (row_variant != 5 && row_variant != 6)
-      return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5 or 6", row_variant);
-    if ((col_variant != 5 && col_variant != 6) || col_tile != 4)
-      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5 or 6 with col_tile 4");
+    if (row_variant != 5 && row_variant != 6 && row_variant != 8)
+      return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5, 6 or 8", row_variant);
+    if ((col_variant != 5 && col_variant != 6 && col_variant != 8) || col_tile != 4)
+      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5, 6 or 8 with col_tile 4");
     pl->row_variant = row_variant;
     pl->col_variant = col_variant;
     return ATM_OK;
   }
-  if (row_variant < 0 || row_variant > 4) return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4", row_variant);
-  if (col_variant < 0 || col_variant > 4) return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4", col_variant);
+  if (row_variant < 0 || (row_variant > 4 && row_variant != 7))
+    return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4 or 7", row_variant);
+  if (col_variant < 0 || (col_variant > 4 && col_variant != 7))
+    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4 or 7", col_variant);
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
     return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);
   if (col_tile * (pl->N / 16) > 512 || col_tile > pl->N)

@@ -305,6 +305,132 @@ ATM_HD void stage_last(float2 (&v)[16], int t, const float2* tw) {
 }
 
 // ---------------------------------------------------------------------------
+// Twiddles held in registers.  A persistent pass runs the same butterflies
+// (the same i of every stage) for every row or column it transforms, so a
+// thread's twiddles never change: it loads, once, the bases W_{LR}^{i p} for
+// the powers p = 1, 2, 4, 8 below each stage's radix, and forms the other
+// twiddles as products exactly as TWREC = 1 forms them from table loads.  The
+// results are TWREC = 1's bit for bit, with no shared-memory twiddle traffic.
+// ---------------------------------------------------------------------------
+template <int N, int s>
+struct StagePowers {
+  static constexpr int R = StageRadix<N, s>::value;
+  static constexpr int value = R == 16 ? 4 : R == 8 ? 3 : R == 4 ? 2 : 1;
+};
+template <int N, int s>
+struct StageBases {
+  static constexpr int value = (s == 0) ? 0 : (16 / StageRadix<N, s>::value) * StagePowers<N, s>::value;
+};
+template <int N, int s>
+struct BasesBefore {
+  static constexpr int value = BasesBefore<N, s - 1>::value + StageBases<N, s - 1>::value;
+};
+template <int N>
+struct BasesBefore<N, 0> {
+  static constexpr int value = 0;
+};
+template <int N>
+struct TwBases {
+  static constexpr int NB = BasesBefore<N, FftPlan<N>::S>::value;
+  float2 w[NB > 0 ? NB : 1];  // forward-direction bases; the inverse transform conjugates them
+};
+
+template <int N, int s, int TWPAD>
+ATM_HD void load_bases_stage(TwBases<N>& tb, const float2* tw, int t) {
+  if constexpr (s < FftPlan<N>::S) {
+    if constexpr (s > 0) {
+      constexpr int R = StageRadix<N, s>::value;
+      constexpr int L = StageL<N, s>::value;
+      constexpr int T = N / 16;
+      constexpr int B = 16 / R;
+      constexpr int P = StagePowers<N, s>::value;
+      constexpr int off = BasesBefore<N, s>::value;
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int i = (t + b * T) & (L - 1);
+#pragma unroll
+        for (int j = 0; j < P; ++j) tb.w[off + b * P + j] = twiddle<N, L * R, -1, TWPAD>(tw, i << j);
+      }
+    }
+    load_bases_stage<N, s + 1, TWPAD>(tb, tw, t);
+  }
+}
+
+// the bases of thread t (N / 16 threads per transform) from the table tw
+template <int N, int TWPAD = 0>
+ATM_HD void load_twiddle_bases(TwBases<N>& tb, const float2* tw, int t) {
+  load_bases_stage<N, 0, TWPAD>(tb, tw, t);
+}
+
+// twiddles w[m] = W_{LR}^{i m}, 1 <= m < R, of butterfly b of stage s from the bases
+template <int N, int s, int DIR, int R>
+ATM_HD void stage_twiddles_reg(const TwBases<N>& tb, int b, float2 (&w)[R]) {
+  constexpr int P = StagePowers<N, s>::value;
+  constexpr int off = BasesBefore<N, s>::value;
+#pragma unroll
+  for (int m = 1; m < R; ++m) {
+    const int hp = (m >= 8) ? 8 : (m >= 4) ? 4 : (m >= 2) ? 2 : 1;
+    if (m == hp) {
+      const int lg = (m == 8) ? 3 : (m == 4) ? 2 : (m == 2) ? 1 : 0;
+      const float2 base = tb.w[off + b * P + lg];
+      w[m] = DIR < 0 ? base : cconj(base);
+    } else {
+      w[m] = cmul(w[hp], w[m - hp]);
+    }
+  }
+}
+
+// stage_to_smem / stage_last with the twiddles from the bases
+template <int N, int s, int DIR>
+ATM_HD void stage_to_smem_reg(float2 (&v)[16], float2* sm, int t, const TwBases<N>& tb) {
+  constexpr int R = StageRadix<N, s>::value;
+  constexpr int L = StageL<N, s>::value;
+  constexpr int T = N / 16;
+  constexpr int B = 16 / R;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int k = t + b * T;
+    const int i = k & (L - 1);
+    float2 a[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
+    if (L > 1) {
+      float2 w[R];
+      stage_twiddles_reg<N, s, DIR, R>(tb, b, w);
+#pragma unroll
+      for (int m = 1; m < R; ++m) a[m] = cmul(a[m], w[m]);
+    }
+    dft<R, DIR>(a);
+    const int j = (k - i) * R + i;
+#pragma unroll
+    for (int q = 0; q < R; ++q) sm[pad16(j + q * L)] = a[q];
+  }
+}
+
+template <int N, int DIR>
+ATM_HD void stage_last_reg(float2 (&v)[16], int t, const TwBases<N>& tb) {
+  constexpr int s = FftPlan<N>::S - 1;
+  constexpr int R = StageRadix<N, s>::value;
+  constexpr int B = 16 / R;
+  float2 o[16];
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    float2 a[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
+    float2 w[R];
+    stage_twiddles_reg<N, s, DIR, R>(tb, b, w);
+#pragma unroll
+    for (int m = 1; m < R; ++m) a[m] = cmul(a[m], w[m]);
+    dft<R, DIR>(a);
+#pragma unroll
+    for (int q = 0; q < R; ++q) o[b + B * q] = a[q];
+  }
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = o[m];
+}
+
+// ---------------------------------------------------------------------------
 // fixed-point phase: turns(j) = frac(j * S + O) held as a 64-bit binary
 // fraction; the product wraps modulo one turn exactly.  Returned as
 // half-turns in [-1, 1) for sincospif.

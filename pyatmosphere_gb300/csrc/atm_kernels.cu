@@ -57,6 +57,36 @@ __device__ __forceinline__ void fft_dev_db(float2 (&v)[16], float2* smA, float2*
   }
 }
 
+// the same two drivers with each thread's twiddles from its bases in
+// registers (TWREC = 2 arithmetic, no twiddle loads from shared memory)
+template <int N, int DIR, int s = 0>
+__device__ __forceinline__ void fft_dev_reg(float2 (&v)[16], float2* sm, int t, const TwBases<N>& tb) {
+  if constexpr (s == FftPlan<N>::S - 1) {
+    stage_last_reg<N, DIR>(v, t, tb);
+  } else {
+    stage_to_smem_reg<N, s, DIR>(v, sm, t, tb);
+    __syncthreads();
+    stage_from_smem<N, s + 1>(v, sm, t);
+    __syncthreads();
+    fft_dev_reg<N, DIR, s + 1>(v, sm, t, tb);
+  }
+}
+
+template <int N, int DIR, int s = 0>
+__device__ __forceinline__ void fft_dev_db_reg(float2 (&v)[16], float2* smA, float2* smB, int t,
+                                               const TwBases<N>& tb) {
+  static_assert(FftPlan<N>::S == 3, "alternating exchanges need three stages");
+  if constexpr (s == FftPlan<N>::S - 1) {
+    stage_last_reg<N, DIR>(v, t, tb);
+  } else {
+    float2* sm = (s & 1) ? smB : smA;
+    stage_to_smem_reg<N, s, DIR>(v, sm, t, tb);
+    __syncthreads();
+    stage_from_smem<N, s + 1>(v, sm, t);
+    fft_dev_db_reg<N, DIR, s + 1>(v, smA, smB, t, tb);
+  }
+}
+
 // twiddle table copied into shared memory with the pad16 layout
 template <int N>
 __device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restrict__ tw) {
@@ -318,7 +348,11 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
 
   auto fbuf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * RowPipe<N, ROWS>::STAGE); };
   float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * RowPipe<N, ROWS>::STAGE);
-  load_twiddles<N>(tws, a.tw);
+  TwBases<N> tb;
+  if constexpr (TWREC == 2)
+    load_twiddle_bases<N>(tb, a.tw, t);
+  else
+    load_twiddles<N>(tws, a.tw);
   __shared__ __align__(8) uint64_t full_bar[2];
   const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
   if constexpr (BULK) {
@@ -401,7 +435,12 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
       for (int m = 0; m < 16; ++m) ph[m] = src[t + m * T];
     }
     __syncthreads();  // the exchange below overwrites the staged rows
-    if (flags & ROW_INV) fft_dev<N, 1, 0, 1, TWREC>(v, sm, t, tws);
+    if (flags & ROW_INV) {
+      if constexpr (TWREC == 2)
+        fft_dev_reg<N, 1>(v, sm, t, tb);
+      else
+        fft_dev<N, 1, 0, 1, TWREC>(v, sm, t, tws);
+    }
     if (load_phi && (flags & ROW_FOLDED) && a.loss == 1.0f) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], phasor_turns(ph[m]));  // lossless step: no scaling
@@ -421,7 +460,12 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
       for (int m = 0; m < 16; ++m) v[m] = cscale(v[m], a.loss);
     }
     if (flags & ROW_STEP) measure_step<N, ROWS>(a, v, t, y, r, rb, NRB);
-    if (flags & ROW_FWD) fft_dev<N, -1, 0, 1, TWREC>(v, sm, t, tws);
+    if (flags & ROW_FWD) {
+      if constexpr (TWREC == 2)
+        fft_dev_reg<N, -1>(v, sm, t, tb);
+      else
+        fft_dev<N, -1, 0, 1, TWREC>(v, sm, t, tws);
+    }
     if (flags & ROW_STORE) {
       float2* dst = (a.store_out && a.out) ? a.out : a.field;
 #pragma unroll
@@ -508,6 +552,19 @@ __device__ __forceinline__ void fft_dev_grp(float2 (&v)[16], float2* sm, int t, 
     stage_from_smem<N, s + 1>(v, sm, t);
     group_sync(bar, N / 16);
     fft_dev_grp<N, DIR, s + 1, TWPAD, TWREC>(v, sm, t, tw, bar);
+  }
+}
+
+template <int N, int DIR, int s = 0>
+__device__ __forceinline__ void fft_dev_grp_reg(float2 (&v)[16], float2* sm, int t, const TwBases<N>& tb, int bar) {
+  if constexpr (s == FftPlan<N>::S - 1) {
+    stage_last_reg<N, DIR>(v, t, tb);
+  } else {
+    stage_to_smem_reg<N, s, DIR>(v, sm, t, tb);
+    group_sync(bar, N / 16);
+    stage_from_smem<N, s + 1>(v, sm, t);
+    group_sync(bar, N / 16);
+    fft_dev_grp_reg<N, DIR, s + 1>(v, sm, t, tb, bar);
   }
 }
 
@@ -629,7 +686,7 @@ row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int 
   unsigned char* sbase = smem_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u);
   auto stage = [&](int s) { return reinterpret_cast<float2*>(sbase + s * Cfg::STAGE); };
   float2* tws = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + 4 * Cfg::EXCH);
-  load_twiddles<N>(tws, a.tw);
+  if constexpr (TWREC != 2) load_twiddles<N>(tws, a.tw);
   const int flags = a.flags;
   const bool load_field = !(flags & ROW_GEN);
   const bool load_phi = (flags & ROW_PHASOR) != 0;
@@ -700,6 +757,8 @@ row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int 
   const int rl = tid / T, t = tid - rl * T;
   const int bar = 1 + rl;
   float2* exch = reinterpret_cast<float2*>(sbase + 2 * Cfg::STAGE + rl * Cfg::EXCH);
+  TwBases<N> tb;
+  if constexpr (TWREC == 2) load_twiddle_bases<N>(tb, a.tw, t);
   int k = 0;
   for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++k) {
     const int s = k & 1;
@@ -743,7 +802,12 @@ row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int 
       __syncwarp();
       if ((tid & 31) == 0) mbar_arrive_cta(eb0 + 8 * s);
     }
-    if (flags & ROW_INV) fft_dev_grp<N, 1, 0, 1, TWREC>(v, exch, t, tws, bar);
+    if (flags & ROW_INV) {
+      if constexpr (TWREC == 2)
+        fft_dev_grp_reg<N, 1>(v, exch, t, tb, bar);
+      else
+        fft_dev_grp<N, 1, 0, 1, TWREC>(v, exch, t, tws, bar);
+    }
     if (load_phi && (flags & ROW_FOLDED) && a.loss == 1.0f) {
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], phasor_turns(ph[m]));
@@ -764,7 +828,12 @@ row_pass_tiled_kernel(const __grid_constant__ CUtensorMap tiles, RowArgs a, int 
     }
     if (flags & ROW_STEP)
       measure_row_grp<N>(a, a.step_partials, a.step_center, 6, 0, false, v, t, y, r, bar, red[rl]);
-    if (flags & ROW_FWD) fft_dev_grp<N, -1, 0, 1, TWREC>(v, exch, t, tws, bar);
+    if (flags & ROW_FWD) {
+      if constexpr (TWREC == 2)
+        fft_dev_grp_reg<N, -1>(v, exch, t, tb, bar);
+      else
+        fft_dev_grp<N, -1, 0, 1, TWREC>(v, exch, t, tws, bar);
+    }
     if (flags & ROW_STORE) {
       if (out_tiled) {
         float2* d = dst + (size_t)r * N * N + (size_t)yb * 4 * N + rl * 4;
@@ -838,9 +907,11 @@ static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
   if constexpr (N == 512 || N == 1024 || N == 2048) {
-    if (a.variant == 5 || a.variant == 6) {
+    if (a.variant == 5 || a.variant == 6 || a.variant == 8) {
       // the tiled forms: the only forms that read or write the tiled layout
+      // (8: twiddles in registers)
       if (!field_ok || !phi_ok || (a.store_out && a.out && !aligned16(a.out))) return cudaErrorInvalidValue;
+      if (a.variant == 8) return row_tiled_launch<N, 2>(B, a, st);
       return a.variant == 5 ? row_tiled_launch<N, 0>(B, a, st) : row_tiled_launch<N, 1>(B, a, st);
     }
   }
@@ -862,6 +933,12 @@ static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
     if constexpr (one_row)
       if (!meas) return row_pipe_launch<N, 1, 1, 1>(B, a, st);
     return row_pipe_launch<N, RowRows<N>::value, 1, 1>(B, a, st);
+  }
+  if (field_ok && phi_ok && variant == 7) {
+    // as 4 with each thread's twiddles in registers (the same bits)
+    if constexpr (one_row)
+      if (!meas) return row_pipe_launch<N, 1, 1, 2>(B, a, st);
+    return row_pipe_launch<N, RowRows<N>::value, 1, 2>(B, a, st);
   }
   if (field_ok && phi_ok && variant != 1) return row_pipe_launch<N, RowRows<N>::value>(B, a, st);
   return row_plain_launch<N>(B, a, st);
@@ -1012,7 +1089,7 @@ struct ColTma {
 // DBX = 1: the FFT exchanges alternate between the staged tile and a third
 // buffer (one barrier per exchange instead of two, fft_dev_db); hy is then
 // read through L1 instead of shared memory, which holds the third buffer.
-template <int N, int C, int DBX = 0>
+template <int N, int C, int DBX = 0, int TWREG = 0>
 __global__ void __launch_bounds__(C * (N / 16))
 col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
   constexpr int T = N / 16;
@@ -1026,7 +1103,11 @@ col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_
   unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
   auto buf = [&](int s) { return reinterpret_cast<float2*>(sbase + s * ColTma<N, C>::STAGE); };
   float2* tws = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE);
-  load_twiddles<N>(tws, a.tw);
+  TwBases<N> tb;
+  if constexpr (TWREG)
+    load_twiddle_bases<N>(tb, a.tw, t);  // this thread's twiddles in registers (TWREC = 1 arithmetic)
+  else
+    load_twiddles<N>(tws, a.tw);
   float2* hys = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE + ColPipe<N, C>::TW);
   float2* xbuf = reinterpret_cast<float2*>(sbase + 2 * ColTma<N, C>::STAGE + ColPipe<N, C>::TW);
   if (!DBX && !a.inv_only)
@@ -1077,7 +1158,16 @@ col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_
     for (int m = 0; m < 16; ++m) v[m] = tile[(t + m * T) * C + c];
     __syncthreads();  // the exchange below overwrites the staged tile
     float2* sm = tile + c * S;
-    if constexpr (DBX) {
+    if constexpr (DBX && TWREG) {
+      float2* sm2 = xbuf + c * S;
+      if (!a.inv_only) {
+        fft_dev_db_reg<N, -1>(v, sm, sm2, t, tb);
+        const float2 hx = a.hx[x];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(__ldg(a.hy + t + m * T), hx));
+      }
+      fft_dev_db_reg<N, 1>(v, sm, sm2, t, tb);
+    } else if constexpr (DBX) {
       float2* sm2 = xbuf + c * S;
       if (!a.inv_only) {
         fft_dev_db<N, -1, 0, 1>(v, sm, sm2, t, tws);
@@ -1108,7 +1198,7 @@ col_pass_tma_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_
       if (pending[q]) pass_mbar_wait(bar0 + 8 * q, (uint32_t)(((k + (q != s)) >> 1) & 1));
 }
 
-template <int N, int C, int DBX = 0>
+template <int N, int C, int DBX = 0, int TWREG = 0>
 static cudaError_t col_tma_launch(int B, const ColArgs& a, cudaStream_t st) {
   alignas(128) CUtensorMap map;
   if (!encode_field_tiles(&map, a.field, N, B, C, ColTma<N, C>::BOX_ROWS)) return cudaErrorNotSupported;
@@ -1116,11 +1206,11 @@ static cudaError_t col_tma_launch(int B, const ColArgs& a, cudaStream_t st) {
   const int threads = C * (N / 16);
   const size_t smem = DBX ? ColTma<N, C>::SMEM_DB : ColTma<N, C>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(col_pass_tma_kernel<N, C, DBX>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(col_pass_tma_kernel<N, C, DBX, TWREG>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / C);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  col_pass_tma_kernel<N, C, DBX><<<grid, threads, smem, st>>>(map, a, n_items);
+  col_pass_tma_kernel<N, C, DBX, TWREG><<<grid, threads, smem, st>>>(map, a, n_items);
   return cudaGetLastError();
 }
 
@@ -1278,7 +1368,7 @@ __device__ __forceinline__ void tma_store_col(const CUtensorMap* map, uint32_t s
                : "memory");
 }
 
-template <int N>
+template <int N, int TWREG>
 __global__ void __launch_bounds__(ColGroups<N>::NT, 1)
 col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
   using Cfg = ColGroups<N>;
@@ -1290,7 +1380,7 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
   unsigned char* sbase = smem_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u);
   auto stage = [&](int s) { return reinterpret_cast<float2*>(sbase + s * Cfg::TILE); };
   float2* tws = reinterpret_cast<float2*>(sbase + 2 * Cfg::TILE + 4 * Cfg::EXCH);
-  load_twiddles<N>(tws, a.tw);
+  if constexpr (!TWREG) load_twiddles<N>(tws, a.tw);
   const unsigned long long wait_ns = g_pass_wait_ns;
   const uint32_t fb0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
   const uint32_t db0 = (uint32_t)__cvta_generic_to_shared(&done_bar[0]);
@@ -1368,6 +1458,8 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
   const int g = tid / T, t = tid - g * T;
   const int bar = 1 + g;
   float2* exch = reinterpret_cast<float2*>(sbase + 2 * Cfg::TILE + g * Cfg::EXCH);
+  TwBases<N> tb;
+  if constexpr (TWREG) load_twiddle_bases<N>(tb, a.tw, t);
   int k = 0;
   for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++k) {
     const int s = k & 1;
@@ -1385,12 +1477,18 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = tile[colblock_slot(t + m * T, g)];
     if (!a.inv_only) {
-      fft_dev_grp<N, -1, 0, 1>(v, exch, t, tws, bar);
+      if constexpr (TWREG)
+        fft_dev_grp_reg<N, -1>(v, exch, t, tb, bar);
+      else
+        fft_dev_grp<N, -1, 0, 1>(v, exch, t, tws, bar);
       const float2 hx = a.hx[xb * 4 + g];
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(__ldg(a.hy + t + m * T), hx));
     }
-    fft_dev_grp<N, 1, 0, 1>(v, exch, t, tws, bar);
+    if constexpr (TWREG)
+      fft_dev_grp_reg<N, 1>(v, exch, t, tb, bar);
+    else
+      fft_dev_grp<N, 1, 0, 1>(v, exch, t, tws, bar);
 #pragma unroll
     for (int m = 0; m < 16; ++m) tile[colblock_slot(t + m * T, g)] = v[m];
     // this thread's outputs are in the stage: visible to the tensor store (async proxy)
@@ -1399,7 +1497,7 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
   }
 }
 
-template <int N>
+template <int N, int TWREG>
 static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
   alignas(128) CUtensorMap map;
   if (!encode_tiled_field(&map, a.field, N, B, false, ColGroups<N>::BOX)) return cudaErrorNotSupported;
@@ -1407,11 +1505,11 @@ static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
   const int threads = ColGroups<N>::NT;
   const size_t smem = ColGroups<N>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(col_pass_groups_kernel<N>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(col_pass_groups_kernel<N, TWREG>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / 4);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  col_pass_groups_kernel<N><<<grid, threads, smem, st>>>(map, a, n_items);
+  col_pass_groups_kernel<N, TWREG><<<grid, threads, smem, st>>>(map, a, n_items);
   return cudaGetLastError();
 }
 
@@ -1459,8 +1557,9 @@ static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
       return col_pipe_launch<N, C, 0>(B, a, st);
     }
     if constexpr (FftPlan<N>::S == 3 && ColTma<N, C>::SMEM_DB <= 226 * 1024) {
-      if (aligned16(a.field) && a.variant == 4) {
-        const cudaError_t e = col_tma_launch<N, C, 1>(B, a, st);
+      if (aligned16(a.field) && (a.variant == 4 || a.variant == 7)) {
+        // 7: as 4 with each thread's twiddles in registers
+        const cudaError_t e = a.variant == 7 ? col_tma_launch<N, C, 1, 1>(B, a, st) : col_tma_launch<N, C, 1>(B, a, st);
         if (e != cudaErrorNotSupported) return e;
         return col_pipe_launch<N, C, 0>(B, a, st);
       }
@@ -1491,14 +1590,20 @@ static cudaError_t col_dispatch(int C, int B, const ColArgs& a, cudaStream_t st)
 }
 
 cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t st) {
-  if (a.variant == 5 || a.variant == 6) {
-    // the tiled layout: tiles are block columns (4 columns); C does not apply
+  if (a.variant == 5 || a.variant == 6 || a.variant == 8) {
+    // the tiled layout: tiles are block columns (4 columns); C does not apply.
+    // 8: as 6 with each thread's twiddles in registers
     if (!aligned16(a.field)) return cudaErrorInvalidValue;
-    const bool groups = a.variant == 6;
     switch (N) {
-      case 512: return groups ? col_groups_launch<512>(B, a, st) : col_tiled_launch<512>(B, a, st);
-      case 1024: return groups ? col_groups_launch<1024>(B, a, st) : col_tiled_launch<1024>(B, a, st);
-      case 2048: return groups ? col_groups_launch<2048>(B, a, st) : col_tiled_launch<2048>(B, a, st);
+      case 512:
+        return a.variant == 5 ? col_tiled_launch<512>(B, a, st)
+               : a.variant == 8 ? col_groups_launch<512, 1>(B, a, st) : col_groups_launch<512, 0>(B, a, st);
+      case 1024:
+        return a.variant == 5 ? col_tiled_launch<1024>(B, a, st)
+               : a.variant == 8 ? col_groups_launch<1024, 1>(B, a, st) : col_groups_launch<1024, 0>(B, a, st);
+      case 2048:
+        return a.variant == 5 ? col_tiled_launch<2048>(B, a, st)
+               : a.variant == 8 ? col_groups_launch<2048, 1>(B, a, st) : col_groups_launch<2048, 0>(B, a, st);
     }
     return cudaErrorInvalidValue;
   }

@@ -210,6 +210,12 @@ def test_graph_capture_replays_run(torch_cuda):
     assert not np.array_equal(direct, direct2)
 
 
+ROW_FORMS = (0, 1, 2, 3, 4, 7)
+COL_FORMS = (0, 1, 2, 3, 4, 7)
+PRODUCT_ROW = (4, 7)
+PRODUCT_COL = (2, 7)
+
+
 @pytest.mark.parametrize("N", [512, 2048])
 def test_autotune_keeps_results(torch_cuda, N):
     """atm_autotune changes launch shapes (and, with column variant 2, the
@@ -224,25 +230,33 @@ def test_autotune_keeps_results(torch_cuda, N):
     choice = plan.autotune(repeats=2)
     assert choice["tuned"] == 1
     assert choice["col_tile"] in (2, 4, 8, 16) and choice["col_tile"] * N // 16 <= 512
-    assert choice["row_variant"] in (0, 1, 2, 3, 4) and choice["col_variant"] in (0, 1, 2, 3, 4)
+    assert choice["row_variant"] in ROW_FORMS and choice["col_variant"] in COL_FORMS
     after = plan.run(*sp).cpu().numpy()
-    if choice["col_variant"] == 2 or choice["row_variant"] == 4:
+    if choice["col_variant"] in PRODUCT_COL or choice["row_variant"] in PRODUCT_ROW:
         np.testing.assert_allclose(after, before, rtol=2e-5, atol=1e-9)
     else:
         np.testing.assert_array_equal(after, before)
     # every launch form computes the same arithmetic, except the product
-    # twiddles of column variant 2 and row variant 4 (FP32 round-off)
-    for rv in (0, 1, 2, 3, 4):
+    # twiddles (row variants 4 and 7, column variants 2 and 7: FP32 round-off)
+    product = {}
+    for rv in ROW_FORMS:
         for ct in (2, 4, 8, 16):
             if ct * N // 16 > 512:
                 continue
-            for cv in (0, 1, 2, 3, 4):
+            for cv in COL_FORMS:
                 plan.set_variants(rv, ct, cv)
                 got = plan.run(*sp).cpu().numpy()
-                if cv == 2 or rv == 4:
+                if cv in PRODUCT_COL or rv in PRODUCT_ROW:
                     np.testing.assert_allclose(got, before, rtol=2e-5, atol=1e-9, err_msg=f"{rv} {ct} {cv}")
                 else:
                     np.testing.assert_array_equal(got, before, err_msg=f"{rv} {ct} {cv}")
+                if cv in PRODUCT_COL and rv in PRODUCT_ROW:
+                    product[(rv, ct, cv)] = got
+    # twiddle bases in registers (row 7, column 7) give the bits of the table product forms (row 4, column 2)
+    for (rv, ct, cv), got in product.items():
+        ref = product.get((4, ct, 2))
+        if ref is not None:
+            np.testing.assert_array_equal(got, ref, err_msg=f"{rv} {ct} {cv}")
 
 
 def test_step_measures_match_oracle(torch_cuda):

@@ -62,7 +62,7 @@ def test_tiled_run_equals_row_major(torch_cuda, N):
     tl.close()
 
 
-@pytest.mark.parametrize("row_variant,col_variant", [(5, 5), (6, 5), (5, 6), (6, 6)])
+@pytest.mark.parametrize("row_variant,col_variant", [(5, 5), (6, 5), (5, 6), (6, 6), (8, 8)])
 def test_tiled_run_matches_oracle(torch_cuda, row_variant, col_variant):
     torch = torch_cuda
     spec = o.ChannelSpec(N=512, delta=2e-3, w0=0.09, length=10e3, count=5, points=1024, Cn2=1e-15,
@@ -125,5 +125,30 @@ def test_tiled_autotune_keeps_tiled_forms(torch_cuda):
     spec = o.ChannelSpec(N=2048, delta=1.5e-3, count=2, points=256, length=10e3)
     _, tl, _ = _plans(spec, 2)
     choice = tl.autotune(repeats=1)
-    assert choice["row_variant"] in (5, 6) and choice["col_variant"] in (5, 6) and choice["col_tile"] == 4
+    assert choice["row_variant"] in (5, 6, 8) and choice["col_variant"] in (5, 6, 8) and choice["col_tile"] == 4
     assert tl.info["tiled"] == 1
+
+
+def test_register_twiddles_give_the_product_twiddle_bits(torch_cuda):
+    """Twiddle bases held in registers (row 8 / column 8 tiled, row 7 / column 7
+    row-major) form the twiddles as the table product forms do (row 6 tiled,
+    row 4 / column 2 row-major): the runs agree bit for bit."""
+    torch = torch_cuda
+    spec = o.ChannelSpec(N=2048, delta=1.5e-3, w0=0.12, length=20e3, count=3, points=512, Cn2=5e-16,
+                         pupil_radius=0.2)
+    R = 2
+    rm, tl, base = _plans(spec, R)
+    dev = [torch.from_numpy(a).cuda() for a in _spectra(spec, base, 17, R)]
+    runs = {}
+    for name, plan, v in (("rm table", rm, (4, 4, 2)), ("rm reg", rm, (7, 4, 7)), ("tiled reg", tl, (8, 4, 8)),
+                          ("tiled table rows", tl, (6, 4, 8))):
+        plan.set_variants(*v)
+        f = torch.empty((R, 2048, 2048), dtype=torch.complex64, device="cuda")
+        m = plan.run(*dev, field_out=f).cpu().numpy()
+        plan.check()
+        runs[name] = (m, f)
+    for name in ("rm reg", "tiled reg", "tiled table rows"):
+        assert torch.equal(runs[name][1], runs["rm table"][1]), name
+        # the tiled forms reduce the moments in other kernels: round-off apart
+        np.testing.assert_allclose(runs[name][0], runs["rm table"][0], rtol=1e-9, atol=1e-15, err_msg=name)
+    np.testing.assert_array_equal(runs["rm reg"][0], runs["rm table"][0])
