@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define ATM_ABI_VERSION 1
+#define ATM_ABI_VERSION 2  /* 2: AtmPlanInfo.tiled; atm_plan_check, atm_set_wait_budget */
 
 #define ATM_OK 0
 #define ATM_ERR_INVALID (-1)     /* bad argument */

@@ -1042,7 +1042,7 @@ int atm_vacuum(AtmPlan* pl, void* field, int32_t batch, double dz, void* stream)
   atm::ColArgs ca{};
   ca.field = (float2*)field;
   ca.tw = (const float2*)pl->tw.p;
-  ca.variant = tiled ? 5 : (pl->tiled ? 4 : pl->col_variant);
+  ca.variant = tiled ? pl->col_variant : (pl->tiled ? 4 : pl->col_variant);
   ca.status = (int*)pl->status.p;
   ca.hy = (const float2*)pl->vac_h.p;
   ca.hx = (const float2*)pl->vac_h.p + N;

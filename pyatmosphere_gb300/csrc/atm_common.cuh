@@ -56,8 +56,12 @@ ATM_HD float2 csub(float2 a, float2 b) {
   return make_float2(a.x - b.x, a.y - b.y);
 #endif
 }
+// complex product with its two fused multiply-adds written out: every kernel
+// (and the host emulation) rounds it the same way, whatever the compiler
+// would otherwise contract, so launch forms that share the arithmetic share
+// the bits
 ATM_HD float2 cmul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(fmaf(a.x, b.x, -(a.y * b.y)), fmaf(a.x, b.y, a.y * b.x));
 }
 ATM_HD float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 ATM_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }

@@ -25,6 +25,21 @@ void host_stages(std::vector<Regs>& R, float2* sm, const float2* tw) {
   }
 }
 
+// the same stages with each emulated thread's twiddle bases held apart (the
+// register-twiddle forms of the passes)
+template <int N, int DIR, int s>
+void host_stages_reg(std::vector<Regs>& R, float2* sm, const std::vector<atm::TwBases<N>>& tb) {
+  constexpr int T = N / 16;
+  if constexpr (s == atm::FftPlan<N>::S - 1) {
+    for (int t = 0; t < T; ++t) atm::stage_last_reg<N, DIR>(R[t].v, t, tb[t]);
+  } else {
+    for (int t = 0; t < T; ++t) atm::stage_to_smem_reg<N, s, DIR>(R[t].v, sm, t, tb[t]);
+    for (int t = 0; t < T; ++t) atm::stage_from_smem<N, s + 1>(R[t].v, sm, t);
+    host_stages_reg<N, DIR, s + 1>(R, sm, tb);
+  }
+}
+
+// TWREC = 2: bases per emulated thread, as the persistent passes hold them in registers
 template <int N, int TWREC = 0>
 int host_fft(int dir, const float* in, float* out) {
   constexpr int T = N / 16;
@@ -36,10 +51,18 @@ int host_fft(int dir, const float* in, float* out) {
   std::vector<Regs> R(T);
   for (int t = 0; t < T; ++t)
     for (int m = 0; m < 16; ++m) R[t].v[m] = make_float2(in[2 * (t + m * T)], in[2 * (t + m * T) + 1]);
-  if (dir < 0)
+  if constexpr (TWREC == 2) {
+    std::vector<atm::TwBases<N>> tb(T);
+    for (int t = 0; t < T; ++t) atm::load_twiddle_bases<N>(tb[t], tw.data(), t);
+    if (dir < 0)
+      host_stages_reg<N, -1, 0>(R, sm.data(), tb);
+    else
+      host_stages_reg<N, 1, 0>(R, sm.data(), tb);
+  } else if (dir < 0) {
     host_stages<N, -1, 0, TWREC>(R, sm.data(), tw.data());
-  else
+  } else {
     host_stages<N, 1, 0, TWREC>(R, sm.data(), tw.data());
+  }
   for (int t = 0; t < T; ++t)
     for (int m = 0; m < 16; ++m) {
       out[2 * (t + m * T)] = R[t].v[m].x;
@@ -62,6 +85,20 @@ int atm_selftest_fft(int N, int dir, const float* in, float* out) {
     case 1024: return host_fft<1024>(dir, in, out);
     case 2048: return host_fft<2048>(dir, in, out);
     case 4096: return host_fft<4096>(dir, in, out);
+  }
+  return -1;
+}
+
+// the same with the twiddle bases held per thread (register-twiddle forms)
+int atm_selftest_fft_twreg(int N, int dir, const float* in, float* out) {
+  switch (N) {
+    case 64: return host_fft<64, 2>(dir, in, out);
+    case 128: return host_fft<128, 2>(dir, in, out);
+    case 256: return host_fft<256, 2>(dir, in, out);
+    case 512: return host_fft<512, 2>(dir, in, out);
+    case 1024: return host_fft<1024, 2>(dir, in, out);
+    case 2048: return host_fft<2048, 2>(dir, in, out);
+    case 4096: return host_fft<4096, 2>(dir, in, out);
   }
   return -1;
 }

@@ -15,7 +15,7 @@ LIB_DIR = os.path.join(_HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libatm.so")
 SELFTEST_PATH = os.path.join(LIB_DIR, "libatm_selftest.so")
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_PUPILS = 8
 FLAG_SIMT_GEMM = 1
 FLAG_TC_GEMM = 2
@@ -203,6 +203,8 @@ def load_selftest(path: str = SELFTEST_PATH):
     lib.atm_selftest_fft.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.atm_selftest_fft_twrec.restype = ctypes.c_int
     lib.atm_selftest_fft_twrec.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.atm_selftest_fft_twreg.restype = ctypes.c_int
+    lib.atm_selftest_fft_twreg.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.atm_selftest_bessel.restype = ctypes.c_int
     lib.atm_selftest_bessel.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
     lib.atm_selftest_turns.restype = ctypes.c_int

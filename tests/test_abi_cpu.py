@@ -31,14 +31,14 @@ def test_library_exports_every_declared_symbol(built):
     from pyatmosphere_gb300.engine import _lib
     assert set(names) == set(_lib.SIGNATURES), "ctypes signatures must cover include/atm.h"
     lib.atm_abi_version.restype = ctypes.c_int
-    assert lib.atm_abi_version() == 1
+    assert lib.atm_abi_version() == _lib.ABI_VERSION == 2
 
 
 def test_plan_create_rejects_bad_descriptors_without_gpu(built):
     from pyatmosphere_gb300.engine import _lib
     lib = _lib.load(built["libatm"])
     d = _lib.AtmChannelDesc()
-    d.abi_version = 1
+    d.abi_version = _lib.ABI_VERSION
     d.resolution = 100          # not a power of two
     d.delta, d.wvl, d.w0, d.batch = 1e-3, 8e-7, 0.1, 1
     h = ctypes.c_void_p()
@@ -66,6 +66,10 @@ def test_kernel_fft_arithmetic_on_host(built, N):
         out2 = np.zeros(N, np.complex64)
         assert lib.atm_selftest_fft_twrec(N, d, x.ctypes.data, out2.ctypes.data) == 0
         assert np.linalg.norm(out2 - ref) / np.linalg.norm(ref) < 5e-7
+        # twiddle bases held per thread (the register-twiddle passes): the same bits
+        out3 = np.zeros(N, np.complex64)
+        assert lib.atm_selftest_fft_twreg(N, d, x.ctypes.data, out3.ctypes.data) == 0
+        np.testing.assert_array_equal(out3, out2)
 
 
 def test_bessel_coefficients_on_host(built):

@@ -3,7 +3,9 @@ passes) against the row-major forms and the FP64 oracle.
 
 The tiled row pass (variant 5) and column pass (variant 5) run the same FFT
 arithmetic as the row-major bulk-copy row pass (variant 3) and the TMA column
-pass with alternating exchanges (variant 4), and the measures reduce one row
+pass with alternating exchanges (variant 4); the product-twiddle forms (tiled
+row 6 and 8, column 8; row-major row 4 and 7, column 2 and 7) share another
+arithmetic, with or without the twiddle bases in registers.  The measures reduce one row
 per partial in both at N = 2048: there the results are equal bit for bit.  At
 N = 512 and 1024 the row-major forms sum several rows per partial, so the
 moments agree to FP64 round-off and the field bit for bit."""
@@ -32,6 +34,7 @@ def _plans(spec, batch, **kw):
     tl = EnginePlan(spec.N, spec.delta, spec.wvl, spec.w0, spec.F0, pos, spec.length, flags=_lib.FLAG_TILED,
                     **common)
     assert tl.info["tiled"] == 1 and rm.info["tiled"] == 0
+    tl.set_variants(5, 4, 5)  # the table-twiddle tiled forms: rm's arithmetic
     return rm, tl, base
 
 
