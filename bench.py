@@ -232,6 +232,15 @@ def reference_algorithm_on_torch(dev, host_spectra, n_real):
 # ---------------------------------------------------------------------------
 # GB300 engine
 # ---------------------------------------------------------------------------
+def bf16_peak():
+    """The measured dense bf16 burst peak (TFLOP/s) of MEASURED_PEAKS.json, else None."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def surrogate_leg(args, dev):
     """PDT surrogate (the inference configuration): 100,000 seeded queries, 90 %
     inside the training box and 10 % outside it (path length 20-100 km).  The
@@ -281,6 +290,18 @@ def surrogate_leg(args, dev):
     torch.cuda.synchronize()
     q_dev = n_q * reps / (e0.elapsed_time(e1) * 1e-3)
     answered = float(ans.float().mean())
+    # the networks alone (the fused inference kernels of all members): algorithmic FLOPs / time
+    mlps = [m.mlp for m in ens.members]
+    widths = mlps[0].widths
+    flop_q = 2 * sum(widths[i] * widths[i + 1] for i in range(len(widths) - 1)) * len(mlps)
+    e0.record(stream)
+    for _ in range(reps):
+        for m in mlps:
+            m.infer(X, ens.members[0].lo, ens.members[0].hi)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mlp_s = e0.elapsed_time(e1) * 1e-3 / reps
+    mlp_tflops = n_q * flop_q / mlp_s / 1e12
     out_host = torch.empty((n_q, N_HIST), dtype=torch.float32).pin_memory()
 
     def e2e_query():
@@ -331,6 +352,9 @@ def surrogate_leg(args, dev):
             "answered_frac": answered, "simulated_queries_per_s": q_sim, "mixed_queries_per_s": mixed,
             "h2d_bytes_per_batch": int(X_host.numel() * 4), "d2h_bytes_per_batch": int(out_host.numel() * 4),
             "members": len(ens.members), "threshold": ens.threshold,
+            "mlp": {"form": mlps[0].infer_form, "widths": list(widths), "ms_per_batch": mlp_s * 1e3,
+                    "tflops": mlp_tflops, "flop_per_query": flop_q,
+                    "frac_of_bf16_peak": mlp_tflops / bf16_peak() if bf16_peak() else None},
             "heldout_points": n_pts, "heldout_answered_frac": float(a.mean()),
             "frac_ks_le_0.02": float((kb[a] <= 0.02).mean()) if a.any() else None,
             "ks_binned_median": float(np.median(kb[a])) if a.any() else None,

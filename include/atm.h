@@ -139,8 +139,10 @@ typedef struct AtmPlanInfo {
                                     warps with their own named barrier; a producer warp loads and stores
                                     the block columns with TMA,
                                  7: as 4 with each thread's twiddle bases held in registers (the
-                                    product-twiddle arithmetic of 2),
-                                 8: as 6 with each thread's twiddle bases held in registers */
+                                    product-twiddle arithmetic of 2; tiles that the TMA form does
+                                    not take run the form of 2),
+                                 8: as 6 with each thread's twiddle bases held in registers,
+                                 9: as 6 with twiddles formed from powers of two (the bits of 8) */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
                                  form with 128 x 128 tiles (ATM_FLAG_TC_N128), 3 the same with 128 x 256
@@ -254,8 +256,25 @@ int atm_mlp_loss(AtmMlp* mlp, const float* target, int32_t batch, int32_t n_hist
 int atm_mlp_backward(AtmMlp* mlp, const float* dy, int32_t batch, float* grads, void* stream);
 int atm_mlp_adam(AtmMlp* mlp, float lr, float beta1, float beta2, float eps, float weight_decay, int32_t step,
                  void* stream);
+/* Inference: y [batch][out] with a softmax over the first n_hist outputs;
+ * out_of_range[b] = 1 where an input leaves [lo, hi] (lo, hi NULL: no check).
+ * Where the shape allows it (<= 32 inputs, equal hidden widths that are a
+ * multiple of 64 and <= 256, <= 128 outputs) it runs as one fused kernel on
+ * the tensor cores: tcgen05 BF16 MMAs with FP32 accumulation in TMEM, the
+ * activations kept on chip as BF16, the inputs as two BF16 slices (about
+ * 16 bits); any batch in one launch.  Otherwise (or after
+ * atm_mlp_set_infer_form(mlp, 1)) the tile-GEMM form of atm_mlp_forward with
+ * FP32 activations runs, max_batch queries per launch sequence. */
 int atm_mlp_infer(AtmMlp* mlp, const float* x, int32_t batch, const float* lo, const float* hi, int32_t n_hist,
                   float* y, int32_t* out_of_range, void* stream);
+/* 0: the tensor-core form where the shape allows it (default), 1: the tile-GEMM
+ * form, 2: the tensor-core form (ATM_ERR_UNSUPPORTED if the shape does not allow it). */
+int atm_mlp_set_infer_form(AtmMlp* mlp, int32_t form);
+/* The form atm_mlp_infer runs: 1 tile GEMM, 2 tensor cores (or an error code). */
+int atm_mlp_infer_form(const AtmMlp* mlp);
+/* Synchronises the device and reports (then clears) a bounded wait of the
+ * tensor-core inference that ran out: ATM_ERR_TIMEOUT, else ATM_OK. */
+int atm_mlp_check(AtmMlp* mlp);
 
 /* Unit-test entry point of the tensor-core screen GEMM: out[s][m][n] =
  * scale * sum_k A[s][m][k] B[s][n][k] for FP32 device arrays (row stride K),
@@ -272,9 +291,9 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
  * (`batch` realisations, `repeats` timed launches each after one warm-up)
  * and keeps the fastest: row-pass variant (0..4 and 7; a tiled plan: 5, 6, 8),
  * column tile (2..16 columns, at most 512 threads per CTA; a tiled plan: 4)
- * and column-pass variant (0..4 and 7; a tiled plan: 5, 6, 8).  The forms
+ * and column-pass variant (0..4 and 7; a tiled plan: 5, 6, 8, 9).  The forms
  * that build twiddles as products of powers of two (row 4, 6, 7, 8; column
- * 2, 7, 8) round differently from the table forms (FP32 round-off, well
+ * 2, 7, 8, 9) round differently from the table forms (FP32 round-off, well
  * inside the 1e-4 field bound); the results are otherwise the same.  Overwrites the
  * plan's field / screen workspace (zeroes) and blocks until the timing
  * launches finish, so it is called outside CUDA-graph capture, before the
@@ -293,7 +312,7 @@ int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* s
 /* Sets the launch choices atm_autotune makes by hand: row-pass variant 0..4
  * or 7, column tile 2/4/8/16 with at most 512 threads per CTA, column-pass
  * variant 0..4 or 7; a tiled plan (ATM_FLAG_TILED) takes row 5, 6 or 8,
- * column tile 4 and column 5, 6 or 8.  Results do not change, except for
+ * column tile 4 and column 5, 6, 8 or 9.  Results do not change, except for
  * FP32 round-off between the table-twiddle and product-twiddle forms.  No
  * reference counterpart. */
 int atm_plan_set_variants(AtmPlan* plan, int32_t row_variant, int32_t col_tile, int32_t col_variant);

@@ -75,3 +75,26 @@ def loss_and_grad(params, widths, x, t, n_hist, w_mse):
         if l > 0:
             dz = (dz @ bf16_round(W)) * gelu_grad(pres[l])
     return loss, np.concatenate(grads)
+
+
+def infer_tc_emulated(params, widths, x, n_hist):
+    """The arithmetic of the engine's fused tensor-core inference in FP64:
+    inputs as two bfloat16 slices x = hi + lo (lo = bf16(x - hi) formed in
+    FP32), bfloat16 weights, hidden activations rounded to bfloat16 after
+    GELU, FP64 sums in place of the tensor cores' FP32 accumulation; a
+    softmax over the first n_hist outputs, the rest raw."""
+    layers = unpack(np.asarray(params, np.float64), widths)
+    x32 = np.asarray(x, np.float32)
+    hi = bf16_round(x32)
+    lo = bf16_round((x32.astype(np.float64) - hi).astype(np.float32))
+    a = hi + lo
+    for l, (W, b) in enumerate(layers):
+        z = a @ bf16_round(W).T + b
+        if l < len(layers) - 1:
+            a = bf16_round(gelu(z).astype(np.float32))
+        else:
+            a = z
+    h = a[:, :n_hist] - a[:, :n_hist].max(axis=1, keepdims=True)
+    p = np.exp(h)
+    p /= p.sum(axis=1, keepdims=True)
+    return np.concatenate([p, a[:, n_hist:]], axis=1)

@@ -432,8 +432,10 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   // tiled layout: opt-in by flag; the tiled passes write one measure partial per row
   pl->tiled = atm::tiled_supported(pl->N) && (d->flags & ATM_FLAG_TILED) && !(d->flags & ATM_FLAG_ROWMAJOR);
   if (pl->tiled) {
-    pl->row_variant = 8;
-    pl->col_variant = 8;
+    // product twiddles from the table's bases: the tiled forms' registers (one CTA of
+    // 17 warps per SM) leave no room for bases held in registers at N = 2048
+    pl->row_variant = 6;
+    pl->col_variant = 9;
     pl->col_tile = 4;
   }
   pl->rows = pl->tiled ? 1 : atm::row_pass_rows(pl->N);
@@ -951,7 +953,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   for (int C : {2, 4, 8, 16}) {
     if (C * (N / 16) > 512 || C > N) continue;
     if (pl->tiled && C != 4) continue;
-    const std::vector<int> col_forms = pl->tiled ? std::vector<int>{5, 6, 8} : std::vector<int>{0, 1, 2, 3, 4, 7};
+    const std::vector<int> col_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9} : std::vector<int>{0, 1, 2, 3, 4, 7};
     for (int v : col_forms) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
@@ -986,8 +988,8 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
     // a tiled plan's field is only understood by the tiled forms
     if (row_variant != 5 && row_variant != 6 && row_variant != 8)
       return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5, 6 or 8", row_variant);
-    if ((col_variant != 5 && col_variant != 6 && col_variant != 8) || col_tile != 4)
-      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5, 6 or 8 with col_tile 4");
+    if ((col_variant != 5 && col_variant != 6 && col_variant != 8 && col_variant != 9) || col_tile != 4)
+      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5, 6, 8 or 9 with col_tile 4");
     pl->row_variant = row_variant;
     pl->col_variant = col_variant;
     return ATM_OK;

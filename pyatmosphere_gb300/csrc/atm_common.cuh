@@ -366,21 +366,35 @@ ATM_HD void load_twiddle_bases(TwBases<N>& tb, const float2* tw, int t) {
   load_bases_stage<N, 0, TWPAD>(tb, tw, t);
 }
 
-// twiddles w[m] = W_{LR}^{i m}, 1 <= m < R, of butterfly b of stage s from the bases
+// base w8 of a radix-16 butterfly (forward bases; the inverse conjugates)
+template <int N>
+ATM_HD float2 w8_of(const TwBases<N>& tb, int first, int DIR) {
+  const float2 base = tb.w[first + 3];
+  return DIR < 0 ? base : cconj(base);
+}
+
+// a[m] *= W_{LR}^{i m}, 1 <= m < R, for butterfly b of stage s, with the
+// twiddles formed from the bases: w1, w2, w4, w8 are bases; w3 = w2 w1,
+// w(4 + j) = w4 wj, w(8 + j) = w8 wj (j < 4, j < 8).  Each twiddle is applied
+// as soon as it is formed, so only w1 .. w7 stay live for the w(8 + j).
 template <int N, int s, int DIR, int R>
-ATM_HD void stage_twiddles_reg(const TwBases<N>& tb, int b, float2 (&w)[R]) {
+ATM_HD void apply_twiddles_reg(const TwBases<N>& tb, int b, float2 (&a)[R]) {
   constexpr int P = StagePowers<N, s>::value;
   constexpr int off = BasesBefore<N, s>::value;
+  float2 w[R < 8 ? R : 8];
 #pragma unroll
   for (int m = 1; m < R; ++m) {
     const int hp = (m >= 8) ? 8 : (m >= 4) ? 4 : (m >= 2) ? 2 : 1;
+    float2 wm;
     if (m == hp) {
       const int lg = (m == 8) ? 3 : (m == 4) ? 2 : (m == 2) ? 1 : 0;
       const float2 base = tb.w[off + b * P + lg];
-      w[m] = DIR < 0 ? base : cconj(base);
+      wm = DIR < 0 ? base : cconj(base);
     } else {
-      w[m] = cmul(w[hp], w[m - hp]);
+      wm = cmul(m >= 8 ? w8_of(tb, off + b * P, DIR) : w[hp], w[m - hp]);
     }
+    if (m < 8) w[m] = wm;
+    a[m] = cmul(a[m], wm);
   }
 }
 
@@ -398,12 +412,7 @@ ATM_HD void stage_to_smem_reg(float2 (&v)[16], float2* sm, int t, const TwBases<
     float2 a[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
-    if (L > 1) {
-      float2 w[R];
-      stage_twiddles_reg<N, s, DIR, R>(tb, b, w);
-#pragma unroll
-      for (int m = 1; m < R; ++m) a[m] = cmul(a[m], w[m]);
-    }
+    if (L > 1) apply_twiddles_reg<N, s, DIR, R>(tb, b, a);
     dft<R, DIR>(a);
     const int j = (k - i) * R + i;
 #pragma unroll
@@ -422,10 +431,7 @@ ATM_HD void stage_last_reg(float2 (&v)[16], int t, const TwBases<N>& tb) {
     float2 a[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = v[b + B * m];
-    float2 w[R];
-    stage_twiddles_reg<N, s, DIR, R>(tb, b, w);
-#pragma unroll
-    for (int m = 1; m < R; ++m) a[m] = cmul(a[m], w[m]);
+    apply_twiddles_reg<N, s, DIR, R>(tb, b, a);
     dft<R, DIR>(a);
 #pragma unroll
     for (int q = 0; q < R; ++q) o[b + B * q] = a[q];

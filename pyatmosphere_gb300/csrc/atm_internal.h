@@ -237,6 +237,32 @@ cudaError_t launch_screen_table_tc(int B, const ScreenArgs& a, cudaStream_t st);
 cudaError_t launch_cheb_cols_tc(int B, int N, int Kp, int kc0, int D, const float* Ach, __half* hi, __half* lo,
                                 cudaStream_t st);
 cudaError_t tc_error_flag(int* host_flag, bool reset);
+// fused tensor-core inference of the surrogate MLP: a packed BF16 weight
+// image in pieces of <= 128 output rows, laid out as the MMAs read them
+// (K blocks of 64, rows of 128 bytes, 16-byte chunk c of row r at c ^ (r % 8))
+constexpr int kMlpMaxPieces = 16;
+constexpr int kMlpMaxLayers = 8;
+struct MlpPiece {
+  uint32_t src;     // byte offset of the piece in the image
+  uint32_t bytes;   // rows x K blocks x 128
+  int32_t layer;    // the piece holds output rows [col0, col0 + rows) of this layer
+  int32_t rows;     // a multiple of 16, <= 128
+  int32_t col0;     // first output row = first TMEM column of the accumulator
+  int32_t k_steps;  // MMAs of K = 16
+};
+struct MlpTcArgs {
+  const float* x;    // [batch][in] FP32 inputs
+  float* y;          // [batch][out]: softmax over the first n_hist outputs, the rest raw
+  int* oor;          // [batch] 1 where an input leaves [lo, hi]; null: no check
+  const float* lo;   // [in] or null
+  const float* hi;
+  const unsigned char* img;
+  const float* bias[kMlpMaxLayers];
+  int batch, in, k0, hidden, out, out_pad, layers, n_hist, n_pieces;
+  int* status;       // STATUS_GEMM_WAIT on a wait that ran out
+  MlpPiece pieces[kMlpMaxPieces];
+};
+cudaError_t launch_mlp_infer_tc(const MlpTcArgs& a, cudaStream_t st);
 // records the message returned by atm_last_error() on this host thread; returns code
 int set_error(int code, const char* fmt, ...);
 

@@ -1368,7 +1368,9 @@ __device__ __forceinline__ void tma_store_col(const CUtensorMap* map, uint32_t s
                : "memory");
 }
 
-template <int N, int TWREG>
+// TW: 0 twiddles from the table, 1 formed from table bases (powers of two),
+// 2 formed from bases held in registers (the bits of 1)
+template <int N, int TW>
 __global__ void __launch_bounds__(ColGroups<N>::NT, 1)
 col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
   using Cfg = ColGroups<N>;
@@ -1380,7 +1382,7 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
   unsigned char* sbase = smem_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u);
   auto stage = [&](int s) { return reinterpret_cast<float2*>(sbase + s * Cfg::TILE); };
   float2* tws = reinterpret_cast<float2*>(sbase + 2 * Cfg::TILE + 4 * Cfg::EXCH);
-  if constexpr (!TWREG) load_twiddles<N>(tws, a.tw);
+  if constexpr (TW != 2) load_twiddles<N>(tws, a.tw);
   const unsigned long long wait_ns = g_pass_wait_ns;
   const uint32_t fb0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
   const uint32_t db0 = (uint32_t)__cvta_generic_to_shared(&done_bar[0]);
@@ -1459,7 +1461,7 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
   const int bar = 1 + g;
   float2* exch = reinterpret_cast<float2*>(sbase + 2 * Cfg::TILE + g * Cfg::EXCH);
   TwBases<N> tb;
-  if constexpr (TWREG) load_twiddle_bases<N>(tb, a.tw, t);
+  if constexpr (TW == 2) load_twiddle_bases<N>(tb, a.tw, t);
   int k = 0;
   for (int item = blockIdx.x; item < n_items; item += gridDim.x, ++k) {
     const int s = k & 1;
@@ -1477,18 +1479,18 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = tile[colblock_slot(t + m * T, g)];
     if (!a.inv_only) {
-      if constexpr (TWREG)
+      if constexpr (TW == 2)
         fft_dev_grp_reg<N, -1>(v, exch, t, tb, bar);
       else
-        fft_dev_grp<N, -1, 0, 1>(v, exch, t, tws, bar);
+        fft_dev_grp<N, -1, 0, 1, TW>(v, exch, t, tws, bar);
       const float2 hx = a.hx[xb * 4 + g];
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], cmul(__ldg(a.hy + t + m * T), hx));
     }
-    if constexpr (TWREG)
+    if constexpr (TW == 2)
       fft_dev_grp_reg<N, 1>(v, exch, t, tb, bar);
     else
-      fft_dev_grp<N, 1, 0, 1>(v, exch, t, tws, bar);
+      fft_dev_grp<N, 1, 0, 1, TW>(v, exch, t, tws, bar);
 #pragma unroll
     for (int m = 0; m < 16; ++m) tile[colblock_slot(t + m * T, g)] = v[m];
     // this thread's outputs are in the stage: visible to the tensor store (async proxy)
@@ -1497,7 +1499,7 @@ col_pass_groups_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
   }
 }
 
-template <int N, int TWREG>
+template <int N, int TW>
 static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
   alignas(128) CUtensorMap map;
   if (!encode_tiled_field(&map, a.field, N, B, false, ColGroups<N>::BOX)) return cudaErrorNotSupported;
@@ -1505,11 +1507,11 @@ static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
   const int threads = ColGroups<N>::NT;
   const size_t smem = ColGroups<N>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(col_pass_groups_kernel<N, TWREG>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(col_pass_groups_kernel<N, TW>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / 4);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  col_pass_groups_kernel<N, TWREG><<<grid, threads, smem, st>>>(map, a, n_items);
+  col_pass_groups_kernel<N, TW><<<grid, threads, smem, st>>>(map, a, n_items);
   return cudaGetLastError();
 }
 
@@ -1561,10 +1563,13 @@ static cudaError_t col_launch(int B, const ColArgs& a, cudaStream_t st) {
         // 7: as 4 with each thread's twiddles in registers
         const cudaError_t e = a.variant == 7 ? col_tma_launch<N, C, 1, 1>(B, a, st) : col_tma_launch<N, C, 1>(B, a, st);
         if (e != cudaErrorNotSupported) return e;
-        return col_pipe_launch<N, C, 0>(B, a, st);
+        return a.variant == 7 ? col_pipe_launch<N, C, 1>(B, a, st) : col_pipe_launch<N, C, 0>(B, a, st);
       }
     }
   }
+  // 7 where its TMA form does not fit: the pipelined form with the same (product) twiddle bits
+  if (C >= 2 && aligned16(a.field) && ColPipe<N, C>::SMEM <= 220 * 1024 && a.variant == 7)
+    return col_pipe_launch<N, C, 1>(B, a, st);
   return col_plain_launch<N, C>(B, a, st);
 }
 
@@ -1589,21 +1594,26 @@ static cudaError_t col_dispatch(int C, int B, const ColArgs& a, cudaStream_t st)
   return cudaErrorInvalidValue;
 }
 
+template <int N>
+static cudaError_t col_tiled_dispatch(int B, const ColArgs& a, cudaStream_t st) {
+  switch (a.variant) {
+    case 5: return col_tiled_launch<N>(B, a, st);
+    case 6: return col_groups_launch<N, 0>(B, a, st);
+    case 9: return col_groups_launch<N, 1>(B, a, st);
+    case 8: return col_groups_launch<N, 2>(B, a, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t st) {
-  if (a.variant == 5 || a.variant == 6 || a.variant == 8) {
+  if (a.variant == 5 || a.variant == 6 || a.variant == 8 || a.variant == 9) {
     // the tiled layout: tiles are block columns (4 columns); C does not apply.
-    // 8: as 6 with each thread's twiddles in registers
+    // 6: table twiddles, 9: twiddles formed from table bases, 8: from bases in registers
     if (!aligned16(a.field)) return cudaErrorInvalidValue;
     switch (N) {
-      case 512:
-        return a.variant == 5 ? col_tiled_launch<512>(B, a, st)
-               : a.variant == 8 ? col_groups_launch<512, 1>(B, a, st) : col_groups_launch<512, 0>(B, a, st);
-      case 1024:
-        return a.variant == 5 ? col_tiled_launch<1024>(B, a, st)
-               : a.variant == 8 ? col_groups_launch<1024, 1>(B, a, st) : col_groups_launch<1024, 0>(B, a, st);
-      case 2048:
-        return a.variant == 5 ? col_tiled_launch<2048>(B, a, st)
-               : a.variant == 8 ? col_groups_launch<2048, 1>(B, a, st) : col_groups_launch<2048, 0>(B, a, st);
+      case 512: return col_tiled_dispatch<512>(B, a, st);
+      case 1024: return col_tiled_dispatch<1024>(B, a, st);
+      case 2048: return col_tiled_dispatch<2048>(B, a, st);
     }
     return cudaErrorInvalidValue;
   }

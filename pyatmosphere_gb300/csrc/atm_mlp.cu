@@ -185,6 +185,42 @@ __global__ void infer_finish_kernel(float* __restrict__ Y, const float* __restri
   }
 }
 
+// the packed weight image of the tensor-core inference: one thread per
+// 16-byte chunk; layer 0 holds its weights twice along K ([0, k0) for the
+// inputs' hi slice, [k0, 2 k0) for the lo slice)
+struct MlpPackArgs {
+  const uint16_t* w[atm::kMlpMaxLayers];  // BF16 bits [out][in] per layer
+  int in[atm::kMlpMaxLayers], out[atm::kMlpMaxLayers];
+  int k0, n_pieces;
+  atm::MlpPiece pieces[atm::kMlpMaxPieces];
+};
+
+__global__ void mlp_pack_kernel(const __grid_constant__ MlpPackArgs a, uint4* __restrict__ img, int n_chunks) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_chunks) return;
+  const uint32_t byte = (uint32_t)i * 16u;
+  int p = 0;
+  while (p + 1 < a.n_pieces && a.pieces[p + 1].src <= byte) ++p;
+  const atm::MlpPiece pc = a.pieces[p];
+  const uint32_t local = byte - pc.src, kb_bytes = (uint32_t)pc.rows * 128u;
+  const int kb = (int)(local / kb_bytes), rem = (int)(local % kb_bytes);
+  const int r = rem >> 7, c = ((rem >> 4) & 7) ^ (r & 7);  // stored chunk -> logical chunk
+  const int l = pc.layer, row = pc.col0 + r, I = a.in[l];
+  uint32_t wv[4];
+#pragma unroll
+  for (int e = 0; e < 8; e += 2) {
+    uint32_t bits[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      int k = kb * 64 + c * 8 + e + h;
+      if (l == 0) k = k < a.k0 ? k : (k < 2 * a.k0 ? k - a.k0 : I);
+      bits[h] = (row < a.out[l] && k < I) ? a.w[l][(size_t)row * I + k] : 0u;
+    }
+    wv[e / 2] = bits[0] | (bits[1] << 16);  // the lower K index at the lower address
+  }
+  img[i] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+}
+
 }  // namespace
 
 struct AtmMlp {
@@ -203,7 +239,19 @@ struct AtmMlp {
   std::vector<float*> pre;         // pre-activations of hidden layers
   float* d0 = nullptr;             // gradient work buffers
   float* d1 = nullptr;
+  // tensor-core inference (atm_mlp_infer's default where the shape allows it)
+  bool tc_ok = false;
+  int form = 0;                    // 0 auto, 1 tile GEMM, 2 tensor cores
+  int k0 = 16, out_pad = 0;
+  int n_pieces = 0;
+  atm::MlpPiece pieces[atm::kMlpMaxPieces];
+  unsigned char* img = nullptr;    // packed BF16 weights
+  size_t img_bytes = 0;
+  bool img_dirty = true;           // the weights changed since the last packing
+  int* status = nullptr;           // device word: STATUS_GEMM_WAIT
   ~AtmMlp() {
+    cudaFree(img);
+    cudaFree(status);
     cudaFree(w);
     cudaFree(wb);
     cudaFree(g);
@@ -268,6 +316,38 @@ int atm_mlp_create(int32_t n_layers, const int32_t* widths, int32_t max_batch, A
   cudaMemset(p->m, 0, off * 4);
   cudaMemset(p->v, 0, off * 4);
   cudaMemset(p->g, 0, off * 4);
+  // tensor-core inference: <= 32 inputs, equal hidden widths (a multiple of 64, <= 256), <= 128 outputs
+  const int hid = widths[1];
+  bool tc = n_layers >= 2 && widths[0] <= 32 && hid % 64 == 0 && hid <= 256 && widths[n_layers] <= 128;
+  for (int l = 1; tc && l < n_layers; ++l) tc = widths[l] == hid;
+  if (tc) {
+    p->k0 = widths[0] <= 16 ? 16 : 32;
+    p->out_pad = (widths[n_layers] + 15) / 16 * 16;
+    uint32_t src = 0;
+    for (int l = 0; tc && l < n_layers; ++l) {
+      const int rows_l = l == n_layers - 1 ? p->out_pad : hid;
+      const int kblocks = l == 0 ? 1 : hid / 64;
+      for (int r0 = 0; r0 < rows_l; r0 += 128) {
+        if (p->n_pieces == atm::kMlpMaxPieces) {
+          tc = false;
+          break;
+        }
+        atm::MlpPiece& pc = p->pieces[p->n_pieces++];
+        pc.layer = l;
+        pc.rows = std::min(128, rows_l - r0);
+        pc.col0 = r0;
+        pc.k_steps = l == 0 ? 2 * p->k0 / 16 : 4 * kblocks;
+        pc.src = src;
+        pc.bytes = (uint32_t)pc.rows * kblocks * 128u;
+        src += pc.bytes;
+      }
+    }
+    p->img_bytes = src;
+    tc = tc && cudaMalloc(&p->img, p->img_bytes) == cudaSuccess && cudaMalloc(&p->status, sizeof(int)) == cudaSuccess;
+    if (tc) cudaMemset(p->status, 0, sizeof(int));
+    cudaGetLastError();
+  }
+  p->tc_ok = tc;
   *out = p;
   return ATM_OK;
 }
@@ -289,6 +369,7 @@ int atm_mlp_set_params(AtmMlp* p, const float* host) {
   MLP_CUDA(cudaMemset(p->m, 0, p->n_params * 4));
   MLP_CUDA(cudaMemset(p->v, 0, p->n_params * 4));
   MLP_CUDA(cudaDeviceSynchronize());
+  p->img_dirty = true;
   return ATM_OK;
 }
 
@@ -374,6 +455,7 @@ int atm_mlp_adam(AtmMlp* p, float lr, float b1, float b2, float eps, float weigh
   adam_kernel<<<(unsigned)((p->n_params + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       p->w, p->wb, p->g, p->m, p->v, (int)p->n_params, lr, b1, b2, eps, c1, c2, weight_decay);
   MLP_CUDA(cudaGetLastError());
+  p->img_dirty = true;
   return ATM_OK;
 }
 
@@ -383,8 +465,48 @@ int atm_mlp_adam(AtmMlp* p, float lr, float b1, float b2, float eps, float weigh
 int atm_mlp_infer(AtmMlp* p, const float* x, int32_t batch, const float* lo, const float* hi, int32_t n_hist,
                   float* y, int32_t* out_of_range, void* stream) {
   if (!p || !x || !y) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  if (batch < 0) return atm::set_error(ATM_ERR_INVALID, "batch %d", batch);
+  if (n_hist < 1 || n_hist > p->width[p->L]) return atm::set_error(ATM_ERR_INVALID, "n_hist %d", n_hist);
   cudaStream_t st = (cudaStream_t)stream;
   const int O = p->width[p->L], I0 = p->width[0];
+  if (p->tc_ok && p->form != 1) {
+    if (p->img_dirty) {
+      MlpPackArgs pa{};
+      for (int l = 0; l < p->L; ++l) {
+        pa.w[l] = reinterpret_cast<const uint16_t*>(p->wb + p->w_off[l]);
+        pa.in[l] = p->width[l];
+        pa.out[l] = p->width[l + 1];
+      }
+      pa.k0 = p->k0;
+      pa.n_pieces = p->n_pieces;
+      std::copy(p->pieces, p->pieces + p->n_pieces, pa.pieces);
+      const int n_chunks = (int)(p->img_bytes / 16);
+      mlp_pack_kernel<<<(n_chunks + 255) / 256, 256, 0, st>>>(pa, reinterpret_cast<uint4*>(p->img), n_chunks);
+      MLP_CUDA(cudaGetLastError());
+      p->img_dirty = false;
+    }
+    atm::MlpTcArgs a{};
+    a.x = x;
+    a.y = y;
+    a.oor = (lo && hi) ? out_of_range : nullptr;
+    a.lo = (lo && hi && out_of_range) ? lo : nullptr;
+    a.hi = (lo && hi && out_of_range) ? hi : nullptr;
+    a.img = p->img;
+    for (int l = 0; l < p->L; ++l) a.bias[l] = p->w + p->b_off[l];
+    a.batch = batch;
+    a.in = I0;
+    a.k0 = p->k0;
+    a.hidden = p->width[1];
+    a.out = O;
+    a.out_pad = p->out_pad;
+    a.layers = p->L;
+    a.n_hist = n_hist;
+    a.n_pieces = p->n_pieces;
+    a.status = p->status;
+    std::copy(p->pieces, p->pieces + p->n_pieces, a.pieces);
+    MLP_CUDA(atm::launch_mlp_infer_tc(a, st));
+    return ATM_OK;
+  }
   for (int b0 = 0; b0 < batch; b0 += p->max_batch) {
     const int nb = std::min(p->max_batch, batch - b0);
     if (int rc = atm_mlp_forward(p, x + (size_t)b0 * I0, nb, y + (size_t)b0 * O, stream)) return rc;
@@ -394,6 +516,31 @@ int atm_mlp_infer(AtmMlp* p, const float* x, int32_t batch, const float* lo, con
     MLP_CUDA(cudaGetLastError());
   }
   return ATM_OK;
+}
+
+int atm_mlp_set_infer_form(AtmMlp* p, int32_t form) {
+  if (!p) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  if (form < 0 || form > 2) return atm::set_error(ATM_ERR_INVALID, "form %d", form);
+  if (form == 2 && !p->tc_ok)
+    return atm::set_error(ATM_ERR_UNSUPPORTED, "this MLP's shape has no tensor-core inference form");
+  p->form = form;
+  return ATM_OK;
+}
+
+int atm_mlp_infer_form(const AtmMlp* p) {
+  if (!p) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  return p->tc_ok && p->form != 1 ? 2 : 1;
+}
+
+int atm_mlp_check(AtmMlp* p) {
+  if (!p) return atm::set_error(ATM_ERR_INVALID, "NULL argument");
+  MLP_CUDA(cudaDeviceSynchronize());
+  if (!p->status) return ATM_OK;
+  int word = 0;
+  MLP_CUDA(cudaMemcpy(&word, p->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!word) return ATM_OK;
+  MLP_CUDA(cudaMemset(p->status, 0, sizeof(int)));
+  return atm::set_error(ATM_ERR_TIMEOUT, "a bounded wait of the tensor-core inference ran out");
 }
 
 }  // extern "C"

@@ -35,6 +35,7 @@
 // error, waits (bounded) for its copies and MMAs in flight, frees its TMEM
 // and returns.
 #include <cuda.h>  // CUtensorMap and the driver enums (the encoder is fetched at run time)
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -622,6 +623,317 @@ __global__ void split_fp16_kernel(const float* __restrict__ src, int rows, int K
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// fused MLP inference on the tensor cores (the PDT surrogate's query path)
+//
+// One CTA per SM walks 128-query tiles.  Per tile the whole network runs
+// without leaving the SM: the activations stay in shared memory as BF16
+// (K-major, 128-byte swizzle: the A operand of the next layer's MMAs), the
+// accumulators in TMEM (128 lanes = the tile's queries, one column per
+// output unit).  Warp 0 streams the weights -- a packed image laid out as the
+// MMAs read it, pieces of <= 128 output rows -- through two 64 KB slots with
+// bulk copies; warp 1 issues tcgen05.mma kind::f16 (BF16 x BF16, FP32
+// accumulation); warps 2-5 (one TMEM lane per thread = one query) add the
+// bias, apply GELU, and write the next layer's operand, and after the last
+// layer form the softmax histogram and store the outputs.  The inputs enter
+// as two BF16 slices, x = hi + lo (the first layer's weights are repeated
+// for the lo slice), so the features keep about 16 bits.
+// mbarriers: full / empty per weight slot, accumulator full (MMA ->
+// epilogue), operand ready (epilogue -> MMA).  Every wait is bounded.
+// ---------------------------------------------------------------------------
+constexpr int MLP_TM = 128;                        // queries per tile = TMEM lanes = MMA M
+constexpr int MLP_THREADS = 192;                   // warp 0 weights, warp 1 MMAs, warps 2-5 epilogue
+constexpr int MLP_SLOT = 64 * 1024;                // one weight piece: <= 128 rows x 4 K blocks x 128 B
+constexpr int MLP_KB_BYTES = MLP_TM * 128;         // one K block (64 BF16) of the activations
+constexpr int MLP_ACT = 4 * MLP_KB_BYTES;          // activations: 128 x 256 BF16
+constexpr int MLP_SMEM = MLP_ACT + 2 * MLP_SLOT + 1024;
+
+// instruction descriptor: kind::f16 with A = B = BF16, D = FP32, both K-major, M = 128
+__device__ __forceinline__ uint32_t mlp_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(MLP_TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// the epilogue warps (named barrier 1, 128 threads): true when every thread's flag is
+__device__ __forceinline__ bool epi_all(bool ok) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)ok)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 128;\n" ::: "memory"); }
+
+__device__ __forceinline__ float mlp_gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752440f)); }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo_elem, float hi_elem) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x (first element) at the lower address
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane (no wait)
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(addr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+template <int K0>
+__global__ void __launch_bounds__(MLP_THREADS, 1) mlp_infer_tc_kernel(const __grid_constant__ MlpTcArgs a) {
+  static_assert(K0 == 16 || K0 == 32, "the input slices fill one K block");
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t wfull[2], wempty[2], accf, actr, drain;
+  __shared__ uint32_t tmem_holder;
+  __shared__ int abort_word;
+  volatile int* abort_flag = &abort_word;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t act = (raw + 1023) & ~1023u, slot0 = act + MLP_ACT;
+  unsigned char* act_p = smem_raw + (act - raw);  // generic pointer to the activations
+  const int n_tiles = (a.batch + MLP_TM - 1) / MLP_TM;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(smem_u32(&wfull[s]), 1);
+      mbar_init(smem_u32(&wempty[s]), 1);
+    }
+    mbar_init(smem_u32(&accf), 1);
+    mbar_init(smem_u32(&actr), MLP_TM);
+    mbar_init(smem_u32(&drain), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;\n" ::"r"(smem_u32(&tmem_holder))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_holder;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- weight producer: the pieces of every tile, in order, through two slots ----
+      int gp = 0, fills[2] = {0, 0};
+      bool stop = false;
+      for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
+        for (int p = 0; p < a.n_pieces; ++p, ++gp) {
+          const int s = gp & 1;
+          // the MMAs of this slot's previous piece have completed
+          if (gp >= 2 && !mbar_wait_or_abort(smem_u32(&wempty[s]), (uint32_t)(((gp >> 1) - 1) & 1), abort_flag)) {
+            stop = true;
+            break;
+          }
+          const uint32_t fb = smem_u32(&wfull[s]);
+          mbar_arrive_expect_tx(fb, a.pieces[p].bytes);
+          bulk_load(slot0 + (uint32_t)(s * MLP_SLOT), a.img + a.pieces[p].src, a.pieces[p].bytes, fb);
+          ++fills[s];
+        }
+      }
+      // no copy may land after the CTA leaves
+      for (int s = 0; s < 2; ++s)
+        if (fills[s]) mbar_wait(smem_u32(&wfull[s]), (uint32_t)((fills[s] - 1) & 1));
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      int gp = 0, n_act = 0;
+      bool stop = false;
+      for (int t = blockIdx.x; t < n_tiles && !stop; t += gridDim.x) {
+        int p = 0;
+        for (int l = 0; l < a.layers; ++l) {
+          // the layer's operand is in shared memory, and TMEM has been read out
+          if (!mbar_wait_or_abort(smem_u32(&actr), (uint32_t)(n_act & 1), abort_flag)) {
+            stop = true;
+            break;
+          }
+          ++n_act;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          for (; p < a.n_pieces && a.pieces[p].layer == l; ++p, ++gp) {
+            const int s = gp & 1;
+            if (!mbar_wait_or_abort(smem_u32(&wfull[s]), (uint32_t)((gp >> 1) & 1), abort_flag)) {
+              stop = true;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const MlpPiece pc = a.pieces[p];
+            const uint32_t idesc = mlp_idesc(pc.rows);
+            const uint32_t wb = slot0 + (uint32_t)(s * MLP_SLOT), kb_bytes = (uint32_t)pc.rows * 128u;
+            for (int k = 0; k < pc.k_steps; ++k) {
+              const uint32_t kb = (uint32_t)(k >> 2), off = (uint32_t)(k & 3) * 32u;  // 16 BF16 of K = 32 bytes
+              mma_bf16(tmem + (uint32_t)pc.col0, smem_desc(act + kb * MLP_KB_BYTES + off),
+                       smem_desc(wb + kb * kb_bytes + off), idesc, k > 0 ? 1u : 0u);
+            }
+            mma_commit(smem_u32(&wempty[s]));
+          }
+          if (stop) break;
+          mma_commit(smem_u32(&accf));
+        }
+      }
+      // every MMA of this thread has finished before TMEM is freed
+      mma_commit(smem_u32(&drain));
+      mbar_wait(smem_u32(&drain), 0);
+    }
+  } else {
+    // ---- epilogue: warps 2-5, TMEM lane quarter warp % 4; thread = one query of the tile ----
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int et = threadIdx.x - 64;  // 0..127
+    const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+    unsigned char* arow = act_p + row * 128;
+    const int sw = row & 7;
+    int n_acc = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+      const int m0 = t * MLP_TM;
+      const int valid = min(MLP_TM, a.batch - m0);
+      const bool live = row < valid;
+      // inputs -> K block 0 of the operand: x_hi at K [0, K0), x_lo at [K0, 2 K0); the box check
+      {
+        float xs[K0];
+        int out = 0;
+#pragma unroll
+        for (int j = 0; j < K0; ++j) {
+          xs[j] = (live && j < a.in) ? a.x[(size_t)(m0 + row) * a.in + j] : 0.f;
+          if (a.lo && live && j < a.in) out |= !(xs[j] >= a.lo[j] && xs[j] <= a.hi[j]);
+        }
+        if (a.oor && live) a.oor[m0 + row] = out;
+        uint32_t hw[K0 / 2], lw[K0 / 2];
+#pragma unroll
+        for (int j = 0; j < K0; j += 2) {
+          const __nv_bfloat16 h0 = __float2bfloat16_rn(xs[j]), h1 = __float2bfloat16_rn(xs[j + 1]);
+          hw[j / 2] = pack_bf16x2(__bfloat162float(h0), __bfloat162float(h1));
+          lw[j / 2] = pack_bf16x2(xs[j] - __bfloat162float(h0), xs[j + 1] - __bfloat162float(h1));
+        }
+#pragma unroll
+        for (int c = 0; c < K0 / 8; ++c) {
+          *reinterpret_cast<uint4*>(arow + ((c ^ sw) << 4)) =
+              make_uint4(hw[4 * c], hw[4 * c + 1], hw[4 * c + 2], hw[4 * c + 3]);
+          *reinterpret_cast<uint4*>(arow + (((c + K0 / 8) ^ sw) << 4)) =
+              make_uint4(lw[4 * c], lw[4 * c + 1], lw[4 * c + 2], lw[4 * c + 3]);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      mbar_arrive(smem_u32(&actr));
+      bool ok = true;
+      for (int l = 0; l < a.layers; ++l) {
+        int got = 0;
+        if (lane == 0) got = mbar_wait_or_abort(smem_u32(&accf), (uint32_t)(n_acc & 1), abort_flag) ? 1 : 0;
+        got = __shfl_sync(0xffffffffu, got, 0);
+        ++n_acc;
+        if (!epi_all(got != 0)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const float* bias = a.bias[l];
+        if (l < a.layers - 1) {
+          // hidden layer: bias + GELU -> BF16 operand of the next layer
+#pragma unroll 1
+          for (int c0 = 0; c0 < a.hidden; c0 += 32) {
+            uint32_t r0[16], r1[16];
+            tmem_ld16(tmem + lane_addr + (uint32_t)c0, r0);
+            tmem_ld16(tmem + lane_addr + (uint32_t)c0 + 16u, r1);
+            tmem_wait_ld();
+            uint32_t pk[16];
+#pragma unroll
+            for (int j = 0; j < 16; j += 2) {
+              pk[j / 2] = pack_bf16x2(mlp_gelu(__uint_as_float(r0[j]) + bias[c0 + j]),
+                                      mlp_gelu(__uint_as_float(r0[j + 1]) + bias[c0 + j + 1]));
+              pk[8 + j / 2] = pack_bf16x2(mlp_gelu(__uint_as_float(r1[j]) + bias[c0 + 16 + j]),
+                                          mlp_gelu(__uint_as_float(r1[j + 1]) + bias[c0 + 17 + j]));
+            }
+            unsigned char* kb = arow + (c0 >> 6) * MLP_KB_BYTES;
+            const int cc = (c0 & 63) >> 3;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              *reinterpret_cast<uint4*>(kb + (((cc + i) ^ sw) << 4)) =
+                  make_uint4(pk[4 * i], pk[4 * i + 1], pk[4 * i + 2], pk[4 * i + 3]);
+          }
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+          mbar_arrive(smem_u32(&actr));
+        } else {
+          // output layer: softmax over the first n_hist columns (online max / sum), then the outputs
+          float mx = -INFINITY, se = 0.f;
+#pragma unroll 1
+          for (int c0 = 0; c0 < a.n_hist; c0 += 16) {
+            uint32_t r[16];
+            tmem_ld16(tmem + lane_addr + (uint32_t)c0, r);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              if (c0 + j < a.n_hist) {
+                const float z = __uint_as_float(r[j]) + bias[c0 + j];
+                if (z > mx) {
+                  se = se * expf(mx - z) + 1.f;
+                  mx = z;
+                } else {
+                  se += expf(z - mx);
+                }
+              }
+            }
+          }
+          const float inv = 1.f / se;
+          // staging [valid][out] FP32 over the operand (its MMAs have completed)
+          float* stg = reinterpret_cast<float*>(act_p);
+#pragma unroll 1
+          for (int c0 = 0; c0 < a.out_pad; c0 += 16) {
+            uint32_t r[16];
+            tmem_ld16(tmem + lane_addr + (uint32_t)c0, r);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int c = c0 + j;
+              if (live && c < a.out) {
+                const float z = __uint_as_float(r[j]) + bias[c];
+                stg[row * a.out + c] = c < a.n_hist ? expf(z - mx) * inv : z;
+              }
+            }
+          }
+          asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+          epi_sync();
+          float* y = a.y + (size_t)m0 * a.out;
+          for (int i = et; i < valid * a.out; i += MLP_TM) y[i] = stg[i];
+          epi_sync();  // the next tile's inputs overwrite the staging
+        }
+      }
+      if (!ok) break;
+    }
+  }
+
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  // the MLP's own status word (atm_mlp_check), not the plans' device-wide flag
+  if (threadIdx.x == 0 && *abort_flag && a.status) atomicOr(a.status, STATUS_GEMM_WAIT);
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;\n" ::"r"(tmem) : "memory");
+  }
+}
+
 }  // namespace
 
 size_t tc_smem_bytes() { return SMEM; }
@@ -805,6 +1117,33 @@ cudaError_t launch_split_fp16(const float* src, int rows, int K, int lds, int Kp
   const size_t total = (size_t)rows * Kp;
   const int grid = (int)std::min<size_t>((total + 255) / 256, 65535 * 8);
   split_fp16_kernel<<<grid, 256, 0, st>>>(src, rows, K, lds, Kp, hi, lo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_infer_tc(const MlpTcArgs& a, cudaStream_t st) {
+  if (a.batch <= 0) return cudaSuccess;
+  if ((a.k0 != 16 && a.k0 != 32) || a.in > a.k0 || a.hidden < 64 || a.hidden > 256 || a.hidden % 64 ||
+      a.out > 128 || a.out_pad < a.out || a.out_pad % 16 || a.n_hist > a.out || a.n_pieces > kMlpMaxPieces)
+    return cudaErrorInvalidValue;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  static int sms[64] = {};
+  static bool attr_done[64][2] = {};
+  const int form = a.k0 == 16 ? 0 : 1;
+  void (*kernel)(MlpTcArgs) = form == 0 ? mlp_infer_tc_kernel<16> : mlp_infer_tc_kernel<32>;
+  if (!attr_done[dev][form]) {
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, MLP_SMEM);
+    if (e != cudaSuccess) return e;
+    attr_done[dev][form] = true;
+  }
+  if (!sms[dev]) {
+    e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  const int n_tiles = (a.batch + MLP_TM - 1) / MLP_TM;
+  kernel<<<std::min(n_tiles, sms[dev]), MLP_THREADS, MLP_SMEM, st>>>(a);
   return cudaGetLastError();
 }
 

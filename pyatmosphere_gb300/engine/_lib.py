@@ -144,6 +144,9 @@ SIGNATURES = {
     "atm_mlp_infer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p]),
+    "atm_mlp_set_infer_form": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "atm_mlp_infer_form": (ctypes.c_int, [ctypes.c_void_p]),
+    "atm_mlp_check": (ctypes.c_int, [ctypes.c_void_p]),
     "atm_tc_gemm_test": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_void_p,
                                         ctypes.c_int32, ctypes.c_void_p]),

@@ -80,6 +80,23 @@ class EngineMLP:
                                      self._stream()))
         return y, oor
 
+    @property
+    def infer_form(self) -> str:
+        """The form `infer` runs: "tensor cores" (the fused tcgen05 kernel) or "tile gemm"."""
+        rc = int(self.lib.atm_mlp_infer_form(self._h))
+        check(min(rc, 0))
+        return "tensor cores" if rc == 2 else "tile gemm"
+
+    def set_infer_form(self, form: str):
+        """"auto" (tensor cores where the shape allows), "tile gemm" or "tensor cores"."""
+        code = {"auto": 0, "tile gemm": 1, "tensor cores": 2}[form]
+        check(self.lib.atm_mlp_set_infer_form(self._h, code))
+
+    def check(self):
+        """Raises EngineError(ERR_TIMEOUT) if a bounded wait of the tensor-core inference ran out."""
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_mlp_check(self._h))
+
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             with torch.cuda.device(self.device):

@@ -88,3 +88,33 @@ def test_nonfinite_spectra_are_reported(torch_cuda, which):
     np.testing.assert_array_equal(plan.run(*dev).cpu().numpy(), clean)
     plan.check()
     plan.close()
+
+
+def test_mlp_inference_wait_budget_runs_out_then_recovers(torch_cuda):
+    """The fused tensor-core inference shares the GEMM's wait budget: with 5 ns
+    its waits for the operand and the weights run out, the CTAs drain their
+    copies and MMAs and free their TMEM, and atm_mlp_check reports
+    ATM_ERR_TIMEOUT; with the default budget the next call gives the clean bits."""
+    from pyatmosphere_gb300.engine import _lib
+    from pyatmosphere_gb300.engine.plan import set_wait_budget
+    from pyatmosphere_gb300.surrogate.mlp import EngineMLP
+    torch = torch_cuda
+    mlp = EngineMLP([12, 256, 256, 256, 67], max_batch=64)
+    mlp.init_params(5)
+    assert mlp.infer_form == "tensor cores"
+    x = torch.rand((4096, 12), device="cuda")
+    clean, _ = mlp.infer(x)
+    mlp.check()
+    clean = clean.cpu()
+    try:
+        set_wait_budget(5)
+        mlp.infer(x)
+        with pytest.raises(_lib.EngineError) as err:
+            mlp.check()
+        assert err.value.code == _lib.ERR_TIMEOUT
+    finally:
+        set_wait_budget(2_000_000_000)
+    again, _ = mlp.infer(x)
+    mlp.check()
+    assert torch.equal(again.cpu(), clean)
+    mlp.close()

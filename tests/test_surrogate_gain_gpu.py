@@ -1,0 +1,85 @@
+"""The PDT surrogate's gain over the methods without it, on a committed
+held-out set.
+
+tests/golden/surrogate_heldout.npz holds 64 parameter points drawn in the
+training box but not trained on, each with the 64-bin transmittance
+histogram of 8192 fresh realisations (N = 512, 5 screens), their first two
+moments of eta, and the histogram of the nearest training point; it was
+written by `python -m pyatmosphere_gb300.surrogate.experiment ...
+--save-heldout` on the GPU together with the shipped ensemble
+(pyatmosphere_gb300/surrogate/pdt_ensemble.npz).
+
+Each method is scored by the bin-edge KS distance to the fresh histogram:
+* the ensemble (members' mean histogram) on the points its gate answers;
+* the nearest simulated training point's histogram (the lookup a parameter
+  sweep would use without the network);
+* the beta law with the fresh realisations' own <eta>, <eta^2>
+  (theory/pdt/pdt.py:52-56 of the reference) -- an upper bound on the
+  analytic route, since a real query would have to simulate for the moments.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HELDOUT = os.path.join(ROOT, "tests", "golden", "surrogate_heldout.npz")
+ENSEMBLE = os.path.join(ROOT, "pyatmosphere_gb300", "surrogate", "pdt_ensemble.npz")
+
+
+def _edge_ks(p, q):
+    return float(np.abs(np.cumsum(p) - np.cumsum(q)).max())
+
+
+@pytest.fixture(scope="module")
+def scored():
+    import torch
+    from pyatmosphere_gb300.surrogate.baselines import _density_to_probs
+    from pyatmosphere_gb300.surrogate.ensemble import EnsembleSurrogate
+    from pyatmosphere_gb300.surrogate.model import Box, features
+    from pyatmosphere_gb300.theory import pdt as P
+    if not (os.path.exists(HELDOUT) and os.path.exists(ENSEMBLE)):
+        pytest.skip("the held-out set or the shipped ensemble is missing")
+    z = np.load(HELDOUT)
+    names = ("Cn2", "L", "w0", "wvl", "focused", "aperture", "l0", "L0")
+    params = {k: np.asarray(z[k], dtype=np.float64) for k in names}
+    ens = EnsembleSurrogate.load(ENSEMBLE, device="cuda")
+    box = Box()
+    X = torch.from_numpy(features(params, box, ens.physics)).cuda()
+    probs, _, oor, score = ens.predict(X)
+    ans = ens.answered(score, oor).cpu().numpy().astype(bool)
+    probs = probs.cpu().numpy().astype(np.float64)
+    fresh = z["fresh_hist"].astype(np.float64)
+    nn = z["nearest_train_hist"].astype(np.float64)
+    mom = z["fresh_eta_moments"]
+    n = len(fresh)
+    net = np.array([_edge_ks(probs[i], fresh[i]) for i in range(n)])
+    near = np.array([_edge_ks(nn[i], fresh[i]) for i in range(n)])
+    beta = np.array([_edge_ks(_density_to_probs(lambda x, i=i: P.beta_pdt(x, mom[i, 0], mom[i, 1])), fresh[i])
+                     for i in range(n)])
+    return {"answered": ans, "net": net, "nearest": near, "beta": beta, "oor": oor.cpu().numpy()}
+
+
+def test_heldout_points_are_inside_the_box(scored):
+    assert not scored["oor"].any()
+
+
+def test_gate_answers_most_points_within_the_ks_target(scored):
+    ans, net = scored["answered"], scored["net"]
+    assert ans.mean() >= 0.5, f"the gate answers only {ans.mean():.2f} of the held-out points"
+    # calibrated for 95 % at KS <= 0.02; 64 points leave sampling slack
+    assert (net[ans] <= 0.02).mean() >= 0.88, (net[ans] <= 0.02).mean()
+
+
+def test_network_beats_the_nearest_training_point(scored):
+    net, near = scored["net"], scored["nearest"]
+    assert np.median(net) < 0.25 * np.median(near), (np.median(net), np.median(near))
+
+
+def test_answered_network_beats_the_beta_law_tail(scored):
+    ans, net, beta = scored["answered"], scored["net"], scored["beta"]
+    assert (net[ans] <= 0.02).mean() >= (beta[ans] <= 0.02).mean(), ((net[ans] <= 0.02).mean(),
+                                                                     (beta[ans] <= 0.02).mean())
+    assert np.quantile(net[ans], 0.9) <= np.quantile(beta[ans], 0.9)
