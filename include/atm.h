@@ -63,6 +63,7 @@ extern "C" {
                                     128 bytes): the column pass then moves whole 128-byte lines; N in
                                     {512, 1024, 2048}.  Inputs and outputs of every call stay row-major. */
 #define ATM_FLAG_ROWMAJOR 128    /* keep the plan's field row-major where the tiled layout would be the default */
+#define ATM_FLAG_FFT_SCREENS 256 /* hold the workspace of atm_run_fft (one more complex64 field per realisation) */
 
 /* per-realisation doubles in measures_out (slot index).  With
  * ATM_FLAG_STEP_MEASURES, ATM_STEP_SLOTS more doubles per screen i follow the
@@ -128,7 +129,10 @@ typedef struct AtmPlanInfo {
                                  5: tiled layout, four rows per CTA with a named barrier per row,
                                  6: as 5 with twiddles formed from powers of two,
                                  7: as 4 with each thread's twiddle bases held in registers,
-                                 8: as 6 with each thread's twiddle bases held in registers */
+                                 8: as 6 with each thread's twiddle bases held in registers,
+                                 9: tiled layout, one row per CTA as 4 (tensor copies of the row's
+                                    share of each 4 x 4 block),
+                                 10: as 9 with each thread's twiddle bases held in registers */
   int32_t col_variant;        /* 0: persistent pipelined column pass, 1: one CTA per column tile,
                                  2: persistent pipelined with twiddles formed from powers of two,
                                  3: persistent with tiles loaded by TMA (loads overlap the FFTs),
@@ -218,6 +222,20 @@ int atm_measures(AtmPlan* plan, const void* field, int32_t batch, double* measur
 int atm_fft_screen(AtmPlan* plan, const float* normals, const float* amp, const void* sub_x, const void* sub_y,
                    const double* sub_mean, int32_t n_sub, int32_t batch, void* screen_out, void* stream);
 
+/* atm_run with FFT phase screens in place of the sparse-spectrum ones: per
+ * screen i the screen of atm_fft_screen is built for every realisation of the
+ * batch (its own workspace; the plan needs ATM_FLAG_FFT_SCREENS) and the beam
+ * is multiplied by exp(-i Re(screen)) between the vacuum steps, as
+ * PhaseScreensPath.generator does with FFTPhaseScreen screens
+ * (pathes.py:61-75, phase_screens.py:37-67).  Same outputs as atm_run.
+ *   normals    [batch][n][2][N][N] float32 (main-grid draws of each screen)
+ *   amp        [n][N][N] float32, each screen's sqrt(Phi_phi(|f|)) 2 pi df
+ *   sub_x, sub_y [batch][n][n_sub][N] complex64; sub_mean [batch][n][2] float64
+ * The plan's spectral grid (f_base) is not used. */
+int atm_run_fft(AtmPlan* plan, const float* normals, const float* amp, const void* sub_x, const void* sub_y,
+                const double* sub_mean, int32_t n_sub, int32_t batch, double* measures_out, void* field_out,
+                void* stream);
+
 /* Re-targets a plan to another channel of the same grid, spectral grid,
  * pupil counts and batch (source, positions, length, losses, shift and
  * pupil radii may change; the screen count may be any 1..n_screens of the
@@ -226,6 +244,23 @@ int atm_fft_screen(AtmPlan* plan, const float* normals, const float* amp, const 
  * Replaces building a new Channel for each parameter point of a sweep
  * (channels.py:17-29). */
 int atm_plan_update(AtmPlan* plan, const AtmChannelDesc* desc);
+
+/* Channel table sets: the state atm_plan_update would set (source, path
+ * geometry, losses, screen shift, pupil radii, and the device tables built
+ * from them), built once per channel for a plan of the same grid, spectral
+ * grid, pupil counts and batch.  atm_run_channel is atm_run with that state in
+ * place of the plan's own; it computes on the host nothing and copies
+ * nothing, so runs of many channels on one plan can be captured into one
+ * CUDA graph (the mixed workload runs as one graph launch).  Results equal
+ * those of a plan created (or re-targeted) for the channel.  A channel must
+ * outlive the runs that use it; atm_channel_create and atm_channel_destroy
+ * synchronise the device.  Replaces building a Channel per parameter point of
+ * a mixed workload (channels.py:17-29). */
+typedef struct AtmChannel AtmChannel;
+int atm_channel_create(AtmPlan* plan, const AtmChannelDesc* desc, AtmChannel** channel);
+int atm_channel_destroy(AtmChannel* channel);
+int atm_run_channel(AtmPlan* plan, AtmChannel* channel, const float* rho, const float* theta, const void* value,
+                    int32_t batch, double* measures_out, void* field_out, float* mean_intensity, void* stream);
 
 /* Seeded spectra on the device: rho, theta [batch][n][P] float32 and value
  * [batch][n][P] complex64 for realisations first_realisation .. +batch-1,
@@ -289,10 +324,10 @@ int atm_tc_gemm_test(const float* A, const float* B, int32_t S, int32_t M, int32
 
 /* Times the launch variants of the FFT passes on this plan's own workspace
  * (`batch` realisations, `repeats` timed launches each after one warm-up)
- * and keeps the fastest: row-pass variant (0..4 and 7; a tiled plan: 5, 6, 8),
+ * and keeps the fastest: row-pass variant (0..4 and 7; a tiled plan: 5, 6, 8, 9, 10),
  * column tile (2..16 columns, at most 512 threads per CTA; a tiled plan: 4)
  * and column-pass variant (0..4 and 7; a tiled plan: 5, 6, 8, 9).  The forms
- * that build twiddles as products of powers of two (row 4, 6, 7, 8; column
+ * that build twiddles as products of powers of two (row 4, 6..10; column
  * 2, 7, 8, 9) round differently from the table forms (FP32 round-off, well
  * inside the 1e-4 field bound); the results are otherwise the same.  Overwrites the
  * plan's field / screen workspace (zeroes) and blocks until the timing
@@ -311,7 +346,7 @@ int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* s
 
 /* Sets the launch choices atm_autotune makes by hand: row-pass variant 0..4
  * or 7, column tile 2/4/8/16 with at most 512 threads per CTA, column-pass
- * variant 0..4 or 7; a tiled plan (ATM_FLAG_TILED) takes row 5, 6 or 8,
+ * variant 0..4 or 7; a tiled plan (ATM_FLAG_TILED) takes row 5, 6, 8, 9 or 10,
  * column tile 4 and column 5, 6, 8 or 9.  Results do not change, except for
  * FP32 round-off between the table-twiddle and product-twiddle forms.  No
  * reference counterpart. */

@@ -45,19 +45,18 @@ class Channel:
             return False
         if isinstance(self.path, VacuumPath):
             return True
-        return isinstance(self.path, PhaseScreensPath) and all(
-            type(s) is SSPhaseScreen for s in self.path.phase_screens)
+        from .engine.runner import screen_kind
+        return isinstance(self.path, PhaseScreensPath) and (
+            all(type(s) is SSPhaseScreen for s in self.path.phase_screens) or screen_kind(self.path) == "fft")
 
     def _run_fused(self, shift=(0, 0), wind=False, length=None, path_output_loss=True):
         import torch
-        from .engine.runner import draw_channel_spectra, get_plan, to_device
+        from .engine.runner import get_plan, run_single, screen_kind
+        if screen_kind(self.path) == "fft" and (tuple(shift) != (0, 0) or wind):
+            raise TypeError("FFT phase screens take no shift / wind")
         plan = get_plan(self, batch=1, shift=shift, path_output_loss=path_output_loss, length=length)
         field = torch.empty((1, plan.N, plan.N), dtype=torch.complex64, device=plan.device)
-        spectra = (None, None, None)
-        if plan.n_screens:
-            self.path.init_phase_screens()
-            spectra = to_device(*draw_channel_spectra(self, 1, wind=wind, clear=False))
-        plan.run(*spectra, field_out=field)
+        run_single(self, plan, field, wind=wind)
         return field[0]
 
     def run(self, pupil=True, *args, **kwargs):

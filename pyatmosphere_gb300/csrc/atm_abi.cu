@@ -163,6 +163,7 @@ struct AtmPlan {
   DevBuf gy_t, hx_t;     // 1-D phases in turns, folded into the GEMM output (TMA form)
   DevBuf step_partials, step_center;  // per-step measures (ATM_FLAG_STEP_MEASURES)
   DevBuf status;                      // device status word (atm::STATUS_*), read by atm_plan_check
+  DevBuf scr;                         // FFT-screen workspace (ATM_FLAG_FFT_SCREENS)
   bool step_meas = false;
   int step_slot0 = 0;
   atm::TcPlan* tcp = nullptr;  // TMA descriptors of the screen GEMM (null: cp.async form)
@@ -178,6 +179,29 @@ struct AtmPlan {
     for (auto* b : bufs)
       if (b->p) cudaFree(b->p);
     for (auto e : ev) cudaEventDestroy(e);
+  }
+};
+
+// the per-channel state of a plan: what atm_plan_update changes (source, path
+// geometry, losses, screen shift, pupil radii) and the device tables built
+// from it.  An AtmChannel holds one such state, built once; atm_run_channel
+// swaps it into the plan for one run.
+struct ChannelState {
+  int n = 0;
+  double wvl = 0, w0 = 0, F0 = 0, length = 0, losses_db = 0, kw = 0, sx = 0, sy = 0;
+  int path_output_loss = 0, source_kind = 0;
+  std::vector<double> positions, dz, tracked_radius;
+  std::vector<float> loss;
+  float final_loss = 1.f;
+  DevBuf ay, ax, hy, hx, pupil_rows, tracked_r;
+};
+
+struct AtmChannel {
+  AtmPlan* plan = nullptr;
+  ChannelState st;
+  ~AtmChannel() {
+    for (DevBuf* b : {&st.ay, &st.ax, &st.hy, &st.hx, &st.pupil_rows, &st.tracked_r})
+      if (b->p) cudaFree(b->p);
   }
 };
 
@@ -377,6 +401,50 @@ int validate(const AtmChannelDesc* d) {
   return ATM_OK;
 }
 
+// exchanges the plan's per-channel state with `c` (device buffers by pointer)
+void swap_state(AtmPlan* pl, ChannelState& c) {
+  std::swap(pl->n, c.n);
+  std::swap(pl->wvl, c.wvl);
+  std::swap(pl->w0, c.w0);
+  std::swap(pl->F0, c.F0);
+  std::swap(pl->length, c.length);
+  std::swap(pl->losses_db, c.losses_db);
+  std::swap(pl->kw, c.kw);
+  std::swap(pl->sx, c.sx);
+  std::swap(pl->sy, c.sy);
+  std::swap(pl->path_output_loss, c.path_output_loss);
+  std::swap(pl->source_kind, c.source_kind);
+  std::swap(pl->positions, c.positions);
+  std::swap(pl->dz, c.dz);
+  std::swap(pl->tracked_radius, c.tracked_radius);
+  std::swap(pl->loss, c.loss);
+  std::swap(pl->final_loss, c.final_loss);
+  std::swap(pl->ay, c.ay);
+  std::swap(pl->ax, c.ax);
+  std::swap(pl->hy, c.hy);
+  std::swap(pl->hx, c.hx);
+  std::swap(pl->pupil_rows, c.pupil_rows);
+  std::swap(pl->tracked_r, c.tracked_r);
+}
+
+// a descriptor the plan can be re-targeted to (atm_plan_update, atm_channel_create)
+int check_retarget(const AtmPlan* pl, const AtmChannelDesc* d) {
+  if (int rc = validate(d)) return rc;
+  if (int rc = check_device(pl)) return rc;
+  if (d->resolution != pl->N || d->delta != pl->delta || d->n_pupils != pl->n_pupils ||
+      d->n_tracked != pl->n_tracked || d->batch > pl->B || d->cheb_cut != pl->cheb_cut)
+    return fail(ATM_ERR_INVALID, "a re-targeted plan keeps grid, pupil counts, batch and cheb_cut");
+  if (d->n_screens > pl->n_alloc || (pl->n_alloc > 0) != (d->n_screens > 0))
+    return fail(ATM_ERR_INVALID, "a re-targeted plan takes 1..%d screens (the creating descriptor's count)",
+                pl->n_alloc);
+  if (pl->n_alloc > 0) {
+    if (d->points != pl->P) return fail(ATM_ERR_INVALID, "a re-targeted plan keeps the spectral grid");
+    for (int p = 0; p < pl->P; ++p)
+      if (d->f_base[p] != pl->f_base[p]) return fail(ATM_ERR_INVALID, "a re-targeted plan keeps the spectral grid");
+  }
+  return ATM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -432,9 +500,9 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
   // tiled layout: opt-in by flag; the tiled passes write one measure partial per row
   pl->tiled = atm::tiled_supported(pl->N) && (d->flags & ATM_FLAG_TILED) && !(d->flags & ATM_FLAG_ROWMAJOR);
   if (pl->tiled) {
-    // product twiddles from the table's bases: the tiled forms' registers (one CTA of
-    // 17 warps per SM) leave no room for bases held in registers at N = 2048
-    pl->row_variant = 6;
+    // one row per CTA (tensor copies of the row's share of each block) and the column
+    // groups, both with product twiddles from the table's bases
+    pl->row_variant = 9;
     pl->col_variant = 9;
     pl->col_tile = 4;
   }
@@ -505,6 +573,12 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
       return rc;
     }
   }
+  if (pl->n > 0 && (d->flags & ATM_FLAG_FFT_SCREENS)) {
+    if ((rc = dev_alloc(pl->scr, B * plane * sizeof(float2), v))) {
+      delete pl;
+      return rc;
+    }
+  }
   if (pl->n > 0) {
     if ((rc = dev_alloc(pl->fbase, (size_t)pl->P * sizeof(float), v))) {
       delete pl;
@@ -537,22 +611,50 @@ int atm_plan_create(const AtmChannelDesc* d, AtmPlan** out) {
 
 int atm_plan_update(AtmPlan* pl, const AtmChannelDesc* d) {
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
-  if (int rc = validate(d)) return rc;
-  if (int rc = check_device(pl)) return rc;
-  if (d->resolution != pl->N || d->delta != pl->delta || d->n_pupils != pl->n_pupils ||
-      d->n_tracked != pl->n_tracked || d->batch > pl->B || d->cheb_cut != pl->cheb_cut)
-    return fail(ATM_ERR_INVALID, "atm_plan_update keeps grid, pupil counts, batch and cheb_cut");
-  if (d->n_screens > pl->n_alloc || (pl->n_alloc > 0) != (d->n_screens > 0))
-    return fail(ATM_ERR_INVALID, "atm_plan_update takes 1..%d screens (the creating descriptor's count)", pl->n_alloc);
-  if (pl->n > 0) {
-    if (d->points != pl->P) return fail(ATM_ERR_INVALID, "atm_plan_update keeps the spectral grid");
-    for (int p = 0; p < pl->P; ++p)
-      if (d->f_base[p] != pl->f_base[p]) return fail(ATM_ERR_INVALID, "atm_plan_update keeps the spectral grid");
-  }
+  if (int rc = check_retarget(pl, d)) return rc;
   ATM_CUDA(cudaDeviceSynchronize());  // tables may still be read by enqueued work
   pl->n = d->n_screens;
   set_geometry(pl, d);
   return plan_tables(pl, d);
+}
+
+int atm_channel_create(AtmPlan* pl, const AtmChannelDesc* d, AtmChannel** out) {
+  if (!out) return fail(ATM_ERR_INVALID, "channel output pointer is NULL");
+  *out = nullptr;
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_retarget(pl, d)) return rc;
+  auto* ch = new AtmChannel();
+  ch->plan = pl;
+  std::vector<DevBuf*> owned;  // the channel frees its own buffers
+  ChannelState& c = ch->st;
+  int rc = dev_alloc(c.ay, pl->ay.bytes, owned);
+  if (!rc) rc = dev_alloc(c.ax, pl->ax.bytes, owned);
+  if (!rc) rc = dev_alloc(c.hy, pl->hy.bytes, owned);
+  if (!rc) rc = dev_alloc(c.hx, pl->hx.bytes, owned);
+  if (!rc) rc = dev_alloc(c.pupil_rows, pl->pupil_rows.bytes, owned);
+  if (!rc) rc = dev_alloc(c.tracked_r, pl->tracked_r.bytes, owned);
+  if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = fail(ATM_ERR_CUDA, "cudaDeviceSynchronize failed");
+  if (!rc) {
+    // build the channel's tables in the plan's place, then give the plan its own state back
+    swap_state(pl, c);
+    pl->n = d->n_screens;
+    set_geometry(pl, d);
+    rc = plan_tables(pl, d);
+    swap_state(pl, c);
+  }
+  if (rc) {
+    delete ch;
+    return rc;
+  }
+  *out = ch;
+  return ATM_OK;
+}
+
+int atm_channel_destroy(AtmChannel* ch) {
+  if (!ch) return ATM_OK;
+  cudaDeviceSynchronize();  // runs may still read its tables
+  delete ch;
+  return ATM_OK;
 }
 
 int atm_plan_destroy(AtmPlan* pl) {
@@ -760,29 +862,15 @@ int finish_measures(AtmPlan* pl, int batch, double* measures, cudaStream_t st) {
   return ATM_OK;
 }
 
-int check_device(const AtmPlan* pl) {
-  int dev = -1;
-  cudaGetDevice(&dev);
-  if (dev != pl->device) return fail(ATM_ERR_INVALID, "plan belongs to device %d, current device is %d", pl->device, dev);
-  return ATM_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value, int32_t batch, double* measures,
-            void* field_out, float* mean_intensity, void* stream) {
-  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
-  if (int rc = check_device(pl)) return rc;
-  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
-  if (!measures) return fail(ATM_ERR_INVALID, "measures_out is NULL");
-  if (pl->n > 0 && (!rho || !theta || !value)) return fail(ATM_ERR_INVALID, "spectra pointers are NULL");
-  cudaStream_t st = (cudaStream_t)stream;
+// the split-step loop of a run: per screen, make_screen(i) leaves the screen in
+// pl->phi (turns; `folded`: the whole phase, else the GEMM part beside Py / Px),
+// then the row pass applies it between the vacuum steps' FFTs and the column
+// pass the transfer function; the last row pass measures
+template <class MakeScreen>
+int propagate(AtmPlan* pl, int batch, MakeScreen&& make_screen, bool folded, double* measures, void* field_out,
+              float* mean_intensity, cudaStream_t st) {
   const int N = pl->N, n = pl->n;
-
   atm::RowArgs ra = row_args(pl, mean_intensity, field_out);
-
   atm::ColArgs ca{};
   ca.field = (float2*)pl->field.p;
   ca.tw = (const float2*)pl->tw.p;
@@ -791,10 +879,9 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
 
   bool measured = false;
   for (int i = 0; i < n; ++i) {
-    atm::ScreenArgs s = screen_args(pl, rho, theta, value, i);
-    if (int rc = run_screen(pl, s, batch, true, st)) return rc;
+    if (int rc = make_screen(i)) return rc;
     int flags = (i == 0 ? atm::ROW_GEN : (pl->dz[i] > 0 ? atm::ROW_INV : 0)) | atm::ROW_PHASOR |
-                (folds(pl) ? atm::ROW_FOLDED : 0);
+                (folded ? atm::ROW_FOLDED : 0);
     const bool next_vac = pl->dz[i + 1] > 0;
     if (next_vac) {
       flags |= atm::ROW_FWD | atm::ROW_STORE;
@@ -847,6 +934,101 @@ int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value
     ATM_CUDA(atm::launch_finalize(batch, fa, st));
   }
   return ATM_OK;
+}
+
+int check_device(const AtmPlan* pl) {
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != pl->device) return fail(ATM_ERR_INVALID, "plan belongs to device %d, current device is %d", pl->device, dev);
+  return ATM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int atm_run(AtmPlan* pl, const float* rho, const float* theta, const void* value, int32_t batch, double* measures,
+            void* field_out, float* mean_intensity, void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
+  if (!measures) return fail(ATM_ERR_INVALID, "measures_out is NULL");
+  if (pl->n > 0 && (!rho || !theta || !value)) return fail(ATM_ERR_INVALID, "spectra pointers are NULL");
+  cudaStream_t st = (cudaStream_t)stream;
+  auto ss_screen = [&](int i) { return run_screen(pl, screen_args(pl, rho, theta, value, i), batch, true, st); };
+  return propagate(pl, batch, ss_screen, folds(pl), measures, field_out, mean_intensity, st);
+}
+
+int atm_run_fft(AtmPlan* pl, const float* normals, const float* amp, const void* sub_x, const void* sub_y,
+                const double* sub_mean, int32_t n_sub, int32_t batch, double* measures, void* field_out,
+                void* stream) {
+  if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
+  if (int rc = check_device(pl)) return rc;
+  if (batch < 1 || batch > pl->B) return fail(ATM_ERR_INVALID, "batch %d out of range [1, %d]", batch, pl->B);
+  if (!measures) return fail(ATM_ERR_INVALID, "measures_out is NULL");
+  if (pl->n < 1 || !pl->scr.p) return fail(ATM_ERR_INVALID, "atm_run_fft needs a plan with screens and ATM_FLAG_FFT_SCREENS");
+  if (!normals || !amp || !sub_mean) return fail(ATM_ERR_INVALID, "NULL screen input");
+  if (n_sub < 0 || (n_sub > 0 && (!sub_x || !sub_y))) return fail(ATM_ERR_INVALID, "bad subharmonic tables");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = pl->N, n = pl->n;
+  const size_t plane = (size_t)N * N;
+  auto fft_screen = [&](int i) -> int {
+    atm::FftScreenArgs fa{};
+    fa.normals = normals + (size_t)i * 2 * plane;
+    fa.nrm_stride = (size_t)n * 2 * plane;
+    fa.amp = amp + (size_t)i * plane;
+    fa.sub_x = n_sub ? (const float2*)sub_x + (size_t)i * n_sub * N : nullptr;
+    fa.sub_y = n_sub ? (const float2*)sub_y + (size_t)i * n_sub * N : nullptr;
+    fa.sub_stride = (size_t)n * n_sub * N;
+    fa.sub_mean = sub_mean + 2 * i;
+    fa.mean_stride = 2 * n;
+    fa.n_sub = n_sub;
+    fa.N = N;
+    fa.field = (float2*)pl->scr.p;
+    fa.phi = (float*)pl->phi.p;
+    {
+      Prof p(pl, ATM_KIND_SCREEN_PREP, st);
+      ATM_CUDA(atm::launch_fft_screen_spectrum(batch, fa, st));
+    }
+    // the screen's inverse 2-D transform on its own (row-major) workspace
+    atm::RowArgs ra{};
+    ra.field = (float2*)pl->scr.p;
+    ra.tw = (const float2*)pl->tw.p;
+    ra.loss = 1.f;
+    ra.delta = (float)pl->delta;
+    ra.delta64 = pl->delta;
+    ra.flags = atm::ROW_INV | atm::ROW_STORE;
+    ra.variant = pl->tiled ? 3 : pl->row_variant;
+    ra.status = (int*)pl->status.p;
+    {
+      Prof p(pl, ATM_KIND_ROW_PASS, st);
+      ATM_CUDA(atm::launch_row_pass(N, batch, ra, st));
+    }
+    atm::ColArgs ca{};
+    ca.field = (float2*)pl->scr.p;
+    ca.tw = (const float2*)pl->tw.p;
+    ca.variant = pl->tiled ? 4 : pl->col_variant;
+    ca.inv_only = 1;
+    ca.status = (int*)pl->status.p;
+    {
+      Prof p(pl, ATM_KIND_COL_PASS, st);
+      ATM_CUDA(atm::launch_col_pass(N, batch, pl->tiled ? 0 : pl->col_tile, ca, st));
+    }
+    Prof p(pl, ATM_KIND_SCREEN_EVAL, st);
+    ATM_CUDA(atm::launch_fft_screen_finish(batch, fa, st));
+    return ATM_OK;
+  };
+  return propagate(pl, batch, fft_screen, true, measures, field_out, nullptr, st);
+}
+
+int atm_run_channel(AtmPlan* pl, AtmChannel* ch, const float* rho, const float* theta, const void* value,
+                    int32_t batch, double* measures, void* field_out, float* mean_intensity, void* stream) {
+  if (!pl || !ch) return fail(ATM_ERR_INVALID, "plan / channel is NULL");
+  if (ch->plan != pl) return fail(ATM_ERR_INVALID, "the channel was built for another plan");
+  swap_state(pl, ch->st);
+  const int rc = atm_run(pl, rho, theta, value, batch, measures, field_out, mean_intensity, stream);
+  swap_state(pl, ch->st);
+  return rc;
 }
 
 int atm_measures(AtmPlan* pl, const void* field, int32_t batch, double* measures, void* stream) {
@@ -933,7 +1115,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   double best_row = -1.0;
   int row_variant = 0;
   // a tiled plan chooses among the tiled forms only (the others do not know its layout)
-  const std::vector<int> row_forms = pl->tiled ? std::vector<int>{5, 6, 8} : std::vector<int>{0, 1, 2, 3, 4, 7};
+  const std::vector<int> row_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9, 10} : std::vector<int>{0, 1, 2, 3, 4, 7};
   for (int v : row_forms) {
     ra.variant = v;
     const double ms = time_it([&] { return atm::launch_row_pass(N, batch, ra, st); });
@@ -986,8 +1168,8 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
   if (!pl) return fail(ATM_ERR_INVALID, "plan is NULL");
   if (pl->tiled) {
     // a tiled plan's field is only understood by the tiled forms
-    if (row_variant != 5 && row_variant != 6 && row_variant != 8)
-      return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5, 6 or 8", row_variant);
+    if (row_variant != 5 && row_variant != 6 && row_variant != 8 && row_variant != 9 && row_variant != 10)
+      return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5, 6, 8, 9 or 10", row_variant);
     if ((col_variant != 5 && col_variant != 6 && col_variant != 8 && col_variant != 9) || col_tile != 4)
       return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5, 6, 8 or 9 with col_tile 4");
     pl->row_variant = row_variant;
@@ -1074,6 +1256,10 @@ int atm_fft_screen(AtmPlan* pl, const float* normals, const float* amp, const vo
   fa.N = pl->N;
   fa.field = (float2*)pl->field.p;
   fa.out = (float2*)screen_out;
+  fa.phi = nullptr;
+  fa.nrm_stride = 2 * (size_t)pl->N * pl->N;
+  fa.sub_stride = (size_t)n_sub * pl->N;
+  fa.mean_stride = 2;
   ATM_CUDA(atm::launch_fft_screen_spectrum(batch, fa, st));
   atm::RowArgs ra{};
   ra.field = (float2*)pl->field.p;

@@ -110,7 +110,11 @@ struct FftScreenArgs {
   const double* sub_mean;   // [B][2] mean of the subharmonic part (re, im)
   int n_sub, N;
   float2* field;            // [B][N][N] workspace
-  float2* out;              // [B][N][N] complex screen
+  float2* out;              // [B][N][N] complex screen (when phi is null)
+  float* phi;               // [B][N][N] the screen's real part in turns (Re / 2 pi), or null
+  size_t nrm_stride;        // floats between realisations in normals (2 N^2 for one screen each)
+  size_t sub_stride;        // float2 between realisations in sub_x / sub_y (n_sub N for one screen each)
+  int mean_stride;          // doubles between realisations in sub_mean (2 for one screen each)
 };
 
 // one high-frequency spectral term, phases as 64-bit binary fractions of a turn
@@ -222,6 +226,10 @@ bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int
 // by_rows: 3-D {32, N^2/16, B}, consecutive blocks of a block row (boxes of box_blocks blocks);
 // otherwise 3-D, one block column (boxes of box_blocks blocks down the column)
 bool encode_tiled_field(void* map, const float2* field, int N, int B, bool by_rows, int box_blocks);
+// tensor map of a tiled field [B][N][N] as {32 floats of a block, N^2/16 blocks, B} with boxes
+// of 8 floats (one row's 4 complex64 of a block) x box_blocks blocks, no swizzle: one row of a
+// block row per copy, landing as that row in row-major order
+bool encode_tiled_rows(void* map, const float2* field, int N, int B, int box_blocks);
 // fold_y [S][M] / fold_x [S][Nn] (nullable, turns): added to every output
 cudaError_t launch_tc_gemm_tma(const TcPlan* p, int S, float* out, float scale, const float* fold_y,
                                const float* fold_x, int* status, cudaStream_t st);

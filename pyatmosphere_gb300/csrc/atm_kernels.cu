@@ -322,7 +322,8 @@ template <int N, int ROWS>
 struct RowPipe {
   static constexpr size_t STAGE = (size_t)ROWS * Padded<N>::value * sizeof(float2);
   static constexpr size_t TW = (size_t)Padded<N>::value * sizeof(float2);
-  static constexpr size_t SMEM = 2 * STAGE + TW;
+  static constexpr size_t SMEM = 2 * STAGE + TW + 128;  // + slack: stages start on 128 bytes
+  static_assert(STAGE % 128 == 0, "tensor copies land on 128-byte boundaries");
 };
 
 // ROWS rows per CTA: RowRows<N> (about 256 threads) or 1 (N/16 threads, so
@@ -331,10 +332,13 @@ struct RowPipe {
 // moves each next row with one bulk copy (TMA) onto an mbarrier, so the
 // other threads never hold for the memory system and the copies overlap the
 // FFTs (bounded waits: on timeout the CTA records an error, waits for its
-// copies in flight and returns).
-template <int N, int ROWS, int BULK, int TWREC = 0>
+// copies in flight and returns).  TILED = 1 (with BULK): the field may be in
+// the tiled layout (a.tiled): a row then arrives by tensor copies of its
+// 32-byte share of each 4 x 4 block (map `rows`: 8 floats x up to 256 blocks,
+// no swizzle), which land as the row-major row, and is stored into its blocks.
+template <int N, int ROWS, int BULK, int TWREC = 0, int TILED = 0>
 __global__ void __launch_bounds__(ROWS * (N / 16), (ROWS * (N / 16) <= 128) ? 4 : ((ROWS * (N / 16) <= 256) ? 2 : 1))
-row_pass_pipe_kernel(RowArgs a, int n_items) {
+row_pass_pipe_kernel(const __grid_constant__ CUtensorMap rows, RowArgs a, int n_items) {
   constexpr int T = N / 16;
   constexpr int P = Padded<N>::value;
   constexpr int NT = ROWS * T;
@@ -346,8 +350,12 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
   const bool load_field = !(flags & ROW_GEN);
   const bool load_phi = (flags & ROW_PHASOR) != 0;
 
-  auto fbuf = [&](int s) { return reinterpret_cast<float2*>(smem_raw + s * RowPipe<N, ROWS>::STAGE); };
-  float2* tws = reinterpret_cast<float2*>(smem_raw + 2 * RowPipe<N, ROWS>::STAGE);
+  unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
+  auto fbuf = [&](int s) { return reinterpret_cast<float2*>(sbase + s * RowPipe<N, ROWS>::STAGE); };
+  float2* tws = reinterpret_cast<float2*>(sbase + 2 * RowPipe<N, ROWS>::STAGE);
+  const bool in_tiled = TILED && (a.tiled & TILE_IN) && load_field;
+  float2* const dst_base = (a.store_out && a.out) ? a.out : a.field;
+  const bool out_tiled = TILED && (a.tiled & TILE_OUT) && dst_base == a.field;
   TwBases<N> tb;
   if constexpr (TWREC == 2)
     load_twiddle_bases<N>(tb, a.tw, t);
@@ -376,12 +384,27 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
                    "r"((uint32_t)(ROWS * N * sizeof(float2)))
                    : "memory");
-      for (int row = 0; row < ROWS; ++row)
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                (uint32_t)__cvta_generic_to_shared(dst + row * P)),
-            "l"(src + (size_t)row * N), "r"((uint32_t)(N * sizeof(float2))), "r"(bar)
-            : "memory");
+      if (in_tiled) {
+        // row y = block row y / 4, float offset 8 (y % 4) inside each block (32-byte aligned)
+        constexpr int BOXB = (N / 4 < 256) ? N / 4 : 256;
+        for (int row = 0; row < ROWS; ++row) {
+          const int y = y0 + row;
+          for (int b = 0; b < N / 4 / BOXB; ++b)
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                "%3, %4}], [%5];\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst + row * P + b * BOXB * 4)),
+                "l"(reinterpret_cast<uint64_t>(&rows)), "r"(8 * (y & 3)), "r"((y >> 2) * (N / 4) + b * BOXB), "r"(r),
+                "r"(bar)
+                : "memory");
+        }
+      } else {
+        for (int row = 0; row < ROWS; ++row)
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                  (uint32_t)__cvta_generic_to_shared(dst + row * P)),
+              "l"(src + (size_t)row * N), "r"((uint32_t)(N * sizeof(float2))), "r"(bar)
+              : "memory");
+      }
       pending[s] = true;
     } else {
       for (int c = tid; c < ROWS * N / 2; c += NT) {
@@ -467,9 +490,18 @@ row_pass_pipe_kernel(RowArgs a, int n_items) {
         fft_dev<N, -1, 0, 1, TWREC>(v, sm, t, tws);
     }
     if (flags & ROW_STORE) {
-      float2* dst = (a.store_out && a.out) ? a.out : a.field;
+      if (out_tiled) {
+        // element x of row y: block (y / 4, x / 4), slot 4 (y % 4) + x % 4
+        float2* d = dst_base + (size_t)r * N * N + (size_t)(y >> 2) * 4 * N + (y & 3) * 4;
 #pragma unroll
-      for (int m = 0; m < 16; ++m) dst[rowoff + t + m * T] = v[m];
+        for (int m = 0; m < 16; ++m) {
+          const int x = t + m * T;
+          d[(x >> 2) * 16 + (x & 3)] = v[m];
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) dst_base[rowoff + t + m * T] = v[m];
+      }
     }
     if (flags & ROW_MEAS) measure_row<N, ROWS>(a, v, t, y, r, rb, NRB);
     if constexpr (BULK) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // refilled by TMA
@@ -870,17 +902,23 @@ static cudaError_t row_tiled_launch(int B, const RowArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int N, int ROWS, int BULK = 0, int TWREC = 0>
+template <int N, int ROWS, int BULK = 0, int TWREC = 0, int TILED = 0>
 static cudaError_t row_pipe_launch(int B, const RowArgs& a, cudaStream_t st) {
+  alignas(128) CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  if constexpr (TILED) {
+    const bool in_tiled = (a.tiled & TILE_IN) && !(a.flags & ROW_GEN);
+    if (in_tiled && !encode_tiled_rows(&map, a.field, N, B, (N / 4 < 256) ? N / 4 : 256)) return cudaErrorNotSupported;
+  }
   static LaunchCache cache;
   const int threads = ROWS * (N / 16);
   const size_t smem = RowPipe<N, ROWS>::SMEM;
   int grid_max = 0;
-  cudaError_t e = cache.get(row_pass_pipe_kernel<N, ROWS, BULK, TWREC>, threads, smem, &grid_max);
+  cudaError_t e = cache.get(row_pass_pipe_kernel<N, ROWS, BULK, TWREC, TILED>, threads, smem, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / ROWS);
   const int grid = std::max(1, std::min(n_items, grid_max));
-  row_pass_pipe_kernel<N, ROWS, BULK, TWREC><<<grid, threads, smem, st>>>(a, n_items);
+  row_pass_pipe_kernel<N, ROWS, BULK, TWREC, TILED><<<grid, threads, smem, st>>>(map, a, n_items);
   return cudaGetLastError();
 }
 
@@ -907,6 +945,12 @@ static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
   if constexpr (N == 512 || N == 1024 || N == 2048) {
+    if (a.variant == 9 || a.variant == 10) {
+      // the tiled layout one row per CTA (the form of 4 / 7): tensor copies of a row's
+      // share of each block in, stores into the blocks out
+      if (!field_ok || !phi_ok) return cudaErrorInvalidValue;
+      return a.variant == 9 ? row_pipe_launch<N, 1, 1, 1, 1>(B, a, st) : row_pipe_launch<N, 1, 1, 2, 1>(B, a, st);
+    }
     if (a.variant == 5 || a.variant == 6 || a.variant == 8) {
       // the tiled forms: the only forms that read or write the tiled layout
       // (8: twiddles in registers)
@@ -2149,7 +2193,7 @@ __global__ void fft_screen_spectrum_kernel(FftScreenArgs a) {
   const size_t plane = (size_t)N * N, o = (size_t)ky * N + kx;
   const float sgn = ((kx + ky) & 1) ? -1.f : 1.f;
   const float amp = a.amp[o] * sgn;
-  const float* nr = a.normals + (size_t)r * 2 * plane;
+  const float* nr = a.normals + (size_t)r * a.nrm_stride;
   a.field[(size_t)r * plane + o] = make_float2(nr[o] * amp, nr[plane + o] * amp);
 }
 
@@ -2166,14 +2210,17 @@ __global__ void fft_screen_finish_kernel(FftScreenArgs a) {
   const size_t plane = (size_t)N * N, o = (size_t)y * N + x;
   float2 v = a.field[(size_t)r * plane + o];
   if ((x + y) & 1) v = make_float2(-v.x, -v.y);
-  const float2* sx = a.sub_x + (size_t)r * a.n_sub * N;
-  const float2* sy = a.sub_y + (size_t)r * a.n_sub * N;
+  const float2* sx = a.sub_x + (size_t)r * a.sub_stride;
+  const float2* sy = a.sub_y + (size_t)r * a.sub_stride;
   float2 acc = make_float2(0.f, 0.f);
   for (int j = 0; j < a.n_sub; ++j) acc = cadd(acc, cmul(sx[(size_t)j * N + x], sy[(size_t)j * N + y]));
   v = cadd(v, acc);
-  v.x -= (float)a.sub_mean[2 * r];
-  v.y -= (float)a.sub_mean[2 * r + 1];
-  a.out[(size_t)r * plane + o] = v;
+  v.x -= (float)a.sub_mean[(size_t)r * a.mean_stride];
+  v.y -= (float)a.sub_mean[(size_t)r * a.mean_stride + 1];
+  if (a.phi)
+    a.phi[(size_t)r * plane + o] = v.x * 0.15915494309189533577f;  // radians -> turns
+  else
+    a.out[(size_t)r * plane + o] = v;
 }
 
 cudaError_t launch_fft_screen_finish(int B, const FftScreenArgs& a, cudaStream_t st) {

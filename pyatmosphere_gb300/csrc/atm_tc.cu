@@ -643,7 +643,8 @@ __global__ void split_fp16_kernel(const float* __restrict__ src, int rows, int K
 // epilogue), operand ready (epilogue -> MMA).  Every wait is bounded.
 // ---------------------------------------------------------------------------
 constexpr int MLP_TM = 128;                        // queries per tile = TMEM lanes = MMA M
-constexpr int MLP_THREADS = 192;                   // warp 0 weights, warp 1 MMAs, warps 2-5 epilogue
+constexpr int MLP_EPI = 512;                       // epilogue threads: 4 column slices x 128 rows
+constexpr int MLP_THREADS = 64 + MLP_EPI;          // warp 0 weights, warp 1 MMAs, warps 2-17 epilogue
 constexpr int MLP_SLOT = 64 * 1024;                // one weight piece: <= 128 rows x 4 K blocks x 128 B
 constexpr int MLP_KB_BYTES = MLP_TM * 128;         // one K block (64 BF16) of the activations
 constexpr int MLP_ACT = 4 * MLP_KB_BYTES;          // activations: 128 x 256 BF16
@@ -669,17 +670,17 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
-// the epilogue warps (named barrier 1, 128 threads): true when every thread's flag is
+// the epilogue warps (named barrier 1, MLP_EPI threads): true when every thread's flag is
 __device__ __forceinline__ bool epi_all(bool ok) {
   uint32_t r;
   asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, 512, p;\n selp.u32 %0, 1, 0, q;\n}\n"
       : "=r"(r)
       : "r"((uint32_t)ok)
       : "memory");
   return r != 0;
 }
-__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 128;\n" ::: "memory"); }
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 512;\n" ::: "memory"); }
 
 __device__ __forceinline__ float mlp_gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752440f)); }
 
@@ -718,7 +719,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_infer_tc_kernel(const __gr
       mbar_init(smem_u32(&wempty[s]), 1);
     }
     mbar_init(smem_u32(&accf), 1);
-    mbar_init(smem_u32(&actr), MLP_TM);
+    mbar_init(smem_u32(&actr), MLP_EPI);
     mbar_init(smem_u32(&drain), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -797,20 +798,23 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_infer_tc_kernel(const __gr
       mbar_wait(smem_u32(&drain), 0);
     }
   } else {
-    // ---- epilogue: warps 2-5, TMEM lane quarter warp % 4; thread = one query of the tile ----
+    // ---- epilogue: warps 2-17.  TMEM lane quarter q = warp % 4 (the tile's rows 32 q ..
+    // 32 q + 31, one per lane), column slice cs = (warp - 2) / 4 of each hidden layer ----
     const int q = warp & 3;
+    const int cs = (warp - 2) >> 2;
     const int row = q * 32 + lane;
-    const int et = threadIdx.x - 64;  // 0..127
+    const int et = threadIdx.x - 64;  // 0 .. MLP_EPI - 1
     const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
     unsigned char* arow = act_p + row * 128;
     const int sw = row & 7;
+    const int slice = a.hidden / 4;  // columns of a hidden layer per slice: a multiple of 16
     int n_acc = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
       const int m0 = t * MLP_TM;
       const int valid = min(MLP_TM, a.batch - m0);
       const bool live = row < valid;
-      // inputs -> K block 0 of the operand: x_hi at K [0, K0), x_lo at [K0, 2 K0); the box check
-      {
+      if (cs == 0) {
+        // inputs -> K block 0 of the operand: x_hi at K [0, K0), x_lo at [K0, 2 K0); the box check
         float xs[K0];
         int out = 0;
 #pragma unroll
@@ -850,73 +854,70 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_infer_tc_kernel(const __gr
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const float* bias = a.bias[l];
         if (l < a.layers - 1) {
-          // hidden layer: bias + GELU -> BF16 operand of the next layer
+          // hidden layer, this warp's column slice: bias + GELU -> BF16 operand of the next layer
 #pragma unroll 1
-          for (int c0 = 0; c0 < a.hidden; c0 += 32) {
-            uint32_t r0[16], r1[16];
-            tmem_ld16(tmem + lane_addr + (uint32_t)c0, r0);
-            tmem_ld16(tmem + lane_addr + (uint32_t)c0 + 16u, r1);
+          for (int c0 = cs * slice; c0 < (cs + 1) * slice; c0 += 16) {
+            uint32_t r[16];
+            tmem_ld16(tmem + lane_addr + (uint32_t)c0, r);
             tmem_wait_ld();
-            uint32_t pk[16];
+            uint32_t pk[8];
 #pragma unroll
-            for (int j = 0; j < 16; j += 2) {
-              pk[j / 2] = pack_bf16x2(mlp_gelu(__uint_as_float(r0[j]) + bias[c0 + j]),
-                                      mlp_gelu(__uint_as_float(r0[j + 1]) + bias[c0 + j + 1]));
-              pk[8 + j / 2] = pack_bf16x2(mlp_gelu(__uint_as_float(r1[j]) + bias[c0 + 16 + j]),
-                                          mlp_gelu(__uint_as_float(r1[j + 1]) + bias[c0 + 17 + j]));
-            }
+            for (int j = 0; j < 16; j += 2)
+              pk[j / 2] = pack_bf16x2(mlp_gelu(__uint_as_float(r[j]) + bias[c0 + j]),
+                                      mlp_gelu(__uint_as_float(r[j + 1]) + bias[c0 + j + 1]));
             unsigned char* kb = arow + (c0 >> 6) * MLP_KB_BYTES;
             const int cc = (c0 & 63) >> 3;
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-              *reinterpret_cast<uint4*>(kb + (((cc + i) ^ sw) << 4)) =
-                  make_uint4(pk[4 * i], pk[4 * i + 1], pk[4 * i + 2], pk[4 * i + 3]);
+            *reinterpret_cast<uint4*>(kb + ((cc ^ sw) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4*>(kb + (((cc + 1) ^ sw) << 4)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
           }
           asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
           mbar_arrive(smem_u32(&actr));
         } else {
-          // output layer: softmax over the first n_hist columns (online max / sum), then the outputs
-          float mx = -INFINITY, se = 0.f;
+          // output layer (slice 0's warps hold whole rows): softmax over the first n_hist
+          // columns (online max / sum), the outputs staged as FP32 [valid][out] over the
+          // operand (its MMAs have completed), then stored by all epilogue threads
+          float* stg = reinterpret_cast<float*>(act_p);
+          if (cs == 0) {
+            float mx = -INFINITY, se = 0.f;
 #pragma unroll 1
-          for (int c0 = 0; c0 < a.n_hist; c0 += 16) {
-            uint32_t r[16];
-            tmem_ld16(tmem + lane_addr + (uint32_t)c0, r);
-            tmem_wait_ld();
+            for (int c0 = 0; c0 < a.n_hist; c0 += 16) {
+              uint32_t r[16];
+              tmem_ld16(tmem + lane_addr + (uint32_t)c0, r);
+              tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              if (c0 + j < a.n_hist) {
-                const float z = __uint_as_float(r[j]) + bias[c0 + j];
-                if (z > mx) {
-                  se = se * expf(mx - z) + 1.f;
-                  mx = z;
-                } else {
-                  se += expf(z - mx);
+              for (int j = 0; j < 16; ++j) {
+                if (c0 + j < a.n_hist) {
+                  const float z = __uint_as_float(r[j]) + bias[c0 + j];
+                  if (z > mx) {
+                    se = se * expf(mx - z) + 1.f;
+                    mx = z;
+                  } else {
+                    se += expf(z - mx);
+                  }
                 }
               }
             }
-          }
-          const float inv = 1.f / se;
-          // staging [valid][out] FP32 over the operand (its MMAs have completed)
-          float* stg = reinterpret_cast<float*>(act_p);
+            const float inv = 1.f / se;
 #pragma unroll 1
-          for (int c0 = 0; c0 < a.out_pad; c0 += 16) {
-            uint32_t r[16];
-            tmem_ld16(tmem + lane_addr + (uint32_t)c0, r);
-            tmem_wait_ld();
+            for (int c0 = 0; c0 < a.out_pad; c0 += 16) {
+              uint32_t r[16];
+              tmem_ld16(tmem + lane_addr + (uint32_t)c0, r);
+              tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int c = c0 + j;
-              if (live && c < a.out) {
-                const float z = __uint_as_float(r[j]) + bias[c];
-                stg[row * a.out + c] = c < a.n_hist ? expf(z - mx) * inv : z;
+              for (int j = 0; j < 16; ++j) {
+                const int c = c0 + j;
+                if (live && c < a.out) {
+                  const float z = __uint_as_float(r[j]) + bias[c];
+                  stg[row * a.out + c] = c < a.n_hist ? expf(z - mx) * inv : z;
+                }
               }
             }
           }
           asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
           epi_sync();
           float* y = a.y + (size_t)m0 * a.out;
-          for (int i = et; i < valid * a.out; i += MLP_TM) y[i] = stg[i];
+          for (int i = et; i < valid * a.out; i += MLP_EPI) y[i] = stg[i];
           epi_sync();  // the next tile's inputs overwrite the staging
         }
       }
@@ -985,6 +986,18 @@ bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int
   return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(field), dims,
             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool encode_tiled_rows(void* map, const float2* field, int N, int B, int box_blocks) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !map || ((uintptr_t)field & 127) != 0 || N < 16 || box_blocks < 1 || box_blocks > 256) return false;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const cuuint64_t dims[3] = {32, (cuuint64_t)N * N / 16, (cuuint64_t)B};
+  const cuuint64_t strides[2] = {128, (cuuint64_t)N * N * sizeof(float2)};
+  const cuuint32_t box[3] = {8, (cuuint32_t)box_blocks, 1};
+  return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(field), dims,
+            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // tiled field [B][N][N] (4 x 4 blocks of complex64 = 32 FP32 = 128 bytes):

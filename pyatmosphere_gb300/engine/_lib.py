@@ -25,6 +25,7 @@ FLAG_TC_N256 = 16
 FLAG_TC_N128 = 32
 FLAG_TILED = 64
 FLAG_ROWMAJOR = 128
+FLAG_FFT_SCREENS = 256
 ERR_TIMEOUT = -5
 ERR_NONFINITE = -6
 STEP_SLOTS = 8
@@ -124,6 +125,15 @@ SIGNATURES = {
                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                       ctypes.c_void_p, ctypes.c_void_p]),
     "atm_plan_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AtmChannelDesc)]),
+    "atm_channel_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AtmChannelDesc),
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "atm_channel_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "atm_run_channel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_run_fft": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p]),
     "atm_draw_spectra": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
                                         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p]),

@@ -20,14 +20,22 @@ def _axis(N, step):
     return np.arange(lo, lo + N, dtype=np.float64) * step
 
 
-def screen_inputs(N, delta, psd_phi_f, k, thickness, normals):
+def screen_amplitude(N, delta, psd_phi_f, k, thickness):
+    """sqrt(Phi_phi(|f|)) 2 pi df on the centred frequency grid, DC = 0 (float32)."""
     df = 1.0 / (N * delta)
     ax = _axis(N, df)
     amp = np.sqrt(psd_phi_f(np.sqrt(ax[None, :] ** 2 + ax[:, None] ** 2), k, thickness)) * 2 * np.pi * df
     amp[N // 2, N // 2] = 0.0
+    return amp.astype(np.float32)
+
+
+def subharmonic_factors(N, delta, psd_phi_f, k, thickness, level_normals):
+    """Per 3 x 3 subharmonic level s (draws level_normals[s], shape (2, 3, 3)):
+    the separable factors X_j(x), Y_j(y) and the mean of sum_j X_j Y_j (FP64)."""
+    df = 1.0 / (N * delta)
     x = _axis(N, delta)
     X, Y, mean = [], [], 0j
-    for s, nrm in enumerate(normals[1:]):
+    for s, nrm in enumerate(level_normals):
         sdf = df / 3 ** (s + 1)
         f3 = np.arange(-1, 2, dtype=np.float64) * sdf
         r3 = np.sqrt(f3[None, :] ** 2 + f3[:, None] ** 2)
@@ -40,7 +48,23 @@ def screen_inputs(N, delta, psd_phi_f, k, thickness, normals):
             X.append(Xj)
             Y.append(Yj)
             mean += Xj.mean() * Yj.mean()
-    return amp.astype(np.float32), X, Y, mean
+    return X, Y, mean
+
+
+def screen_inputs(N, delta, psd_phi_f, k, thickness, normals):
+    amp = screen_amplitude(N, delta, psd_phi_f, k, thickness)
+    X, Y, mean = subharmonic_factors(N, delta, psd_phi_f, k, thickness, normals[1:])
+    return amp, X, Y, mean
+
+
+def draw_normals(N, subharmonics):
+    """The standard normals of one FFTPhaseScreen draw in the reference's order
+    (phase_screens.py:46-60): the main grid's real then imaginary part, then
+    per subharmonic level a 3 x 3 real then imaginary part."""
+    out = [np.stack([np.random.normal(size=(N, N)), np.random.normal(size=(N, N))])]
+    for _ in range(subharmonics):
+        out.append(np.stack([np.random.normal(size=(3, 3)), np.random.normal(size=(3, 3))]))
+    return out
 
 
 def fft_screen(ps, normals):

@@ -115,6 +115,27 @@ class EnginePlan:
         self.n_screens = len(positions)
         self._geometry = (wvl, w0, F0, list(positions), length, list(pupils))
 
+    def channel(self, wvl, w0, F0, positions, length, pupils=()) -> "EngineChannel":
+        """A channel table set for this plan (atm_channel_create): the state
+        `update` would set, built once; run it with `run_channel`."""
+        d = self._desc(wvl, w0, F0, positions, length, pupils)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_channel_create(self._handle, ctypes.byref(d), ctypes.byref(h)))
+        return EngineChannel(self, h, len(positions))
+
+    def run_channel(self, ch: "EngineChannel", rho, theta, value, out: Optional[torch.Tensor] = None,
+                    field_out=None) -> torch.Tensor:
+        """atm_run with the channel's state in place of the plan's (atm_run_channel)."""
+        batch = int(rho.shape[0])
+        r, t, v = self._spectra(rho, theta, value, batch)
+        if out is None:
+            out = torch.empty((batch, self.n_out), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_run_channel(self._handle, ch.handle, r, t, v, batch, _tptr(out), _tptr(field_out),
+                                           None, _stream(self.device)))
+        return out
+
     def set_shift(self, shift):
         """Moves every screen by `shift` (x, y) metres (atm_plan_update with the
         plan's geometry), as generate_phase_screen(shift=...) does."""
@@ -188,6 +209,18 @@ class EnginePlan:
         with torch.cuda.device(self.device):
             check(self.lib.atm_run(self._handle, r, t, v, batch, _tptr(out), _tptr(field_out),
                                    _tptr(mean_intensity), _stream(self.device)))
+        return out
+
+    def run_fft(self, normals, amp, sub_x, sub_y, sub_mean, n_sub: int, out: Optional[torch.Tensor] = None,
+                field_out=None) -> torch.Tensor:
+        """atm_run with FFT screens (atm_run_fft; the plan needs FLAG_FFT_SCREENS)."""
+        batch = int(normals.shape[0])
+        if out is None:
+            out = torch.empty((batch, self.n_out), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self.lib.atm_run_fft(self._handle, _tptr(normals), _tptr(amp), _tptr(sub_x), _tptr(sub_y),
+                                       _tptr(sub_mean), int(n_sub), batch, _tptr(out), _tptr(field_out),
+                                       _stream(self.device)))
         return out
 
     def screen(self, rho, theta, value, screen: int, phi_out=None, phasor_out=None):
@@ -287,3 +320,25 @@ def fma_peak_tflops(device=None, blocks: int = 0, iters: int = 4096) -> float:
                 best = ms.value if best is None else min(best, ms.value)
     flops = blocks * 256.0 * iters * 16.0
     return flops / (best * 1e-3) / 1e12
+
+
+class EngineChannel:
+    """Handle of a channel table set (atm_channel_create) of one plan."""
+
+    def __init__(self, plan: EnginePlan, handle, n_screens: int):
+        self.plan = plan
+        self.handle = handle
+        self.n_screens = int(n_screens)
+
+    def close(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            with torch.cuda.device(self.plan.device):
+                self.plan.lib.atm_channel_destroy(h)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

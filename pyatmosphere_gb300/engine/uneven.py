@@ -164,3 +164,100 @@ def run_uneven(channels: Sequence[ChannelParams], realisations: int = 64, seed: 
     torch.cuda.synchronize(dev)
     return UnevenResult(pdt=pdt, eta_mean=eta_mean, measures=kept if keep_measures else None,
                         seconds=time.perf_counter() - t0, realisations=realisations, groups=info)
+
+
+def run_uneven_graph(channels: Sequence[ChannelParams], realisations: int = 64, seed: int = 0, bins: int = 64,
+                     device=None, keep_measures: bool = False, autotune: bool = False) -> UnevenResult:
+    """The mixed workload as ONE CUDA graph launch.
+
+    Set-up (outside the timed launch): per grid-size group one plan sized for
+    the group's largest screen count (tuned by atm_autotune when asked), one
+    channel table set per channel (atm_channel_create: source, geometry and
+    transfer tables built once), the channels' sqrt(PSD) rows on the device.
+    Capture: per group one stream, forked from the capturing stream; on it,
+    per channel, the device spectrum draw and atm_run_channel into the
+    channel's slice of one measures array; the streams join at the end.  The
+    graph is instantiated once and launched once for the whole mix; the
+    groups' branches run concurrently on the GPU.  Channel c's realisation r
+    uses Philox counter c * realisations + r, as in run_uneven, so every
+    channel gives the bits of run_uneven and of a fresh plan with the same
+    launch forms."""
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    C, R = len(channels), int(realisations)
+    groups: Dict[tuple, List[int]] = {}
+    for i, c in enumerate(channels):
+        groups.setdefault(_group_key(c), []).append(i)
+    t_setup = time.perf_counter()
+    state = []
+    n_out = None
+    for key in sorted(groups, key=lambda k: -k[0]):
+        idx = groups[key]
+        c_max = max((channels[i] for i in idx), key=lambda c: c.n_screens)
+        n_max, P = c_max.n_screens, c_max.points
+        plan = EnginePlan(c_max.N, c_max.delta, c_max.wvl, c_max.w0, c_max.F0, c_max.positions(), c_max.length,
+                          f_base=c_max.base(), pupils=[(c_max.pupil_radius,)], batch=R, device=dev)
+        if autotune:
+            plan.autotune(repeats=2)
+        n_out = plan.n_out if n_out is None else n_out
+        chans = {i: plan.channel(channels[i].wvl, channels[i].w0, channels[i].F0, channels[i].positions(),
+                                 channels[i].length, pupils=[(channels[i].pupil_radius,)]) for i in idx}
+        sq = {i: torch.from_numpy(channels[i].sqrt_psd()).to(dev).expand(channels[i].n_screens, -1).contiguous()
+              for i in idx}
+        buf = {"rho": torch.empty(R * n_max * P, dtype=torch.float32, device=dev)}
+        buf["theta"] = torch.empty_like(buf["rho"])
+        buf["value"] = torch.empty(R * n_max * P, dtype=torch.complex64, device=dev)
+        state.append((key, idx, plan, chans, sq, buf, P))
+    out_all = torch.empty((C, R, n_out), dtype=torch.float64, device=dev)
+
+    def launch_group(idx, plan, chans, sq, buf, P):
+        for i in sorted(idx, key=lambda j: -channels[j].n_screens):
+            n = channels[i].n_screens
+            rho = buf["rho"][:R * n * P].view(R, n, P)
+            theta = buf["theta"][:R * n * P].view(R, n, P)
+            value = buf["value"][:R * n * P].view(R, n, P)
+            plan.draw_spectra(seed, i * R, sq[i], rho, theta, value)
+            plan.run_channel(chans[i], rho, theta, value, out=out_all[i])
+
+    # warm-up outside the capture: the engine's per-device launch settings get cached
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for key, idx, plan, chans, sq, buf, P in state:
+            launch_group(idx[:1], plan, chans, sq, buf, P)
+    torch.cuda.synchronize(dev)
+    t_capture = time.perf_counter()
+    streams = [torch.cuda.Stream(device=dev) for _ in state]
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        for s, (key, idx, plan, chans, sq, buf, P) in zip(streams, state):
+            s.wait_stream(side)
+            with torch.cuda.stream(s):
+                launch_group(idx, plan, chans, sq, buf, P)
+        for s in streams:
+            side.wait_stream(s)
+    torch.cuda.synchronize(dev)
+    t_ready = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(side)
+    graph.replay()
+    e1.record(side)
+    torch.cuda.synchronize(dev)
+    seconds = e0.elapsed_time(e1) * 1e-3
+    for key, idx, plan, chans, sq, buf, P in state:
+        plan.check()
+    eta = out_all[:, :, _lib.OUT_PUPIL0].clamp(0.0, 1.0)
+    cell = torch.clamp((eta * bins).floor(), max=bins - 1).long()
+    counts = torch.zeros((C, bins), dtype=torch.float64, device=dev).scatter_add_(1, cell, torch.ones_like(eta))
+    pdt = (counts / R).cpu().numpy()
+    eta_mean = eta.mean(dim=1).cpu().numpy()
+    kept = [m for m in out_all.cpu().numpy()] if keep_measures else None
+    info = {key[0]: {"channels": len(idx), "max_screens": max(channels[i].n_screens for i in idx),
+                     "tuned": {k: plan.info[k] for k in ("col_tile", "row_variant", "col_variant")}}
+            for key, idx, plan, chans, sq, buf, P in state}
+    info["graph"] = {"setup_s": t_capture - t_setup, "capture_s": t_ready - t_capture, "launches": 1}
+    del graph
+    for key, idx, plan, chans, sq, buf, P in state:
+        for ch in chans.values():
+            ch.close()
+        plan.close()
+    return UnevenResult(pdt=pdt, eta_mean=eta_mean, measures=kept, seconds=seconds, realisations=R, groups=info)

@@ -131,11 +131,8 @@ class FFTPhaseScreen(PhaseScreen):
     def draw_normals(self):
         """Standard normals in the reference's draw order (real then imaginary
         part, main grid then each subharmonic level)."""
-        N = self.grid.N
-        out = [np.stack([np.random.normal(size=(N, N)), np.random.normal(size=(N, N))])]
-        for _ in range(self.subharmonics):
-            out.append(np.stack([np.random.normal(size=(3, 3)), np.random.normal(size=(3, 3))]))
-        return out
+        from .engine.fft_screen import draw_normals
+        return draw_normals(self.grid.N, self.subharmonics)
 
     def generate_phase_screen(self, *args, normals=None, **kwargs):
         from .engine.fft_screen import fft_screen

@@ -70,17 +70,15 @@ def _to_numpy(t):
 def _channel_run(ref, original):
     @functools.wraps(original)
     def run(self, pupil=True, *args, **kwargs):
-        from .engine.runner import draw_channel_spectra, fusable, get_plan, to_device
+        from .engine.runner import fusable, get_plan, run_single, screen_kind
         if not enabled(ref) or args or not set(kwargs) <= {"shift", "wind"} or not fusable(self):
             return original(self, pupil, *args, **kwargs)
+        if screen_kind(self.path) == "fft" and kwargs:
+            return original(self, pupil, *args, **kwargs)  # FFT screens take no shift / wind
         import torch
         plan = get_plan(self, batch=1, shift=kwargs.get("shift", (0, 0)), path_output_loss=True)
         field = torch.empty((1, plan.N, plan.N), dtype=torch.complex64, device=plan.device)
-        spectra = (None, None, None)
-        if plan.n_screens:
-            self.path.init_phase_screens()
-            spectra = to_device(*draw_channel_spectra(self, 1, wind=kwargs.get("wind", False), clear=False))
-        plan.run(*spectra, field_out=field)
+        run_single(self, plan, field, wind=kwargs.get("wind", False))
         plan.check()
         out = _to_numpy(field[0])
         return self.pupil.output(out) if pupil else out
@@ -177,12 +175,17 @@ def classify_reference(ref, channel, mtype, ops):
 
 
 def _batch_plan_reference(ref, sim):
-    from .engine.runner import fusable
+    from .engine.runner import fusable, screen_kind
     plans = {}
     for channel, by_time in sim.measures.items():
         if not fusable(channel):
             return None
+        fft = screen_kind(channel.path) == "fft"
         for time, by_type in by_time.items():
+            if fft and time is not None:
+                return None  # FFT screens do not move with time
+            if fft and "phase_screen" in by_type:
+                return None
             for mtype, by_ops in by_type.items():
                 for ops, ms in by_ops.items():
                     kind = classify_reference(ref, channel, mtype, ops)

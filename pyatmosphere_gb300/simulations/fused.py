@@ -105,7 +105,7 @@ def run_batched(plans, batch: int) -> int:
     for time value t.  Appends each measure's values and returns the number
     of realisations run."""
     import numpy as np
-    from ..engine.runner import draw_channel_spectra, get_plan, to_device
+    from ..engine.runner import draw_channel_fft, draw_channel_spectra, get_plan, screen_kind, to_device
     live = [m for ms in plans.values() for m, _, _ in ms if not m.is_done]
     wanted = [m.max_size - len(m) for m in live if m.max_size is not None]
     R = max(1, min(batch, max(wanted) if wanted else batch))
@@ -113,11 +113,18 @@ def run_batched(plans, batch: int) -> int:
     for c in chans:
         c.path.init_phase_screens()
     draws = {c: [] for c in chans}
+    fft = {c: screen_kind(c.path) == "fft" for c in chans}
     for _ in range(R):
         for c in chans:
-            draws[c].append(draw_channel_spectra(c, 1, wind=True, clear=True))
+            draws[c].append(draw_channel_fft(c, 1) if fft[c] else draw_channel_spectra(c, 1, wind=True, clear=True))
     for c, entries in plans.items():
-        spectra = [np.concatenate([d[k] for d in draws[c]]) for k in range(3)]
+        if fft[c]:
+            # normals, sub_x, sub_y, sub_mean per realisation; the amplitude grids and n_sub are shared
+            cat = {k: np.concatenate([d[k] for d in draws[c]]) for k in (0, 2, 3, 4)}
+            spectra = (cat[0], draws[c][0][1], cat[2], cat[3], cat[4])
+            n_sub = draws[c][0][5]
+        else:
+            spectra = [np.concatenate([d[k] for d in draws[c]]) for k in range(3)]
         pupils = sorted({k[1] for _, k, _ in entries if k[0] == "pupil"})
         tracked = sorted({k[1][0] for _, k, _ in entries if k[0] == "tracked"})
         steps = any(k[0].startswith("step") for _, k, _ in entries)
@@ -129,6 +136,9 @@ def run_batched(plans, batch: int) -> int:
         outs, sfs = {}, {}
         try:
             for t in shifts:
+                if fft[c]:
+                    outs[t] = plan.run_fft(*dev, n_sub).cpu().numpy()  # one time value (no shift)
+                    continue
                 plan.set_shift((0.0, t))
                 outs[t] = plan.run(*dev).cpu().numpy()
                 if want_sf:

@@ -155,11 +155,14 @@ class Simulation:
     def _batch_plan(self):
         """Per channel: [(measure, fused kind, time tuple or None)], or None if
         some measure is outside what the engine fuses."""
+        from ..engine.runner import screen_kind
         from .fused import classify
         plans = {}
         for (channel, time, mtype, ops), group in self._groups.items():
             if not getattr(channel, "_fused_ok", lambda: False)():
                 return None
+            if screen_kind(channel.path) == "fft" and (time is not None or mtype == "phase_screen"):
+                return None  # FFT screens do not move with time; the screen measures use atm_screen
             kind = classify(channel, mtype, ops)
             if kind is None:
                 return None

@@ -62,7 +62,9 @@ def test_geometry_is_read_from_the_reference_objects(stock_reference):
     assert runner.source_kind(ch.source) == ("gaussian", 808e-9, 0.05, float("inf"))
     assert runner.grid_size(ch.grid) == 64
     assert runner.fusable(ch)
-    assert not runner.fusable(ref_channel(ref, screen="fft"))
+    fft = ref_channel(ref, screen="fft")
+    assert runner.fusable(fft) and runner.screen_kind(fft.path) == "fft"  # atm_run_fft
+    assert runner.screen_kind(ch.path) == "ss"
 
 
 def test_batched_path_takes_the_reference_results(stock_reference):

@@ -4,7 +4,7 @@ passes) against the row-major forms and the FP64 oracle.
 The tiled row pass (variant 5) and column pass (variant 5) run the same FFT
 arithmetic as the row-major bulk-copy row pass (variant 3) and the TMA column
 pass with alternating exchanges (variant 4); the product-twiddle forms (tiled
-row 6 and 8, column 8 and 9; row-major row 4 and 7, column 2 and 7) share another
+row 6, 8, 9 and 10, column 8 and 9; row-major row 4 and 7, column 2 and 7) share another
 arithmetic, with or without the twiddle bases in registers.  The measures reduce one row
 per partial in both at N = 2048: there the results are equal bit for bit.  At
 N = 512 and 1024 the row-major forms sum several rows per partial, so the
@@ -65,7 +65,8 @@ def test_tiled_run_equals_row_major(torch_cuda, N):
     tl.close()
 
 
-@pytest.mark.parametrize("row_variant,col_variant", [(5, 5), (6, 5), (5, 6), (6, 6), (8, 8), (6, 9)])
+@pytest.mark.parametrize("row_variant,col_variant", [(5, 5), (6, 5), (5, 6), (6, 6), (8, 8), (6, 9), (9, 9),
+                                                      (10, 8)])
 def test_tiled_run_matches_oracle(torch_cuda, row_variant, col_variant):
     torch = torch_cuda
     spec = o.ChannelSpec(N=512, delta=2e-3, w0=0.09, length=10e3, count=5, points=1024, Cn2=1e-15,
@@ -128,7 +129,8 @@ def test_tiled_autotune_keeps_tiled_forms(torch_cuda):
     spec = o.ChannelSpec(N=2048, delta=1.5e-3, count=2, points=256, length=10e3)
     _, tl, _ = _plans(spec, 2)
     choice = tl.autotune(repeats=1)
-    assert choice["row_variant"] in (5, 6, 8) and choice["col_variant"] in (5, 6, 8, 9) and choice["col_tile"] == 4
+    assert choice["row_variant"] in (5, 6, 8, 9, 10) and choice["col_variant"] in (5, 6, 8, 9)
+    assert choice["col_tile"] == 4
     assert tl.info["tiled"] == 1
 
 
@@ -144,13 +146,14 @@ def test_register_twiddles_give_the_product_twiddle_bits(torch_cuda):
     dev = [torch.from_numpy(a).cuda() for a in _spectra(spec, base, 17, R)]
     runs = {}
     for name, plan, v in (("rm table", rm, (4, 4, 2)), ("rm reg", rm, (7, 4, 7)), ("tiled reg", tl, (8, 4, 8)),
-                          ("tiled table rows", tl, (6, 4, 8)), ("tiled table", tl, (6, 4, 9))):
+                          ("tiled table rows", tl, (6, 4, 8)), ("tiled table", tl, (6, 4, 9)),
+                          ("tiled one-row", tl, (9, 4, 9)), ("tiled one-row reg", tl, (10, 4, 8))):
         plan.set_variants(*v)
         f = torch.empty((R, 2048, 2048), dtype=torch.complex64, device="cuda")
         m = plan.run(*dev, field_out=f).cpu().numpy()
         plan.check()
         runs[name] = (m, f)
-    for name in ("rm reg", "tiled reg", "tiled table rows", "tiled table"):
+    for name in ("rm reg", "tiled reg", "tiled table rows", "tiled table", "tiled one-row", "tiled one-row reg"):
         assert torch.equal(runs[name][1], runs["rm table"][1]), name
         # the tiled forms reduce the moments in other kernels: round-off apart
         np.testing.assert_allclose(runs[name][0], runs["rm table"][0], rtol=1e-9, atol=1e-15, err_msg=name)

@@ -68,3 +68,49 @@ def test_channels_match_the_oracle(mix):
             assert got[r, _lib.OUT_PUPIL0] == pytest.approx(ref[r]["eta_0"], rel=2e-5, abs=1e-7)
             assert got[r, _lib.OUT_ETA_TOTAL] == pytest.approx(ref[r]["eta_total"], rel=2e-5)
             assert got[r, _lib.OUT_MEAN_X2] == pytest.approx(ref[r]["mean_x2"], rel=1e-4)
+
+
+def test_graph_mix_matches_the_sequential_run(mix):
+    """The whole mix as one CUDA graph launch (channel table sets,
+    atm_run_channel, one stream per grid size): every channel's measures and
+    PDT equal the re-targeted sequential run's, bit for bit (hence a fresh
+    plan's, by the test above)."""
+    from pyatmosphere_gb300.engine.uneven import run_uneven_graph
+    chans, res = mix
+    g = run_uneven_graph(chans, realisations=4, seed=9, keep_measures=True)
+    assert g.groups["graph"]["launches"] == 1
+    for i in range(len(chans)):
+        np.testing.assert_array_equal(g.measures[i], res.measures[i])
+    np.testing.assert_array_equal(g.pdt, res.pdt)
+
+
+def test_channel_table_sets_on_one_plan():
+    """atm_run_channel with a table set equals atm_plan_update + atm_run on the
+    same plan, and leaves the plan's own channel in place."""
+    import torch
+    from pyatmosphere_gb300.engine import EnginePlan
+    from pyatmosphere_gb300.engine.uneven import ChannelParams
+    a = ChannelParams(N=256, n_screens=4, length=4e3, Cn2=2e-15, w0=0.06, wvl=808e-9, extent=1.0, points=256,
+                      pupil_radius=0.08)
+    b = ChannelParams(N=256, n_screens=2, length=1.5e3, Cn2=8e-15, w0=0.1, wvl=1550e-9, focused=True, extent=1.0,
+                      points=256, pupil_radius=0.05)
+    R = 3
+    plan = EnginePlan(a.N, a.delta, a.wvl, a.w0, a.F0, a.positions(), a.length, f_base=a.base(),
+                      pupils=[(a.pupil_radius,)], batch=R)
+    ch = plan.channel(b.wvl, b.w0, b.F0, b.positions(), b.length, pupils=[(b.pupil_radius,)])
+    rho = torch.empty((R, 2, 256), dtype=torch.float32, device="cuda")
+    theta = torch.empty_like(rho)
+    value = torch.empty((R, 2, 256), dtype=torch.complex64, device="cuda")
+    plan.draw_spectra(4, 0, torch.from_numpy(b.sqrt_psd()).cuda().expand(2, -1).contiguous(), rho, theta, value)
+    ra = torch.empty((R, 4, 256), dtype=torch.float32, device="cuda")
+    ta = torch.empty_like(ra)
+    va = torch.empty((R, 4, 256), dtype=torch.complex64, device="cuda")
+    plan.draw_spectra(5, 0, torch.from_numpy(a.sqrt_psd()).cuda().expand(4, -1).contiguous(), ra, ta, va)
+    own = plan.run(ra, ta, va).cpu().numpy()
+    via_set = plan.run_channel(ch, rho, theta, value).cpu().numpy()
+    np.testing.assert_array_equal(plan.run(ra, ta, va).cpu().numpy(), own)  # the plan's own channel is back
+    plan.update(b.wvl, b.w0, b.F0, b.positions(), b.length, pupils=[(b.pupil_radius,)])
+    np.testing.assert_array_equal(plan.run(rho, theta, value).cpu().numpy(), via_set)
+    plan.check()
+    ch.close()
+    plan.close()
