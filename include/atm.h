@@ -34,7 +34,8 @@
 extern "C" {
 #endif
 
-#define ATM_ABI_VERSION 2  /* 2: AtmPlanInfo.tiled; atm_plan_check, atm_set_wait_budget */
+#define ATM_ABI_VERSION 3  /* 2: AtmPlanInfo.tiled; atm_plan_check, atm_set_wait_budget;
+                              3: atm_channel_draw_spectra */
 
 #define ATM_OK 0
 #define ATM_ERR_INVALID (-1)     /* bad argument */
@@ -272,6 +273,15 @@ int atm_run_channel(AtmPlan* plan, AtmChannel* channel, const float* rho, const 
  * use host-drawn spectra where realisations must match the reference. */
 int atm_draw_spectra(AtmPlan* plan, uint64_t seed, uint64_t first_realisation, const float* sqrt_psd,
                      int32_t batch, float* rho, float* theta, void* value, void* stream);
+
+/* atm_draw_spectra for a channel table set: n is the channel's screen count
+ * (not the plan's), so sqrt_psd is [n][P] and the outputs [batch][n][P] in the
+ * layout atm_run_channel reads.  Replaces the draws of each screen's
+ * _get_spectrum for one parameter point of a mixed workload
+ * (phase_screens.py:93-106). */
+int atm_channel_draw_spectra(AtmPlan* plan, AtmChannel* channel, uint64_t seed, uint64_t first_realisation,
+                             const float* sqrt_psd, int32_t batch, float* rho, float* theta, void* value,
+                             void* stream);
 
 /* ---- PDT surrogate MLP (no reference counterpart: the learned part of the
  * engine; it answers PDTResult-style queries, simulations/pdt.py:11-66,

@@ -1297,6 +1297,17 @@ int atm_draw_spectra(AtmPlan* pl, uint64_t seed, uint64_t first_realisation, con
   return ATM_OK;
 }
 
+int atm_channel_draw_spectra(AtmPlan* pl, AtmChannel* ch, uint64_t seed, uint64_t first_realisation,
+                             const float* sqrt_psd, int32_t batch, float* rho, float* theta, void* value,
+                             void* stream) {
+  if (!pl || !ch) return fail(ATM_ERR_INVALID, "plan / channel is NULL");
+  if (ch->plan != pl) return fail(ATM_ERR_INVALID, "the channel was built for another plan");
+  swap_state(pl, ch->st);
+  const int rc = atm_draw_spectra(pl, seed, first_realisation, sqrt_psd, batch, rho, theta, value, stream);
+  swap_state(pl, ch->st);
+  return rc;
+}
+
 int atm_profile_begin(AtmPlan* pl, int32_t max_launches) {
   if (!pl || max_launches < 1) return fail(ATM_ERR_INVALID, "bad profile arguments");
   if (int rc = check_device(pl)) return rc;

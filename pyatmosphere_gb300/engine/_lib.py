@@ -15,7 +15,7 @@ LIB_DIR = os.path.join(_HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libatm.so")
 SELFTEST_PATH = os.path.join(LIB_DIR, "libatm_selftest.so")
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_PUPILS = 8
 FLAG_SIMT_GEMM = 1
 FLAG_TC_GEMM = 2
@@ -137,6 +137,9 @@ SIGNATURES = {
     "atm_draw_spectra": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
                                         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p]),
+    "atm_channel_draw_spectra": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
+                                                ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
     "atm_mlp_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                                       ctypes.POINTER(ctypes.c_void_p)]),
     "atm_mlp_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -128,7 +128,7 @@ class EnginePlan:
                     field_out=None) -> torch.Tensor:
         """atm_run with the channel's state in place of the plan's (atm_run_channel)."""
         batch = int(rho.shape[0])
-        r, t, v = self._spectra(rho, theta, value, batch)
+        r, t, v = self._spectra(rho, theta, value, batch, ch.n_screens)
         if out is None:
             out = torch.empty((batch, self.n_out), dtype=torch.float64, device=self.device)
         with torch.cuda.device(self.device):
@@ -159,12 +159,25 @@ class EnginePlan:
         check(self.lib.atm_plan_set_variants(self._handle, int(row_variant), int(col_tile), int(col_variant)))
         self._refresh_info()
 
-    def draw_spectra(self, seed, first, sqrt_psd, rho, theta, value):
-        """Seeded spectra on the device (atm_draw_spectra) into the given tensors."""
+    def draw_spectra(self, seed, first, sqrt_psd, rho, theta, value, channel: Optional["EngineChannel"] = None):
+        """Seeded spectra on the device into the given tensors: atm_draw_spectra
+        for the plan's own screens, atm_channel_draw_spectra for a channel
+        table set's (sqrt_psd [n][P], rho / theta / value [batch][n][P] with n
+        the channel's screen count)."""
         batch = int(rho.shape[0])
+        n = self.n_screens if channel is None else channel.n_screens
+        self._spectra(rho, theta, value, batch, n)
+        if sqrt_psd.device != self.device or sqrt_psd.dtype != torch.float32 or not sqrt_psd.is_contiguous() or \
+                tuple(sqrt_psd.shape) != (n, self.P):
+            raise ValueError(f"sqrt_psd must be a contiguous float32 [{n}, {self.P}] tensor on {self.device}")
         with torch.cuda.device(self.device):
-            check(self.lib.atm_draw_spectra(self._handle, int(seed), int(first), _tptr(sqrt_psd), batch, _tptr(rho),
-                                            _tptr(theta), _tptr(value), _stream(self.device)))
+            if channel is None:
+                check(self.lib.atm_draw_spectra(self._handle, int(seed), int(first), _tptr(sqrt_psd), batch,
+                                                _tptr(rho), _tptr(theta), _tptr(value), _stream(self.device)))
+            else:
+                check(self.lib.atm_channel_draw_spectra(self._handle, channel.handle, int(seed), int(first),
+                                                        _tptr(sqrt_psd), batch, _tptr(rho), _tptr(theta),
+                                                        _tptr(value), _stream(self.device)))
 
     def check(self):
         """Waits for the plan's work on the current stream and raises
@@ -189,15 +202,16 @@ class EnginePlan:
             pass
 
     # ------------------------------------------------------------------
-    def _spectra(self, rho, theta, value, batch):
-        if self.n_screens == 0:
+    def _spectra(self, rho, theta, value, batch, n_screens=None):
+        n_screens = self.n_screens if n_screens is None else n_screens
+        if n_screens == 0:
             return None, None, None
         for t, dt in ((rho, torch.float32), (theta, torch.float32), (value, torch.complex64)):
             if t.device != self.device or t.dtype != dt or not t.is_contiguous():
                 raise ValueError("spectra must be contiguous CUDA tensors (float32, float32, complex64) "
                                  f"on {self.device}")
-            if tuple(t.shape) != (batch, self.n_screens, self.P):
-                raise ValueError(f"spectra shape {tuple(t.shape)} != {(batch, self.n_screens, self.P)}")
+            if tuple(t.shape) != (batch, n_screens, self.P):
+                raise ValueError(f"spectra shape {tuple(t.shape)} != {(batch, n_screens, self.P)}")
         return _tptr(rho), _tptr(theta), _tptr(value)
 
     def run(self, rho, theta, value, out: Optional[torch.Tensor] = None, field_out=None,

@@ -215,7 +215,7 @@ def run_uneven_graph(channels: Sequence[ChannelParams], realisations: int = 64, 
             rho = buf["rho"][:R * n * P].view(R, n, P)
             theta = buf["theta"][:R * n * P].view(R, n, P)
             value = buf["value"][:R * n * P].view(R, n, P)
-            plan.draw_spectra(seed, i * R, sq[i], rho, theta, value)
+            plan.draw_spectra(seed, i * R, sq[i], rho, theta, value, channel=chans[i])
             plan.run_channel(chans[i], rho, theta, value, out=out_all[i])
 
     # warm-up outside the capture: the engine's per-device launch settings get cached
@@ -237,10 +237,12 @@ def run_uneven_graph(channels: Sequence[ChannelParams], realisations: int = 64, 
             side.wait_stream(s)
     torch.cuda.synchronize(dev)
     t_ready = time.perf_counter()
+    # graph.replay() launches on the current stream: time it there
+    cur = torch.cuda.current_stream(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(side)
+    e0.record(cur)
     graph.replay()
-    e1.record(side)
+    e1.record(cur)
     torch.cuda.synchronize(dev)
     seconds = e0.elapsed_time(e1) * 1e-3
     for key, idx, plan, chans, sq, buf, P in state:

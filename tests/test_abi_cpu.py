@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(built):
     from pyatmosphere_gb300.engine import _lib
     assert set(names) == set(_lib.SIGNATURES), "ctypes signatures must cover include/atm.h"
     lib.atm_abi_version.restype = ctypes.c_int
-    assert lib.atm_abi_version() == _lib.ABI_VERSION == 2
+    assert lib.atm_abi_version() == _lib.ABI_VERSION == 3
 
 
 def test_plan_create_rejects_bad_descriptors_without_gpu(built):

@@ -65,7 +65,10 @@ def test_simulation_takes_the_batched_fft_path():
     atm_run_fft per batch) gives the per-realisation Channel.run values."""
     import pyatmosphere_gb300 as pa
     from pyatmosphere_gb300 import measures, simulations
-    ch = _channel(pa)
+    # 0.101 m is 25.25 pixels: no pixel centre lies within float32 round-off of the rim, so the
+    # mirror's float32 pupil and the fused FP64 pupil mask the same pixels (at 0.1 m = 25 pixels
+    # the 20 lattice points on the rim flip between the two predicates)
+    ch = _channel(pa, pupil=0.101)
     pdt = simulations.PDTResult(ch, max_size=4)
     beam = simulations.BeamResult(ch, max_size=4)
     sim = simulations.Simulation([pdt, beam])

@@ -101,7 +101,8 @@ def test_channel_table_sets_on_one_plan():
     rho = torch.empty((R, 2, 256), dtype=torch.float32, device="cuda")
     theta = torch.empty_like(rho)
     value = torch.empty((R, 2, 256), dtype=torch.complex64, device="cuda")
-    plan.draw_spectra(4, 0, torch.from_numpy(b.sqrt_psd()).cuda().expand(2, -1).contiguous(), rho, theta, value)
+    plan.draw_spectra(4, 0, torch.from_numpy(b.sqrt_psd()).cuda().expand(2, -1).contiguous(), rho, theta, value,
+                      channel=ch)
     ra = torch.empty((R, 4, 256), dtype=torch.float32, device="cuda")
     ta = torch.empty_like(ra)
     va = torch.empty((R, 4, 256), dtype=torch.complex64, device="cuda")
