@@ -1115,7 +1115,9 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   double best_row = -1.0;
   int row_variant = 0;
   // a tiled plan chooses among the tiled forms only (the others do not know its layout)
-  const std::vector<int> row_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9, 10} : std::vector<int>{0, 1, 2, 3, 4, 7};
+  const bool warp_fft = N == 1024 || N == 2048;  // row 11 / column 10: warp FFTs
+  std::vector<int> row_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9, 10} : std::vector<int>{0, 1, 2, 3, 4, 7};
+  if (!pl->tiled && warp_fft) row_forms.push_back(11);
   for (int v : row_forms) {
     ra.variant = v;
     const double ms = time_it([&] { return atm::launch_row_pass(N, batch, ra, st); });
@@ -1135,7 +1137,8 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   for (int C : {2, 4, 8, 16}) {
     if (C * (N / 16) > 512 || C > N) continue;
     if (pl->tiled && C != 4) continue;
-    const std::vector<int> col_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9} : std::vector<int>{0, 1, 2, 3, 4, 7};
+    std::vector<int> col_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9} : std::vector<int>{0, 1, 2, 3, 4, 7};
+    if (!pl->tiled && warp_fft && C == 4) col_forms.push_back(10);
     for (int v : col_forms) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
@@ -1176,10 +1179,13 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
     pl->col_variant = col_variant;
     return ATM_OK;
   }
-  if (row_variant < 0 || (row_variant > 4 && row_variant != 7))
-    return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4 or 7", row_variant);
-  if (col_variant < 0 || (col_variant > 4 && col_variant != 7))
-    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4 or 7", col_variant);
+  const bool warp_fft = pl->N == 1024 || pl->N == 2048;  // row 11 / column 10: warp FFTs
+  if (row_variant < 0 || (row_variant > 4 && row_variant != 7 && !(row_variant == 11 && warp_fft)))
+    return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4, 7%s", row_variant, warp_fft ? " or 11" : "");
+  if (col_variant < 0 || (col_variant > 4 && col_variant != 7 && !(col_variant == 10 && warp_fft)))
+    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4, 7%s", col_variant, warp_fft ? " or 10" : "");
+  if (col_variant == 10 && col_tile != 4)
+    return fail(ATM_ERR_INVALID, "col_variant 10 takes col_tile 4");
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
     return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);
   if (col_tile * (pl->N / 16) > 512 || col_tile > pl->N)

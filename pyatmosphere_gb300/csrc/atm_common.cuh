@@ -441,6 +441,142 @@ ATM_HD void stage_last_reg(float2 (&v)[16], int t, const TwBases<N>& tb) {
 }
 
 // ---------------------------------------------------------------------------
+// Warp FFT: length N = 32 R (R = 32 or 64) held by 32 lanes, R elements each.
+// Lane j holds element j + 32 m in v[m], before and after a transform, so a
+// forward transform, a pointwise product and an inverse transform chain with
+// no reordering.  With n = j + 32 m and k = kb + R ka:
+//   X[kb + R ka] = sum_j W_32^(j ka) W_N^(j kb) sum_m x[j + 32 m] W_R^(m kb),
+// W_L = exp(DIR 2 pi i / L).  A transform is
+//   stage 1: DFT_R over m in registers, then the twiddle W_N^(j kb), then
+//            Y[j][kb] into an exchange buffer (one 32 x R transpose);
+//   stage 2: lane j takes kb = j + 32 h (h < R / 32), reads Y[0..31][kb] and
+//            runs DFT_32 over them in registers.
+// X[j + 32 h + R ka] is element j + 32 (h + (R / 32) ka), held in
+// v[h + (R / 32) ka]: the input's layout.  Compared with the radix-16
+// Stockham form (two exchanges per transform for N = 2048) the warp form
+// exchanges once, and within one warp (or one lane group) only.
+// ---------------------------------------------------------------------------
+// cos(pi k / 32), k = 0..16 (FP64 values rounded to FP32)
+ATM_HD constexpr float cos_pi32(int k) {
+  return k == 0    ? 1.0f
+         : k == 1  ? 0.99518472667219692873f
+         : k == 2  ? 0.98078528040323043058f
+         : k == 3  ? 0.95694033573220882438f
+         : k == 4  ? 0.92387953251128673848f
+         : k == 5  ? 0.88192126434835504956f
+         : k == 6  ? 0.83146961230254523567f
+         : k == 7  ? 0.77301045336273699338f
+         : k == 8  ? 0.70710678118654757274f
+         : k == 9  ? 0.63439328416364548779f
+         : k == 10 ? 0.55557023301960228867f
+         : k == 11 ? 0.47139673682599780857f
+         : k == 12 ? 0.38268343236508983729f
+         : k == 13 ? 0.29028467725446233105f
+         : k == 14 ? 0.19509032201612833135f
+         : k == 15 ? 0.09801714032956077016f
+                   : 0.0f;
+}
+
+// W_64^e = exp(DIR 2 pi i e / 64)
+template <int DIR>
+ATM_HD constexpr float2 w64(int e) {
+  e &= 63;
+  const int q = e >> 4, r = e & 15;
+  const float c = cos_pi32(r), s = cos_pi32(16 - r);  // cos, sin of pi r / 32
+  const float cr = q == 0 ? c : q == 1 ? -s : q == 2 ? -c : s;
+  const float sr = q == 0 ? s : q == 1 ? c : q == 2 ? -s : -c;
+  return float2{cr, DIR < 0 ? -sr : sr};
+}
+
+// a W_R^e for R dividing 64 and e known when the caller is unrolled; the
+// quarter turns are exact
+template <int R, int DIR>
+ATM_HD float2 twc(float2 a, int e) {
+  const int e64 = (e * (64 / R)) & 63;
+  if (e64 == 0) return a;
+  if (e64 == 16) return cmul_i<DIR>(a);
+  if (e64 == 32) return make_float2(-a.x, -a.y);
+  if (e64 == 48) return cmul_i<-DIR>(a);
+  return cmul(a, w64<DIR>(e64));
+}
+
+// natural-order DFT of length R1 R2 in registers, b_q = sum_m a_m W_(R1 R2)^(m q):
+// with m = m1 + R1 m2 and q = q2 + R2 q1, DFT_R2 over m2, the twiddle
+// W^(m1 q2), DFT_R1 over m1.  Streamed: input m passes through pre(m, x) as
+// it is gathered and output q goes to emit(q, y) as soon as its group is
+// formed, so that beside the R elements only one group of R1 or R2 values
+// (and whatever pre / emit load for it) is live at a time.
+template <int R1, int R2, int DIR, class PreF, class EmitF>
+ATM_HD void dft_2l(float2 (&a)[R1 * R2], PreF&& pre, EmitF&& emit) {
+  constexpr int R = R1 * R2;
+#pragma unroll
+  for (int m1 = 0; m1 < R1; ++m1) {
+    float2 t[R2];
+#pragma unroll
+    for (int m2 = 0; m2 < R2; ++m2) t[m2] = pre(m1 + R1 * m2, a[m1 + R1 * m2]);
+    dft<R2, DIR>(t);
+#pragma unroll
+    for (int q2 = 0; q2 < R2; ++q2) a[m1 + R1 * q2] = twc<R, DIR>(t[q2], m1 * q2);
+  }
+#pragma unroll
+  for (int q2 = 0; q2 < R2; ++q2) {
+    float2 t[R1];
+#pragma unroll
+    for (int m1 = 0; m1 < R1; ++m1) t[m1] = a[m1 + R1 * q2];
+    dft<R1, DIR>(t);
+#pragma unroll
+    for (int q1 = 0; q1 < R1; ++q1) emit(q2 + R2 * q1, t[q1]);
+  }
+}
+
+// the radix split of the warp FFT's in-register DFTs
+template <int R>
+struct WfftSplit;
+template <> struct WfftSplit<32> { static constexpr int R1 = 4, R2 = 8; };
+template <> struct WfftSplit<64> { static constexpr int R1 = 8, R2 = 8; };
+
+struct WfftNoPre {
+  ATM_HD float2 operator()(int, float2 x) const { return x; }
+};
+
+// stage 1 of lane j: pre(m, x) scales input m on the way in (a pointwise
+// product between two transforms), tw(kb) returns exp(-2 pi i j kb / N) (the
+// forward direction; the inverse conjugates it), put(kb, y) stores Y[j][kb]
+template <int R, int DIR, class TwF, class PutF, class PreF = WfftNoPre>
+ATM_HD void wfft_stage1(float2 (&v)[R], TwF&& tw, PutF&& put, PreF&& pre = PreF()) {
+  dft_2l<WfftSplit<R>::R1, WfftSplit<R>::R2, DIR>(v, pre, [&](int kb, float2 y) {
+    if (kb == 0) {
+      put(0, y);
+    } else {
+      const float2 w = tw(kb);
+      put(kb, cmul(y, DIR < 0 ? w : cconj(w)));
+    }
+  });
+}
+
+// stage 2 of lane j: get(h, jj) returns Y[jj][j + 32 h]; output element q
+// (the transform's element j + 32 q) passes through post(q, y) as it is formed
+template <int R, int DIR, class GetF, class PostF = WfftNoPre>
+ATM_HD void wfft_stage2(float2 (&v)[R], GetF&& get, PostF&& post = PostF()) {
+  constexpr int H = R / 32;
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    float2 u[32];
+#pragma unroll
+    for (int jj = 0; jj < 32; ++jj) u[jj] = get(h, jj);
+    dft_2l<4, 8, DIR>(u, WfftNoPre(), [&](int ka, float2 y) { v[h + H * ka] = post(h + H * ka, y); });
+  }
+}
+
+// exchange-buffer slot of Y[jj][kb] for one transform of 32 x R elements:
+// row kb of 32 slots, the lane index XOR-swizzled so that the stores of one
+// kb (lanes jj) and the loads of one jj (lanes kb = j + 32 h) both spread
+// over the 16 eight-byte bank pairs of each half warp.  `sw` is the
+// swizzle of row kb: kb & 15 when the 32 lanes are one warp; (kb & 3) |
+// (c << 2) when a warp holds lanes of four transforms c (8 lanes each).
+ATM_HD int wfft_slot(int kb, int jj, int sw) { return kb * 32 + (jj ^ sw); }
+
+// ---------------------------------------------------------------------------
 // fixed-point phase: turns(j) = frac(j * S + O) held as a 64-bit binary
 // fraction; the product wraps modulo one turn exactly.  Returned as
 // half-turns in [-1, 1) for sincospif.

@@ -940,10 +940,176 @@ static cudaError_t row_plain_launch(int B, const RowArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// row pass with warp FFTs (N = 1024, 2048; row-major field): one warp per
+// row, W warps per CTA, rows strided over a persistent grid.  Lane 0 moves
+// the warp's next row into the warp's staging buffer with one bulk copy as
+// soon as the current row has left it, so a row is always in flight; the
+// screen phases of the row are loaded into registers when the row starts and
+// arrive while the inverse transform runs.  Lane j holds elements j + 32 m
+// (the warp FFT's layout, atm_common.cuh); each transform exchanges once
+// through the warp's own exchange buffer, with no barrier beyond __syncwarp.
+// Passes with measures (ROW_MEAS, ROW_STEP) or the unfolded screen phasor go
+// to the one-row product-twiddle form instead (row_launch).  The staging
+// wait is bounded (error word, then a drain of the copy in flight).
+// ---------------------------------------------------------------------------
+template <int N>
+struct RowWarp {
+  static constexpr int R = N / 32;
+  static constexpr int W = N == 2048 ? 6 : 12;                   // warps per CTA, one CTA per SM
+  static constexpr size_t ROW = (size_t)N * sizeof(float2);       // a staged row / an exchange buffer
+  static constexpr size_t TWT = (size_t)R * 32 * sizeof(float2);  // W_N^(j kb) per lane j
+  static constexpr size_t SMEM = 128 + (size_t)W * 2 * ROW + TWT;
+};
+
+template <int N>
+__global__ void __launch_bounds__(RowWarp<N>::W * 32, 1) row_pass_wfft_kernel(RowArgs a, int n_rows) {
+  using Cfg = RowWarp<N>;
+  constexpr int R = Cfg::R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[Cfg::W];
+  unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
+  const int warp = threadIdx.x >> 5, j = threadIdx.x & 31;
+  float2* stage = reinterpret_cast<float2*>(sbase + (size_t)warp * 2 * Cfg::ROW);
+  float2* xw = stage + N;
+  float2* twt = reinterpret_cast<float2*>(sbase + (size_t)Cfg::W * 2 * Cfg::ROW);
+  // twt[kb][jj] = exp(-2 pi i jj kb / N) = tw[jj kb]  (jj kb < N)
+  for (int i = threadIdx.x; i < R * 32; i += blockDim.x) twt[i] = a.tw[(i >> 5) * (i & 31)];
+  const uint32_t fb = (uint32_t)__cvta_generic_to_shared(&full_bar[warp]);
+  if (j == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fb) : "memory");
+  if (threadIdx.x == 0) asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  __syncthreads();
+  const int flags = a.flags;
+  const bool load_field = !(flags & ROW_GEN);
+  const unsigned long long wait_ns = g_pass_wait_ns;
+  const uint32_t sdst = (uint32_t)__cvta_generic_to_shared(stage);
+  auto fetch = [&](int row) {  // lane 0
+    const int r = row / N, y = row - r * N;
+    const float2* src = a.field + (size_t)r * N * N + (size_t)y * N;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::ROW)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     sdst),
+                 "l"(src), "r"((uint32_t)Cfg::ROW), "r"(fb)
+                 : "memory");
+  };
+  auto tw = [&](int kb) { return twt[kb * 32 + j]; };
+  auto put = [&](int kb, float2 y) { xw[wfft_slot(kb, j, kb & 15)] = y; };
+  auto get = [&](int h, int jj) {
+    const int kb = j + 32 * h;
+    return xw[wfft_slot(kb, jj, kb & 15)];
+  };
+  const int stride = gridDim.x * Cfg::W;
+  int row = blockIdx.x * Cfg::W + warp;
+  bool pending = false;  // lane 0: a copy issued and not yet waited for
+  if (load_field && j == 0 && row < n_rows) {
+    fetch(row);
+    pending = true;
+  }
+  int k = 0;
+  for (; row < n_rows; row += stride, ++k) {
+    const int r = row / N, y = row - r * N;
+    const size_t rowoff = (size_t)r * N * N + (size_t)y * N;
+    float2 v[R];
+    if (load_field) {
+      const bool ok = pass_mbar_wait(fb, (uint32_t)(k & 1), wait_ns);
+      if (j == 0 && ok) pending = false;
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (j == 0) {
+          atomicExch(&g_pass_error, 1);
+          if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+        }
+        break;
+      }
+#pragma unroll
+      for (int m = 0; m < R; ++m) v[m] = stage[j + 32 * m];
+      // the next row's copy (the async proxy) may overwrite the stage once every lane has read it
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      __syncwarp();
+      if (j == 0 && row + stride < n_rows) {
+        fetch(row + stride);
+        pending = true;
+      }
+    } else {
+      const float2 gy = a.ay[y];
+#pragma unroll
+      for (int m = 0; m < R; ++m) v[m] = cmul(gy, a.ax[j + 32 * m]);
+    }
+    // the screen phases (folded: one phasor per pixel), in flight during the inverse transform
+    float ph[R];
+    if (flags & ROW_PHASOR) {
+      const float* p = a.phi + rowoff;
+#pragma unroll
+      for (int m = 0; m < R; ++m) ph[m] = p[j + 32 * m];
+    }
+    // the screen phasor and the step's loss (a lossless step multiplies by the bare phasor),
+    // applied to each element as the inverse transform forms it (or, without an inverse, as
+    // the forward gathers it), so that the phases leave registers one by one
+    const float loss = a.loss;
+    auto screen = [&](int m, float2 x) {
+      if (flags & ROW_PHASOR) {
+        const float2 p = phasor_turns(ph[m]);
+        return cmul(x, loss == 1.0f ? p : cscale(p, loss));
+      }
+      return loss == 1.0f ? x : cscale(x, loss);
+    };
+    if (flags & ROW_INV) {
+      wfft_stage1<R, 1>(v, tw, put);
+      __syncwarp();
+      wfft_stage2<R, 1>(v, get, screen);
+      __syncwarp();  // every lane has read its rows before the next transform stores
+    }
+    if (flags & ROW_FWD) {
+      if (flags & ROW_INV)
+        wfft_stage1<R, -1>(v, tw, put);
+      else
+        wfft_stage1<R, -1>(v, tw, put, screen);
+      __syncwarp();
+      wfft_stage2<R, -1>(v, get);
+      __syncwarp();
+    } else if (!(flags & ROW_INV) && ((flags & ROW_PHASOR) || loss != 1.0f)) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) v[m] = screen(m, v[m]);
+    }
+    if (flags & ROW_STORE) {
+      float2* dst = ((a.store_out && a.out) ? a.out : a.field) + rowoff;
+#pragma unroll
+      for (int m = 0; m < R; ++m) dst[j + 32 * m] = v[m];
+    }
+  }
+  // no copy may land after the CTA leaves
+  if (j == 0 && pending) pass_mbar_wait(fb, (uint32_t)(k & 1));
+}
+
+template <int N>
+static cudaError_t row_wfft_launch(int B, const RowArgs& a, cudaStream_t st) {
+  using Cfg = RowWarp<N>;
+  static LaunchCache cache;
+  const int threads = Cfg::W * 32;
+  int grid_max = 0;
+  cudaError_t e = cache.get(row_pass_wfft_kernel<N>, threads, Cfg::SMEM, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_rows = B * N;
+  const int grid = std::max(1, std::min((n_rows + Cfg::W - 1) / Cfg::W, grid_max));
+  row_pass_wfft_kernel<N><<<grid, threads, Cfg::SMEM, st>>>(a, n_rows);
+  return cudaGetLastError();
+}
+
 template <int N>
 static cudaError_t row_launch(int B, const RowArgs& a, cudaStream_t st) {
   const bool field_ok = (a.flags & ROW_GEN) || aligned16(a.field);
   const bool phi_ok = !(a.flags & ROW_PHASOR) || aligned16(a.phi);
+  if constexpr (N == 1024 || N == 2048) {
+    if (a.variant == 11 && !a.tiled) {
+      // 11: warp FFTs.  Its passes without measures; the others in the one-row product form
+      const bool plain = field_ok && phi_ok && !(a.flags & (ROW_MEAS | ROW_STEP)) &&
+                         (!(a.flags & ROW_PHASOR) || (a.flags & ROW_FOLDED)) && !a.mean_I && !a.intensity;
+      if (plain) return row_wfft_launch<N>(B, a, st);
+      RowArgs b = a;
+      b.variant = 4;
+      return row_launch<N>(B, b, st);
+    }
+  }
   if constexpr (N == 512 || N == 1024 || N == 2048) {
     if (a.variant == 9 || a.variant == 10) {
       // the tiled layout one row per CTA (the form of 4 / 7): tensor copies of a row's
@@ -1559,6 +1725,170 @@ static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// column pass with warp FFTs (N = 1024, 2048; row-major field).  Two groups of
+// four warps per CTA (one CTA per SM) share a ring of three stages, each
+// holding a tile of 4 columns x N rows moved by tensor copies (boxes of 4
+// columns x 256 rows; the stage laid out [N rows][4 columns]).  The CTA's
+// tiles t = 0, 1, 2, ... (pairs of neighbouring tiles) go to group t % 2 and
+// stage t % 3: two stages are being transformed while the third is loading.  Lane (a = lane / 4, c =
+// lane % 4) of warp w is lane j = 8 w + a of column c's warp FFT: the
+// instruction that reads 8 rows x 4 columns of the stage (no bank conflict)
+// hands lane j the rows j + 32 m, the warp FFT's layout.  Each transform
+// exchanges once through the group's current stage (the column's N slots,
+// swizzled by wfft_slot) on the group's named barrier.  Once the inverse's
+// exchange has been read the stage is free: the group's first thread loads
+// tile t + 3 into it (for the other group) while the group stores its
+// result from registers, 8 rows x 4 columns (eight full 32-byte sectors)
+// per store instruction.  A consumer waits first on the stage's `issued`
+// mbarrier (the load of its use was issued), then on its `full` mbarrier, so
+// the parity it waits on is never two phases old.  Every wait is bounded
+// (error word, then a drain of the copies in flight).
+// ---------------------------------------------------------------------------
+template <int N>
+struct ColWarp {
+  static constexpr int R = N / 32;
+  static constexpr int G = 2;                                     // groups of four warps
+  static constexpr int S = 3;                                     // stages
+  static constexpr size_t TILE = (size_t)N * 4 * sizeof(float2);  // one stage
+  static constexpr size_t TWT = (size_t)R * 32 * sizeof(float2);  // W_N^(j kb) per lane j
+  static constexpr size_t HY = (size_t)N * sizeof(float2);        // the step's hy
+  static constexpr size_t SMEM = 128 + S * TILE + TWT + HY;
+  static constexpr int BOX_ROWS = 256;
+  static constexpr int BOXES = N / BOX_ROWS;
+};
+
+template <int N>
+__global__ void __launch_bounds__(ColWarp<N>::G * 128, 1)
+col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
+  using Cfg = ColWarp<N>;
+  constexpr int R = Cfg::R;
+  constexpr int G = Cfg::G;
+  constexpr int S = Cfg::S;
+  constexpr int NCT = N / 4;  // tiles per realisation
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[S], issued_bar[S];
+  __shared__ int n_issued[S], n_consumed[S];  // loads issued / waited for, per stage
+  const int tid = threadIdx.x;
+  const int g = tid >> 7, gt = tid & 127;
+  const int w = gt >> 5, lane = tid & 31;
+  const int a4 = lane >> 2, c = lane & 3;
+  const int j = 8 * w + a4;  // lane of column c's transform
+  const int bar = 1 + g;
+  unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
+  float2* twt = reinterpret_cast<float2*>(sbase + (size_t)S * Cfg::TILE);
+  float2* hys = twt + R * 32;
+  for (int i = tid; i < R * 32; i += blockDim.x) twt[i] = a.tw[(i >> 5) * (i & 31)];
+  if (!a.inv_only)
+    for (int i = tid; i < N; i += blockDim.x) hys[i] = a.hy[i];
+  // the CTA's tiles: pairs of neighbouring tiles, item(t) = 2 (blockIdx.x + (t / 2) gridDim.x) + t % 2, so
+  // that the two groups work on neighbouring columns (n_items is even: N / 4 tiles per realisation)
+  const int n_pairs = n_items / 2;
+  const int n_t = (int)blockIdx.x < n_pairs ? 2 * ((n_pairs - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) : 0;
+  auto item_of = [&](int t) { return 2 * ((int)blockIdx.x + (t >> 1) * (int)gridDim.x) + (t & 1); };
+  auto stage_addr = [&](int st) { return (uint32_t)__cvta_generic_to_shared(sbase + (size_t)st * Cfg::TILE); };
+  auto bar_addr = [&](uint64_t* b, int st) { return (uint32_t)__cvta_generic_to_shared(&b[st]); };
+  auto load = [&](int t) {  // by one thread; then arrives on the stage's `issued` barrier
+    const int st = t % S;
+    const int item = item_of(t);
+    const int r = item / NCT, x0 = (item - r * NCT) * 4;
+    const uint32_t fb = bar_addr(full_bar, st);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::TILE)
+                 : "memory");
+#pragma unroll 1
+    for (int b = 0; b < Cfg::BOXES; ++b)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+          "[%5];\n" ::"r"(stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * 4 * sizeof(float2))),
+          "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(2 * x0), "r"(b * Cfg::BOX_ROWS), "r"(r), "r"(fb)
+          : "memory");
+    n_issued[st] += 1;
+    mbar_arrive_cta(bar_addr(issued_bar, st));
+  };
+  if (tid == 0) {
+    for (int st = 0; st < S; ++st) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_addr(full_bar, st)) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_addr(issued_bar, st)) : "memory");
+      n_issued[st] = 0;
+      n_consumed[st] = 0;
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    for (int t = 0; t < S && t < n_t; ++t) load(t);
+  }
+  __syncthreads();
+  const unsigned long long wait_ns = g_pass_wait_ns;
+  auto tw = [&](int kb) { return twt[kb * 32 + j]; };
+  for (int t = g; t < n_t; t += G) {
+    const int st = t % S, use = t / S;
+    float2* stg = reinterpret_cast<float2*>(sbase + (size_t)st * Cfg::TILE);
+    // the load of this use issued (by the other group after its tile t - 3, or at the start), then landed
+    const bool ok = pass_mbar_wait(bar_addr(issued_bar, st), (uint32_t)(use & 1), wait_ns) &&
+                    pass_mbar_wait(bar_addr(full_bar, st), (uint32_t)(use & 1), wait_ns);
+    if (!group_all(bar, 128, ok)) {
+      if (gt == 0) {
+        atomicExch(&g_pass_error, 1);
+        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      }
+      break;
+    }
+    if (gt == 0) n_consumed[st] = use + 1;
+    const int item = item_of(t);
+    const int r = item / NCT, x0 = (item - r * NCT) * 4;
+    float2 v[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) v[m] = stg[(32 * m + 8 * w + a4) * 4 + c];
+    group_sync(bar, 128);  // the exchanges below overwrite the tile
+    float2* xc = stg + c * N;  // column c's exchange rows
+    auto put = [&](int kb, float2 y) { xc[wfft_slot(kb, j, (kb & 3) | (c << 2))] = y; };
+    auto get = [&](int h, int jj) {
+      const int kb = j + 32 * h;
+      return xc[wfft_slot(kb, jj, (kb & 3) | (c << 2))];
+    };
+    if (!a.inv_only) {
+      wfft_stage1<R, -1>(v, tw, put);
+      group_sync(bar, 128);
+      wfft_stage2<R, -1>(v, get);
+      group_sync(bar, 128);  // every lane has read its rows before the inverse stores
+      // the transfer function H = hy[ky] hx[kx], applied as the inverse gathers its inputs
+      const float2 hx = a.hx[x0 + c];
+      wfft_stage1<R, 1>(v, tw, put, [&](int q, float2 y) { return cmul(y, cmul(hys[j + 32 * q], hx)); });
+    } else {
+      wfft_stage1<R, 1>(v, tw, put);
+    }
+    group_sync(bar, 128);
+    wfft_stage2<R, 1>(v, get);
+    // the stage is free once every lane has read its rows: tile t + 3 goes into it
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    group_sync(bar, 128);
+    if (gt == 0 && t + S < n_t) load(t + S);
+    float2* f = a.field + (size_t)r * N * N + x0 + c;
+#pragma unroll
+    for (int q = 0; q < R; ++q) f[(size_t)(32 * q + 8 * w + a4) * N] = v[q];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // no copy may land after the CTA leaves: a load issued and never waited for (a group left early)
+    for (int st = 0; st < S; ++st)
+      if (n_issued[st] > n_consumed[st]) pass_mbar_wait(bar_addr(full_bar, st), (uint32_t)(n_consumed[st] & 1));
+  }
+}
+
+template <int N>
+static cudaError_t col_wfft_launch(int B, const ColArgs& a, cudaStream_t st) {
+  using Cfg = ColWarp<N>;
+  alignas(128) CUtensorMap map;
+  if (!encode_field_tiles(&map, a.field, N, B, 4, Cfg::BOX_ROWS)) return cudaErrorNotSupported;
+  static LaunchCache cache;
+  const int threads = Cfg::G * 128;
+  int grid_max = 0;
+  cudaError_t e = cache.get(col_pass_wfft_kernel<N>, threads, Cfg::SMEM, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_items = B * (N / 4);
+  const int grid = std::max(1, std::min(n_items / 2, grid_max));
+  col_pass_wfft_kernel<N><<<grid, threads, Cfg::SMEM, st>>>(map, a, n_items);
+  return cudaGetLastError();
+}
+
 template <int N, int C, int TWREC>
 static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
   static LaunchCache cache;
@@ -1659,6 +1989,13 @@ cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t 
       case 1024: return col_tiled_dispatch<1024>(B, a, st);
       case 2048: return col_tiled_dispatch<2048>(B, a, st);
     }
+    return cudaErrorInvalidValue;
+  }
+  if (a.variant == 10) {
+    // warp FFTs, tiles of 4 columns (C does not apply)
+    if (!aligned16(a.field)) return cudaErrorInvalidValue;
+    if (N == 1024) return col_wfft_launch<1024>(B, a, st);
+    if (N == 2048) return col_wfft_launch<2048>(B, a, st);
     return cudaErrorInvalidValue;
   }
   if (C <= 0) C = col_tile_default(N);

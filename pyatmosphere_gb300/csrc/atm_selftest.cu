@@ -3,6 +3,7 @@
 // here are the same __host__ __device__ code the kernels run; the Stockham
 // stages are executed thread by thread between the points where the kernels
 // synchronise.  Used by the CPU test suite; needs no GPU.
+#include <type_traits>
 #include <vector>
 
 #include "atm_common.cuh"
@@ -71,9 +72,64 @@ int host_fft(int dir, const float* in, float* out) {
   return 0;
 }
 
+// the warp FFT of length N = 32 R, its 32 lanes emulated one after another on
+// each side of the exchange.  mode 0: the exchange swizzle of a warp that
+// holds all 32 lanes (row pass); mode 1 + c: that of column c of a
+// four-column group (column pass)
+template <int R>
+int host_wfft(int dir, int mode, const float* in, float* out) {
+  constexpr int N = 32 * R;
+  std::vector<float2> tw(N), twt(R * 32), xbuf(N);
+  for (int i = 0; i < N; ++i) {
+    const double a = -2.0 * 3.14159265358979323846 * i / N;
+    tw[i] = make_float2((float)cos(a), (float)sin(a));
+  }
+  for (int i = 0; i < R * 32; ++i) twt[i] = tw[(i >> 5) * (i & 31)];
+  auto sw = [&](int kb) { return mode == 0 ? (kb & 15) : ((kb & 3) | ((mode - 1) << 2)); };
+  struct Lane {
+    float2 v[R];
+  };
+  std::vector<Lane> L(32);
+  for (int j = 0; j < 32; ++j)
+    for (int m = 0; m < R; ++m) L[j].v[m] = make_float2(in[2 * (j + 32 * m)], in[2 * (j + 32 * m) + 1]);
+  auto run = [&](auto dirc) {
+    constexpr int D = decltype(dirc)::value;
+    for (int j = 0; j < 32; ++j)
+      atm::wfft_stage1<R, D>(
+          L[j].v, [&](int kb) { return twt[kb * 32 + j]; },
+          [&](int kb, float2 y) { xbuf[atm::wfft_slot(kb, j, sw(kb))] = y; });
+    for (int j = 0; j < 32; ++j)
+      atm::wfft_stage2<R, D>(L[j].v, [&](int h, int jj) {
+        const int kb = j + 32 * h;
+        return xbuf[atm::wfft_slot(kb, jj, sw(kb))];
+      });
+  };
+  if (dir < 0)
+    run(std::integral_constant<int, -1>{});
+  else
+    run(std::integral_constant<int, 1>{});
+  for (int j = 0; j < 32; ++j)
+    for (int q = 0; q < R; ++q) {
+      out[2 * (j + 32 * q)] = L[j].v[q].x;
+      out[2 * (j + 32 * q) + 1] = L[j].v[q].y;
+    }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+// length-N warp FFT (N = 1024 or 2048; dir = -1 forward, +1 unnormalised
+// inverse) of interleaved complex data, exchange swizzle `mode` (see host_wfft)
+int atm_selftest_wfft(int N, int dir, int mode, const float* in, float* out) {
+  if (mode < 0 || mode > 4) return -1;
+  switch (N) {
+    case 1024: return host_wfft<32>(dir, mode, in, out);
+    case 2048: return host_wfft<64>(dir, mode, in, out);
+  }
+  return -1;
+}
 
 // length-N FFT (dir = -1 forward, +1 unnormalised inverse) of interleaved complex data
 int atm_selftest_fft(int N, int dir, const float* in, float* out) {

@@ -221,6 +221,8 @@ def load_selftest(path: str = SELFTEST_PATH):
     lib.atm_selftest_fft_twrec.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.atm_selftest_fft_twreg.restype = ctypes.c_int
     lib.atm_selftest_fft_twreg.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.atm_selftest_wfft.restype = ctypes.c_int
+    lib.atm_selftest_wfft.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.atm_selftest_bessel.restype = ctypes.c_int
     lib.atm_selftest_bessel.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
     lib.atm_selftest_turns.restype = ctypes.c_int

@@ -72,6 +72,74 @@ def test_kernel_fft_arithmetic_on_host(built, N):
         np.testing.assert_array_equal(out3, out2)
 
 
+@pytest.mark.parametrize("N", [1024, 2048])
+def test_warp_fft_arithmetic_on_host(built, N):
+    """The warp FFT of the row / column pass forms 11 / 10 (one exchange per
+    transform, lanes emulated on the host) against numpy in FP64; every
+    exchange swizzle gives the same bits."""
+    from pyatmosphere_gb300.engine._lib import load_selftest
+    lib = load_selftest(built["selftest"])
+    rng = np.random.default_rng(N + 1)
+    x = (rng.standard_normal(N) + 1j * rng.standard_normal(N)).astype(np.complex64)
+    for d in (-1, 1):
+        ref = np.fft.fft(x.astype(np.complex128)) if d < 0 else np.fft.ifft(x.astype(np.complex128)) * N
+        outs = []
+        for mode in range(5):
+            out = np.zeros(N, np.complex64)
+            assert lib.atm_selftest_wfft(N, d, mode, x.ctypes.data, out.ctypes.data) == 0
+            outs.append(out)
+        assert np.linalg.norm(outs[0] - ref) / np.linalg.norm(ref) < 3e-7
+        for out in outs[1:]:
+            np.testing.assert_array_equal(out, outs[0])
+    assert lib.atm_selftest_wfft(512, -1, 0, x.ctypes.data, x.ctypes.data) == -1
+
+
+def _wfft_slot(kb, jj, sw):
+    return kb * 32 + (jj ^ sw)
+
+
+@pytest.mark.parametrize("R", [32, 64])
+def test_warp_fft_exchange_is_bank_conflict_free(R):
+    """Each half warp's eight-byte stores and loads of the warp-FFT exchange
+    land on 16 distinct bank pairs, for the row pass (a warp = one transform's
+    32 lanes) and the column pass (a warp = 8 lanes of each of 4 columns);
+    the slots of a transform are a permutation of its N slots."""
+    N = 32 * R
+    half_warps = [range(0, 16), range(16, 32)]
+    # row pass: lane j of the warp is the transform's lane j
+    for kb in range(R):
+        for hw in half_warps:
+            assert len({_wfft_slot(kb, j, kb & 15) % 16 for j in hw}) == 16
+    for h in range(R // 32):
+        for jj in range(32):
+            for hw in half_warps:
+                assert len({_wfft_slot(j + 32 * h, jj, (j + 32 * h) & 15) % 16 for j in hw}) == 16
+    assert sorted(_wfft_slot(kb, jj, kb & 15) for kb in range(R) for jj in range(32)) == list(range(N))
+    # column pass: lane (a = lane // 4, c = lane % 4) of warp w is lane j = 8 w + a of column c,
+    # whose exchange rows start at slot c N
+    for w in range(4):
+        for kb in range(R):
+            for hw in half_warps:
+                slots = {(c * N + _wfft_slot(kb, 8 * w + lane // 4, (kb & 3) | (c << 2))) % 16
+                         for lane in hw for c in [lane % 4]}
+                assert len(slots) == 16
+        for h in range(R // 32):
+            for jj in range(32):
+                for hw in half_warps:
+                    slots = set()
+                    for lane in hw:
+                        c, kb = lane % 4, 8 * w + lane // 4 + 32 * h
+                        slots.add((c * N + _wfft_slot(kb, jj, (kb & 3) | (c << 2))) % 16)
+                    assert len(slots) == 16
+    for c in range(4):
+        assert sorted(_wfft_slot(kb, jj, (kb & 3) | (c << 2)) for kb in range(R) for jj in range(32)) == list(range(N))
+    # the tile read / write-back: instruction m of warp w covers 32 consecutive slots
+    for w in range(4):
+        for m in range(R):
+            slots = [(32 * m + 8 * w + lane // 4) * 4 + lane % 4 for lane in range(32)]
+            assert slots == list(range(slots[0], slots[0] + 32))
+
+
 def test_bessel_coefficients_on_host(built):
     from scipy.special import jv
     from pyatmosphere_gb300.engine._lib import load_selftest

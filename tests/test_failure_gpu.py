@@ -41,13 +41,16 @@ def _setup(torch, N, flags=0, variants=None, R=2):
     return plan, [torch.from_numpy(a).cuda() for a in arrs]
 
 
-@pytest.mark.parametrize("form", ["row-major TMA forms", "tiled"])
+@pytest.mark.parametrize("form", ["row-major TMA forms", "tiled", "warp-FFT column groups"])
 def test_wait_budget_runs_out_then_recovers(torch_cuda, form):
     from pyatmosphere_gb300.engine import _lib
     from pyatmosphere_gb300.engine.plan import set_wait_budget
     torch = torch_cuda
     if form == "tiled":
         plan, dev = _setup(torch, 512, flags=_lib.FLAG_TILED)
+    elif form == "warp-FFT column groups":
+        # column variant 10: two groups handing stages to each other through mbarriers
+        plan, dev = _setup(torch, 1024, variants=(3, 4, 10))
     else:
         plan, dev = _setup(torch, 512, variants=(3, 4, 3))  # bulk-copied rows, TMA column tiles
     assert plan.info["gemm_form"] == 3  # persistent TMA tensor-core GEMM
