@@ -635,15 +635,18 @@ def run_gb300(args, rank, world, local_rank):
             "kernels": {k: {"ms": r3(e["avg_ms"]), "n": e["launches"], "share": r3(e["share"]),
                             **({"frac": r3(e["frac"]), "bound": e["bound"]} if "frac" in e else {})}
                         for k, e in kernels.items()},
-            "mixed": None if mixed is None else {k: mixed[k] for k in ("channels", "realisations_per_channel",
-                                                                      "seconds", "channels_per_s",
-                                                                      "realisations_per_s", "one_graph")
+            "mixed": None if mixed is None else {k: r3(mixed[k]) if isinstance(mixed[k], float) else mixed[k]
+                                                 for k in ("channels", "realisations_per_channel", "graph_launches",
+                                                           "seconds", "channels_per_s", "realisations_per_s",
+                                                           "setup_s", "capture_s")
                                                  if k in mixed},
-            "surrogate": None if sur is None else {k: r3(sur[k]) if isinstance(sur[k], float) else sur[k]
-                                                   for k in ("queries_per_s", "mixed_queries_per_s",
-                                                             "answered_frac", "frac_ks_le_0.02",
-                                                             "ks_binned_median", "heldout_answered_frac")
-                                                   if k in sur},
+            "surrogate": None if sur is None else dict(
+                {k: r3(sur[k]) if isinstance(sur[k], float) else sur[k]
+                 for k in ("queries_per_s", "e2e_queries_per_s", "mixed_queries_per_s", "simulated_queries_per_s",
+                           "answered_frac", "heldout_answered_frac", "frac_ks_le_0.02", "ks_binned_median",
+                           "ks_continuous_median", "all_frac_ks_le_0.02")
+                 if k in sur},
+                mlp_tflops=r3(sur["mlp"]["tflops"]), mlp_frac_of_bf16_peak=r3(sur["mlp"]["frac_of_bf16_peak"])),
             "plain": {"value": r3(plain), "batched_over_plain": r3(value / world / plain) if plain else None,
                       "torch_reference_algorithm": r3(torch_ref),
                       "batched_over_torch_reference": r3(value / world / torch_ref) if torch_ref else None},
