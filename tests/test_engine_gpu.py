@@ -356,3 +356,36 @@ def test_product_twiddle_column_pass_matches_oracle(torch_cuda):
     plan.run(*to_dev(torch, rho, theta, value), field_out=field)
     res, u = o.simulate(spec, rho, theta, value, return_field=True)
     assert o.rel_l2(field.cpu().numpy()[0], u) < FIELD_TOL
+
+
+@pytest.mark.parametrize("N", [1024, 2048])
+def test_warp_fft_passes_match_oracle(torch_cuda, N):
+    """The warp-FFT forms (row variant 11, column variant 10) keep the FP64
+    parity bound on fields and measures, at both grid sizes they serve, for a
+    batch of 3 (the column pass's two groups on neighbouring tiles of several
+    realisations), and through atm_vacuum on the same plan."""
+    torch = torch_cuda
+    spec = o.ChannelSpec(N=N, delta=3.0 / N, w0=0.1, length=20e3, count=4, Cn2=1e-15, pupil_radius=0.15)
+    R = 3
+    plan, base = make_plan(spec, batch=R)
+    plan.set_variants(11, 4, 10)
+    rho, theta, value = spectra(spec, base, seed=77, R=R)
+    field = torch.empty((R, N, N), dtype=torch.complex64, device="cuda")
+    got = plan.run(*to_dev(torch, rho, theta, value), field_out=field).cpu().numpy()
+    plan.check()
+    f = field.cpu().numpy()
+    for r in range(R):
+        res, u = o.simulate(spec, rho[r:r + 1], theta[r:r + 1], value[r:r + 1], return_field=True)
+        res = {r: res[0]}
+        assert o.rel_l2(f[r], u) < FIELD_TOL
+        assert got[r, 0] == pytest.approx(res[r]["eta_total"], rel=1e-5)
+        assert got[r, 8] == pytest.approx(res[r]["eta_0"], rel=1e-5)
+        assert got[r, 3] == pytest.approx(res[r]["mean_x2"], rel=1e-5)
+    # a vacuum step on the same plan (atm_vacuum runs the plan's column form)
+    g = o.gaussian_source(N, spec.delta, spec.wvl, spec.w0, spec.F0)
+    dev = torch.from_numpy(np.stack([g] * 2).astype(np.complex64)).cuda()
+    plan.vacuum(dev, 5e3)
+    ref = o.vacuum(g, 5e3, spec.k, spec.delta)
+    for r in range(2):
+        assert o.rel_l2(dev[r].cpu().numpy(), ref) < FIELD_TOL
+    plan.close()
