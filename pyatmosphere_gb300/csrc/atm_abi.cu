@@ -1138,7 +1138,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
     if (C * (N / 16) > 512 || C > N) continue;
     if (pl->tiled && C != 4) continue;
     std::vector<int> col_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9} : std::vector<int>{0, 1, 2, 3, 4, 7};
-    if (!pl->tiled && warp_fft && C == 4) col_forms.push_back(10);
+    if (warp_fft && C == 4) col_forms.push_back(pl->tiled ? 13 : 10);
     for (int v : col_forms) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
@@ -1173,8 +1173,9 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
     // a tiled plan's field is only understood by the tiled forms
     if (row_variant != 5 && row_variant != 6 && row_variant != 8 && row_variant != 9 && row_variant != 10)
       return fail(ATM_ERR_INVALID, "row_variant %d: a tiled plan takes 5, 6, 8, 9 or 10", row_variant);
-    if ((col_variant != 5 && col_variant != 6 && col_variant != 8 && col_variant != 9) || col_tile != 4)
-      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5, 6, 8 or 9 with col_tile 4");
+    const bool warp13 = col_variant == 13 && (pl->N == 1024 || pl->N == 2048);
+    if ((col_variant != 5 && col_variant != 6 && col_variant != 8 && col_variant != 9 && !warp13) || col_tile != 4)
+      return fail(ATM_ERR_INVALID, "a tiled plan takes col_variant 5, 6, 8 or 9 (13 at N = 1024, 2048) with col_tile 4");
     pl->row_variant = row_variant;
     pl->col_variant = col_variant;
     return ATM_OK;

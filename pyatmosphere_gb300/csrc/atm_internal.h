@@ -222,6 +222,7 @@ void tc_plan_destroy(TcPlan* p);
 // tensor map (128-byte storage of a CUtensorMap) of a complex64 field [B][N][N]
 // in boxes of C columns x box_rows rows; false without an encoder or alignment
 bool encode_field_tiles(void* map, const float2* field, int N, int B, int C, int box_rows);
+bool encode_tiled_cols_plain(void* map, const float2* field, int N, int B, int box_blocks);
 // tensor maps of a tiled field [B][N][N] (128-byte blocks, 128-byte swizzle):
 // by_rows: 3-D {32, N^2/16, B}, consecutive blocks of a block row (boxes of box_blocks blocks);
 // otherwise 3-D, one block column (boxes of box_blocks blocks down the column)

@@ -1747,7 +1747,7 @@ static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
 // waits on is never two phases old.  Every wait is bounded (error word, then
 // a drain of the copies in flight).
 // ---------------------------------------------------------------------------
-template <int N>
+template <int N, int TILED = 0>
 struct ColWarp {
   static constexpr int R = N / 32;
   static constexpr int G = 2;                                     // groups of four warps
@@ -1756,14 +1756,17 @@ struct ColWarp {
   static constexpr size_t TWT = (size_t)R * 32 * sizeof(float2);  // W_N^(j kb) per lane j
   static constexpr size_t HY = (size_t)N * sizeof(float2);        // the step's hy
   static constexpr size_t SMEM = 128 + S * TILE + TWT + HY;
-  static constexpr int BOX_ROWS = 256;
+  // row-major field: boxes of 4 columns x 256 rows; tiled field: boxes of 256 blocks (1024 rows) of
+  // one block column, whole 128-byte blocks
+  static constexpr int BOX_ROWS = TILED ? (N < 1024 ? N : 1024) : 256;
   static constexpr int BOXES = N / BOX_ROWS;
 };
 
-template <int N, int TSTORE>
+template <int N, int TSTORE, int TILED = 0>
 __global__ void __launch_bounds__(ColWarp<N>::G * 128, 1)
 col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_items) {
-  using Cfg = ColWarp<N>;
+  using Cfg = ColWarp<N, TILED>;
+  static_assert(!TILED || TSTORE, "the tiled layout is written back by tensor stores");
   constexpr int R = Cfg::R;
   constexpr int G = Cfg::G;
   constexpr int S = Cfg::S;
@@ -1798,12 +1801,17 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::TILE)
                  : "memory");
 #pragma unroll 1
-    for (int b = 0; b < Cfg::BOXES; ++b)
+    for (int b = 0; b < Cfg::BOXES; ++b) {
+      // row-major: {2 x0 floats, rows, realisation}; tiled: {0, block column, block row of the batch}
+      const int c0 = TILED ? 0 : 2 * x0;
+      const int c1 = TILED ? x0 / 4 : b * Cfg::BOX_ROWS;
+      const int c2 = TILED ? r * (N / 4) + b * (Cfg::BOX_ROWS / 4) : r;
       asm volatile(
           "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
           "[%5];\n" ::"r"(stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * 4 * sizeof(float2))),
-          "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(2 * x0), "r"(b * Cfg::BOX_ROWS), "r"(r), "r"(fb)
+          "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(c0), "r"(c1), "r"(c2), "r"(fb)
           : "memory");
+    }
     n_issued[st] += 1;
     mbar_arrive_cta(bar_addr(issued_bar, st));
   };
@@ -1870,8 +1878,9 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
       if (gt == 0) {
 #pragma unroll 1
         for (int b = 0; b < Cfg::BOXES; ++b)
-          tma_store_col(&tiles, stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * 4 * sizeof(float2)), 2 * x0,
-                        b * Cfg::BOX_ROWS, r);
+          tma_store_col(&tiles, stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * 4 * sizeof(float2)),
+                        TILED ? 0 : 2 * x0, TILED ? x0 / 4 : b * Cfg::BOX_ROWS,
+                        TILED ? r * (N / 4) + b * (Cfg::BOX_ROWS / 4) : r);
         asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
         if (t + S < n_t) {
           asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
@@ -1897,19 +1906,21 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
   }
 }
 
-template <int N, int TSTORE>
+template <int N, int TSTORE, int TILED = 0>
 static cudaError_t col_wfft_launch(int B, const ColArgs& a, cudaStream_t st) {
-  using Cfg = ColWarp<N>;
+  using Cfg = ColWarp<N, TILED>;
   alignas(128) CUtensorMap map;
-  if (!encode_field_tiles(&map, a.field, N, B, 4, Cfg::BOX_ROWS)) return cudaErrorNotSupported;
+  const bool mapped = TILED ? encode_tiled_cols_plain(&map, a.field, N, B, Cfg::BOX_ROWS / 4)
+                            : encode_field_tiles(&map, a.field, N, B, 4, Cfg::BOX_ROWS);
+  if (!mapped) return cudaErrorNotSupported;
   static LaunchCache cache;
   const int threads = Cfg::G * 128;
   int grid_max = 0;
-  cudaError_t e = cache.get(col_pass_wfft_kernel<N, TSTORE>, threads, Cfg::SMEM, &grid_max);
+  cudaError_t e = cache.get(col_pass_wfft_kernel<N, TSTORE, TILED>, threads, Cfg::SMEM, &grid_max);
   if (e != cudaSuccess) return e;
   const int n_items = B * (N / 4);
   const int grid = std::max(1, std::min(n_items / 2, grid_max));
-  col_pass_wfft_kernel<N, TSTORE><<<grid, threads, Cfg::SMEM, st>>>(map, a, n_items);
+  col_pass_wfft_kernel<N, TSTORE, TILED><<<grid, threads, Cfg::SMEM, st>>>(map, a, n_items);
   return cudaGetLastError();
 }
 
@@ -1994,6 +2005,8 @@ static cudaError_t col_dispatch(int C, int B, const ColArgs& a, cudaStream_t st)
 
 template <int N>
 static cudaError_t col_tiled_dispatch(int B, const ColArgs& a, cudaStream_t st) {
+  if constexpr (N == 1024 || N == 2048)
+    if (a.variant == 13) return col_wfft_launch<N, 1, 1>(B, a, st);  // warp FFTs on whole 128-byte blocks
   switch (a.variant) {
     case 5: return col_tiled_launch<N>(B, a, st);
     case 6: return col_groups_launch<N, 0>(B, a, st);
@@ -2004,7 +2017,7 @@ static cudaError_t col_tiled_dispatch(int B, const ColArgs& a, cudaStream_t st) 
 }
 
 cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t st) {
-  if (a.variant == 5 || a.variant == 6 || a.variant == 8 || a.variant == 9) {
+  if (a.variant == 5 || a.variant == 6 || a.variant == 8 || a.variant == 9 || a.variant == 13) {
     // the tiled layout: tiles are block columns (4 columns); C does not apply.
     // 6: table twiddles, 9: twiddles formed from table bases, 8: from bases in registers
     if (!aligned16(a.field)) return cudaErrorInvalidValue;

@@ -1026,6 +1026,21 @@ bool encode_tiled_field(void* map, const float2* field, int N, int B, bool by_ro
             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// the block columns of a tiled field without swizzle: a box of box_blocks
+// blocks of one block column lands as [4 box_blocks rows][4 columns], the
+// layout of a row-major column tile (the warp-FFT column pass reads either)
+bool encode_tiled_cols_plain(void* map, const float2* field, int N, int B, int box_blocks) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !map || ((uintptr_t)field & 127) != 0 || N < 16 || box_blocks < 1 || box_blocks > 256) return false;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const cuuint64_t dims[3] = {32, (cuuint64_t)N / 4, (cuuint64_t)B * N / 4};
+  const cuuint64_t strides[2] = {128, (cuuint64_t)N * 32};
+  const cuuint32_t box[3] = {32, 1, (cuuint32_t)box_blocks};
+  return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(field), dims,
+            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 struct TcPlan {
   TmaOperands ops;
   int S, M, Nn, Kp;

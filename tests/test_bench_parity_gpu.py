@@ -7,7 +7,8 @@ B = 256, default flags (tensor-core TMA GEMM with the 1-D phase fold).  The
 launch forms that atm_autotune can pick are pinned with set_variants, one
 parametrised case each: the row-major forms (row 4, 7 or 11, column tile 4,
 column 3, 4, 7 or 10; 11 and 10 are the warp-FFT forms) and the tiled forms
-(row 6, 8 or 9, column 6, 8 or 9).  For each:
+(row 6, 8, 9 or 10, column 6, 8, 9 or 13, the warp-FFT form on whole 128-byte
+blocks).  For each:
   * 16 realisations against the complex128 oracle: field rel-L2 <= 1e-4 each
     (field_out of a B = 16 plan with the same forms), eta and the second
     moments to 1e-5 relative, the centroids and mean_xy to 1e-5 of their
@@ -36,7 +37,8 @@ pytestmark = pytest.mark.gpu
 BENCH_SEED = 2024
 FORMS = [("row-major", 0, (4, 4, 4)), ("row-major", 0, (4, 4, 3)), ("row-major", 0, (7, 4, 7)),
          ("row-major", 0, (11, 4, 10)), ("row-major", 0, (11, 4, 7)), ("row-major", 0, (7, 4, 10)),
-         ("tiled", 64, (6, 4, 6)), ("tiled", 64, (8, 4, 8)), ("tiled", 64, (6, 4, 9)), ("tiled", 64, (9, 4, 9))]
+         ("tiled", 64, (6, 4, 6)), ("tiled", 64, (8, 4, 8)), ("tiled", 64, (6, 4, 9)), ("tiled", 64, (9, 4, 9)),
+         ("tiled", 64, (9, 4, 13)), ("tiled", 64, (10, 4, 13))]
 
 
 def _bench_spec():
