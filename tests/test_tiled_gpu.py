@@ -129,7 +129,8 @@ def test_tiled_autotune_keeps_tiled_forms(torch_cuda):
     spec = o.ChannelSpec(N=2048, delta=1.5e-3, count=2, points=256, length=10e3)
     _, tl, _ = _plans(spec, 2)
     choice = tl.autotune(repeats=1)
-    assert choice["row_variant"] in (5, 6, 8, 9, 10) and choice["col_variant"] in (5, 6, 8, 9)
+    # 13: the warp-FFT column groups on whole 128-byte blocks (N = 1024, 2048)
+    assert choice["row_variant"] in (5, 6, 8, 9, 10) and choice["col_variant"] in (5, 6, 8, 9, 13)
     assert choice["col_tile"] == 4
     assert tl.info["tiled"] == 1
 
