@@ -122,6 +122,7 @@ class PointSimulator:
         self.value = torch.empty((B, n, P), dtype=torch.complex64, device=self.device)
         self.out = None
         self._base_key = None
+        self._variants = None  # launch forms atm_autotune picked for this size and batch (l0 does not change them)
 
     def _geometry(self, q):
         cfg = self.cfg
@@ -145,6 +146,12 @@ class PointSimulator:
                 self.plan.close()
             self.plan = EnginePlan(cfg.N, self.delta, float(q["wvl"]), float(q["w0"]), F0, pos, L, **kw)
             self._base_key = key
+            # the FFT-pass launch forms: tuned once, then reused by the plans of later spectral grids
+            if self._variants is None:
+                t = self.plan.autotune(repeats=2)
+                self._variants = (t["row_variant"], t["col_tile"], t["col_variant"])
+            else:
+                self.plan.set_variants(*self._variants)
         else:
             self.plan.update(float(q["wvl"]), float(q["w0"]), F0, pos, L, pupils=[(float(q["aperture"]),)])
         model = MVKModel(Cn2=float(q["Cn2"]), l0=float(q["l0"]), L0=float(q["L0"]))
