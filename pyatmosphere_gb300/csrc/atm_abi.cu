@@ -1115,7 +1115,8 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   double best_row = -1.0;
   int row_variant = 0;
   // a tiled plan chooses among the tiled forms only (the others do not know its layout)
-  const bool warp_fft = N == 1024 || N == 2048;  // row 11 / column 10: warp FFTs
+  const bool warp_fft = N == 1024 || N == 2048;         // row 11: warp FFTs
+  const bool col_warp = warp_fft || N == 4096;          // column 10: warp FFTs (64-lane transforms at 4096)
   std::vector<int> row_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9, 10} : std::vector<int>{0, 1, 2, 3, 4, 7};
   if (!pl->tiled && warp_fft) row_forms.push_back(11);
   for (int v : row_forms) {
@@ -1138,7 +1139,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
     if (C * (N / 16) > 512 || C > N) continue;
     if (pl->tiled && C != 4) continue;
     std::vector<int> col_forms = pl->tiled ? std::vector<int>{5, 6, 8, 9} : std::vector<int>{0, 1, 2, 3, 4, 7};
-    if (warp_fft && C == 4) col_forms.push_back(pl->tiled ? 13 : 10);
+    if (pl->tiled && warp_fft && C == 4) col_forms.push_back(13);
     for (int v : col_forms) {
       ca.variant = v;
       const double ms = time_it([&] { return atm::launch_col_pass(N, batch, C, ca, st); });
@@ -1147,6 +1148,16 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
         col_tile = C;
         col_variant = v;
       }
+    }
+  }
+  if (!pl->tiled && col_warp) {
+    // the warp-FFT column groups choose their own tile (4 columns, 2 at 4096); recorded as column tile 4
+    ca.variant = 10;
+    const double ms = time_it([&] { return atm::launch_col_pass(N, batch, 4, ca, st); });
+    if (ms >= 0 && (best_col < 0 || ms < best_col)) {
+      best_col = ms;
+      col_tile = 4;
+      col_variant = 10;
     }
   }
   cudaEventDestroy(e0);
@@ -1180,16 +1191,18 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
     pl->col_variant = col_variant;
     return ATM_OK;
   }
-  const bool warp_fft = pl->N == 1024 || pl->N == 2048;  // row 11 / column 10: warp FFTs
+  const bool warp_fft = pl->N == 1024 || pl->N == 2048;  // row 11: warp FFTs
+  const bool col_warp = warp_fft || pl->N == 4096;         // column 10: warp FFTs
   if (row_variant < 0 || (row_variant > 4 && row_variant != 7 && !(row_variant == 11 && warp_fft)))
     return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4, 7%s", row_variant, warp_fft ? " or 11" : "");
-  if (col_variant < 0 || (col_variant > 4 && col_variant != 7 && !(col_variant == 10 && warp_fft)))
-    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4, 7%s", col_variant, warp_fft ? " or 10" : "");
+  if (col_variant < 0 || (col_variant > 4 && col_variant != 7 && !(col_variant == 10 && col_warp)))
+    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4, 7%s", col_variant, col_warp ? " or 10" : "");
   if (col_variant == 10 && col_tile != 4)
     return fail(ATM_ERR_INVALID, "col_variant 10 takes col_tile 4");
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
     return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);
-  if (col_tile * (pl->N / 16) > 512 || col_tile > pl->N)
+  // (the warp-FFT column groups are 256 threads whatever the recorded tile)
+  if (col_variant != 10 && (col_tile * (pl->N / 16) > 512 || col_tile > pl->N))
     return fail(ATM_ERR_UNSUPPORTED, "col_tile %d exceeds 512 threads per CTA at N = %d", col_tile, pl->N);
   pl->row_variant = row_variant;
   pl->col_tile = col_tile;

@@ -554,17 +554,23 @@ ATM_HD void wfft_stage1(float2 (&v)[R], TwF&& tw, PutF&& put, PreF&& pre = PreF(
   });
 }
 
-// stage 2 of lane j: get(h, jj) returns Y[jj][j + 32 h]; output element q
-// (the transform's element j + 32 q) passes through post(q, y) as it is formed
-template <int R, int DIR, class GetF, class PostF = WfftNoPre>
+// stage 2 of lane j of an L-lane transform (L = 32 or 64): get(h, jj) returns
+// Y[jj][j + L h]; output element q (the transform's element j + L q) passes
+// through post(q, y) as it is formed.  With L lanes the derivation above
+// reads n = j + L m, k = kb + R ka, N = L R: stage 1 is the same DFT_R over
+// m with the twiddle W_N^(j kb), stage 2 a DFT_L over j per kb = j + L h.
+template <int R, int DIR, int L = 32, class GetF, class PostF = WfftNoPre>
 ATM_HD void wfft_stage2(float2 (&v)[R], GetF&& get, PostF&& post = PostF()) {
-  constexpr int H = R / 32;
+  static_assert(L == 32 || L == 64, "warp FFTs of 32 or 64 lanes");
+  constexpr int H = R / L;
+  static_assert(H >= 1 && H * L == R, "stage 2 needs R a multiple of L");
 #pragma unroll
   for (int h = 0; h < H; ++h) {
-    float2 u[32];
+    float2 u[L];
 #pragma unroll
-    for (int jj = 0; jj < 32; ++jj) u[jj] = get(h, jj);
-    dft_2l<4, 8, DIR>(u, WfftNoPre(), [&](int ka, float2 y) { v[h + H * ka] = post(h + H * ka, y); });
+    for (int jj = 0; jj < L; ++jj) u[jj] = get(h, jj);
+    dft_2l<WfftSplit<L>::R1, WfftSplit<L>::R2, DIR>(u, WfftNoPre(),
+                                                       [&](int ka, float2 y) { v[h + H * ka] = post(h + H * ka, y); });
   }
 }
 
@@ -575,6 +581,9 @@ ATM_HD void wfft_stage2(float2 (&v)[R], GetF&& get, PostF&& post = PostF()) {
 // swizzle of row kb: kb & 15 when the 32 lanes are one warp; (kb & 3) |
 // (c << 2) when a warp holds lanes of four transforms c (8 lanes each).
 ATM_HD int wfft_slot(int kb, int jj, int sw) { return kb * 32 + (jj ^ sw); }
+// the same for an L-lane transform: row kb of L slots
+template <int L>
+ATM_HD int wfft_slot_l(int kb, int jj, int sw) { return kb * L + (jj ^ sw); }
 
 // ---------------------------------------------------------------------------
 // fixed-point phase: turns(j) = frac(j * S + O) held as a 64-bit binary

@@ -1749,18 +1749,33 @@ static cudaError_t col_groups_launch(int B, const ColArgs& a, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 template <int N, int TILED = 0>
 struct ColWarp {
-  static constexpr int R = N / 32;
+  static constexpr int L = N == 4096 ? 64 : 32;                   // lanes of one column's transform
+  static constexpr int C = 128 / L;                               // columns per tile: a group of 4 warps
+  static constexpr int RW = 32 / C;                               // rows per warp and load instruction
+  static constexpr int R = N / L;                                 // elements per lane
+  static constexpr bool TW_REG = L == 64;                         // twiddles from per-lane register bases
   static constexpr int G = 2;                                     // groups of four warps
   static constexpr int S = 3;                                     // stages
-  static constexpr size_t TILE = (size_t)N * 4 * sizeof(float2);  // one stage
-  static constexpr size_t TWT = (size_t)R * 32 * sizeof(float2);  // W_N^(j kb) per lane j
+  static constexpr size_t TILE = (size_t)N * C * sizeof(float2);  // one stage
+  static constexpr size_t TWT = TW_REG ? 0 : (size_t)R * L * sizeof(float2);  // W_N^(j kb) per lane j
   static constexpr size_t HY = (size_t)N * sizeof(float2);        // the step's hy
   static constexpr size_t SMEM = 128 + S * TILE + TWT + HY;
-  // row-major field: boxes of 4 columns x 256 rows; tiled field: boxes of 256 blocks (1024 rows) of
+  // row-major field: boxes of C columns x 256 rows; tiled field: boxes of 256 blocks (1024 rows) of
   // one block column, whole 128-byte blocks
   static constexpr int BOX_ROWS = TILED ? (N < 1024 ? N : 1024) : 256;
   static constexpr int BOXES = N / BOX_ROWS;
+  static_assert(!TILED || C == 4, "the tiled layout's block columns are 4 columns wide");
+  static_assert(SMEM <= 227 * 1024, "stages exceed shared memory");
 };
+
+// exchange swizzle of row kb of column c (see wfft_slot): with 4 columns per
+// warp (8 lanes each) (kb & 3) | (c << 2), with 2 columns (16 lanes each)
+// (kb & 7) | (c << 3); either spreads a half warp's 8-byte stores of one kb
+// and its loads of one jj over 16 distinct bank pairs
+template <int C>
+__device__ __forceinline__ int wfft_col_swizzle(int kb, int c) {
+  return C == 4 ? ((kb & 3) | (c << 2)) : ((kb & 7) | (c << 3));
+}
 
 template <int N, int TSTORE, int TILED = 0>
 __global__ void __launch_bounds__(ColWarp<N>::G * 128, 1)
@@ -1768,26 +1783,37 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
   using Cfg = ColWarp<N, TILED>;
   static_assert(!TILED || TSTORE, "the tiled layout is written back by tensor stores");
   constexpr int R = Cfg::R;
+  constexpr int L = Cfg::L;
+  constexpr int C = Cfg::C;
   constexpr int G = Cfg::G;
   constexpr int S = Cfg::S;
-  constexpr int NCT = N / 4;  // tiles per realisation
+  constexpr int NCT = N / C;  // tiles per realisation
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[S], issued_bar[S];
   __shared__ int n_issued[S], n_consumed[S];  // loads issued / waited for, per stage
   const int tid = threadIdx.x;
   const int g = tid >> 7, gt = tid & 127;
   const int w = gt >> 5, lane = tid & 31;
-  const int a4 = lane >> 2, c = lane & 3;
-  const int j = 8 * w + a4;  // lane of column c's transform
+  const int a4 = lane / C, c = lane % C;
+  const int j = Cfg::RW * w + a4;  // lane of column c's transform
   const int bar = 1 + g;
   unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
   float2* twt = reinterpret_cast<float2*>(sbase + (size_t)S * Cfg::TILE);
-  float2* hys = twt + R * 32;
-  for (int i = tid; i < R * 32; i += blockDim.x) twt[i] = a.tw[(i >> 5) * (i & 31)];
+  float2* hys = twt + Cfg::TWT / sizeof(float2);
+  if constexpr (!Cfg::TW_REG)
+    for (int i = tid; i < R * L; i += blockDim.x) twt[i] = a.tw[(i / L) * (i % L)];  // (i / L)(i % L) < N
   if (!a.inv_only)
     for (int i = tid; i < N; i += blockDim.x) hys[i] = a.hy[i];
+  // twiddles of this lane for L = 64 (R = 64): W^(j kb) = W^(j (kb & 7)) W^(8 j (kb >> 3)); the eight
+  // W^(8 j i) stay in registers, W^(j (kb & 7)) comes from the table (L1 / L2), one per group of the
+  // stage's outputs (they are emitted with kb & 7 fixed within a group)
+  float2 twb[Cfg::TW_REG ? 8 : 1];
+  if constexpr (Cfg::TW_REG) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) twb[i] = a.tw[(8 * j * i) % N];
+  }
   // the CTA's tiles: pairs of neighbouring tiles, item(t) = 2 (blockIdx.x + (t / 2) gridDim.x) + t % 2, so
-  // that the two groups work on neighbouring columns (n_items is even: N / 4 tiles per realisation)
+  // that the two groups work on neighbouring columns (n_items is even: N / C tiles per realisation)
   const int n_pairs = n_items / 2;
   const int n_t = (int)blockIdx.x < n_pairs ? 2 * ((n_pairs - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) : 0;
   auto item_of = [&](int t) { return 2 * ((int)blockIdx.x + (t >> 1) * (int)gridDim.x) + (t & 1); };
@@ -1796,7 +1822,7 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
   auto load = [&](int t) {  // by one thread; then arrives on the stage's `issued` barrier
     const int st = t % S;
     const int item = item_of(t);
-    const int r = item / NCT, x0 = (item - r * NCT) * 4;
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
     const uint32_t fb = bar_addr(full_bar, st);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::TILE)
                  : "memory");
@@ -1808,7 +1834,7 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
       const int c2 = TILED ? r * (N / 4) + b * (Cfg::BOX_ROWS / 4) : r;
       asm volatile(
           "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-          "[%5];\n" ::"r"(stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * 4 * sizeof(float2))),
+          "[%5];\n" ::"r"(stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * C * sizeof(float2))),
           "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(c0), "r"(c1), "r"(c2), "r"(fb)
           : "memory");
     }
@@ -1827,7 +1853,12 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
   }
   __syncthreads();
   const unsigned long long wait_ns = g_pass_wait_ns;
-  auto tw = [&](int kb) { return twt[kb * 32 + j]; };
+  auto tw = [&](int kb) {
+    if constexpr (Cfg::TW_REG)
+      return cmul(__ldg(a.tw + j * (kb & 7)), twb[kb >> 3]);
+    else
+      return twt[kb * L + j];
+  };
   for (int t = g; t < n_t; t += G) {
     const int st = t % S, use = t / S;
     float2* stg = reinterpret_cast<float2*>(sbase + (size_t)st * Cfg::TILE);
@@ -1843,42 +1874,42 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
     }
     if (gt == 0) n_consumed[st] = use + 1;
     const int item = item_of(t);
-    const int r = item / NCT, x0 = (item - r * NCT) * 4;
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
     float2 v[R];
 #pragma unroll
-    for (int m = 0; m < R; ++m) v[m] = stg[(32 * m + 8 * w + a4) * 4 + c];
+    for (int m = 0; m < R; ++m) v[m] = stg[(L * m + j) * C + c];
     group_sync(bar, 128);  // the exchanges below overwrite the tile
     float2* xc = stg + c * N;  // column c's exchange rows
-    auto put = [&](int kb, float2 y) { xc[wfft_slot(kb, j, (kb & 3) | (c << 2))] = y; };
+    auto put = [&](int kb, float2 y) { xc[wfft_slot_l<L>(kb, j, wfft_col_swizzle<C>(kb, c))] = y; };
     auto get = [&](int h, int jj) {
-      const int kb = j + 32 * h;
-      return xc[wfft_slot(kb, jj, (kb & 3) | (c << 2))];
+      const int kb = j + L * h;
+      return xc[wfft_slot_l<L>(kb, jj, wfft_col_swizzle<C>(kb, c))];
     };
     if (!a.inv_only) {
       wfft_stage1<R, -1>(v, tw, put);
       group_sync(bar, 128);
-      wfft_stage2<R, -1>(v, get);
+      wfft_stage2<R, -1, L>(v, get);
       group_sync(bar, 128);  // every lane has read its rows before the inverse stores
       // the transfer function H = hy[ky] hx[kx], applied as the inverse gathers its inputs
       const float2 hx = a.hx[x0 + c];
-      wfft_stage1<R, 1>(v, tw, put, [&](int q, float2 y) { return cmul(y, cmul(hys[j + 32 * q], hx)); });
+      wfft_stage1<R, 1>(v, tw, put, [&](int q, float2 y) { return cmul(y, cmul(hys[j + L * q], hx)); });
     } else {
       wfft_stage1<R, 1>(v, tw, put);
     }
     group_sync(bar, 128);
-    wfft_stage2<R, 1>(v, get);
+    wfft_stage2<R, 1, L>(v, get);
     if constexpr (TSTORE) {
       // the result back into the stage, stored by tensor stores; once they have read it,
       // tile t + 3 goes into it
       group_sync(bar, 128);
 #pragma unroll
-      for (int q = 0; q < R; ++q) stg[(32 * q + 8 * w + a4) * 4 + c] = v[q];
+      for (int q = 0; q < R; ++q) stg[(L * q + j) * C + c] = v[q];
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       group_sync(bar, 128);
       if (gt == 0) {
 #pragma unroll 1
         for (int b = 0; b < Cfg::BOXES; ++b)
-          tma_store_col(&tiles, stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * 4 * sizeof(float2)),
+          tma_store_col(&tiles, stage_addr(st) + (uint32_t)(b * Cfg::BOX_ROWS * C * sizeof(float2)),
                         TILED ? 0 : 2 * x0, TILED ? x0 / 4 : b * Cfg::BOX_ROWS,
                         TILED ? r * (N / 4) + b * (Cfg::BOX_ROWS / 4) : r);
         asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
@@ -1894,7 +1925,7 @@ col_pass_wfft_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n
       if (gt == 0 && t + S < n_t) load(t + S);
       float2* f = a.field + (size_t)r * N * N + x0 + c;
 #pragma unroll
-      for (int q = 0; q < R; ++q) f[(size_t)(32 * q + 8 * w + a4) * N] = v[q];
+      for (int q = 0; q < R; ++q) f[(size_t)(L * q + j) * N] = v[q];
     }
   }
   if (TSTORE && gt == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");  // the group's stores are done
@@ -1911,14 +1942,14 @@ static cudaError_t col_wfft_launch(int B, const ColArgs& a, cudaStream_t st) {
   using Cfg = ColWarp<N, TILED>;
   alignas(128) CUtensorMap map;
   const bool mapped = TILED ? encode_tiled_cols_plain(&map, a.field, N, B, Cfg::BOX_ROWS / 4)
-                            : encode_field_tiles(&map, a.field, N, B, 4, Cfg::BOX_ROWS);
+                            : encode_field_tiles(&map, a.field, N, B, Cfg::C, Cfg::BOX_ROWS);
   if (!mapped) return cudaErrorNotSupported;
   static LaunchCache cache;
   const int threads = Cfg::G * 128;
   int grid_max = 0;
   cudaError_t e = cache.get(col_pass_wfft_kernel<N, TSTORE, TILED>, threads, Cfg::SMEM, &grid_max);
   if (e != cudaSuccess) return e;
-  const int n_items = B * (N / 4);
+  const int n_items = B * (N / Cfg::C);
   const int grid = std::max(1, std::min(n_items / 2, grid_max));
   col_pass_wfft_kernel<N, TSTORE, TILED><<<grid, threads, Cfg::SMEM, st>>>(map, a, n_items);
   return cudaGetLastError();
@@ -2034,6 +2065,7 @@ cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t 
     if (!aligned16(a.field)) return cudaErrorInvalidValue;
     if (N == 1024) return col_wfft_launch<1024, 1>(B, a, st);
     if (N == 2048) return col_wfft_launch<2048, 1>(B, a, st);
+    if (N == 4096) return col_wfft_launch<4096, 1>(B, a, st);  // 64-lane transforms, tiles of 2 columns
     return cudaErrorInvalidValue;
   }
   if (C <= 0) C = col_tile_default(N);

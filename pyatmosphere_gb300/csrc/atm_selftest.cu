@@ -76,42 +76,52 @@ int host_fft(int dir, const float* in, float* out) {
 // each side of the exchange.  mode 0: the exchange swizzle of a warp that
 // holds all 32 lanes (row pass); mode 1 + c: that of column c of a
 // four-column group (column pass)
-template <int R>
+// NL = 64 lanes (N = 4096): mode 1 + c is the swizzle of column c of a
+// two-column group, and the twiddles are formed as the column pass forms
+// them, W^(j (kb & 7)) W^(8 j (kb >> 3))
+template <int R, int NL = 32>
 int host_wfft(int dir, int mode, const float* in, float* out) {
-  constexpr int N = 32 * R;
-  std::vector<float2> tw(N), twt(R * 32), xbuf(N);
+  constexpr int N = NL * R;
+  std::vector<float2> tw(N), twt(R * NL), xbuf(N);
   for (int i = 0; i < N; ++i) {
     const double a = -2.0 * 3.14159265358979323846 * i / N;
     tw[i] = make_float2((float)cos(a), (float)sin(a));
   }
-  for (int i = 0; i < R * 32; ++i) twt[i] = tw[(i >> 5) * (i & 31)];
-  auto sw = [&](int kb) { return mode == 0 ? (kb & 15) : ((kb & 3) | ((mode - 1) << 2)); };
+  for (int i = 0; i < R * NL; ++i) twt[i] = tw[(i / NL) * (i % NL)];
+  auto sw = [&](int kb) {
+    if (NL == 64) return (kb & 7) | ((mode - 1) << 3);
+    return mode == 0 ? (kb & 15) : ((kb & 3) | ((mode - 1) << 2));
+  };
+  auto twiddle = [&](int kb, int j) {
+    if (NL == 64) return atm::cmul(tw[j * (kb & 7)], tw[(8 * j * (kb >> 3)) % N]);
+    return twt[kb * NL + j];
+  };
   struct Lane {
     float2 v[R];
   };
-  std::vector<Lane> L(32);
-  for (int j = 0; j < 32; ++j)
-    for (int m = 0; m < R; ++m) L[j].v[m] = make_float2(in[2 * (j + 32 * m)], in[2 * (j + 32 * m) + 1]);
+  std::vector<Lane> L(NL);
+  for (int j = 0; j < NL; ++j)
+    for (int m = 0; m < R; ++m) L[j].v[m] = make_float2(in[2 * (j + NL * m)], in[2 * (j + NL * m) + 1]);
   auto run = [&](auto dirc) {
     constexpr int D = decltype(dirc)::value;
-    for (int j = 0; j < 32; ++j)
+    for (int j = 0; j < NL; ++j)
       atm::wfft_stage1<R, D>(
-          L[j].v, [&](int kb) { return twt[kb * 32 + j]; },
-          [&](int kb, float2 y) { xbuf[atm::wfft_slot(kb, j, sw(kb))] = y; });
-    for (int j = 0; j < 32; ++j)
-      atm::wfft_stage2<R, D>(L[j].v, [&](int h, int jj) {
-        const int kb = j + 32 * h;
-        return xbuf[atm::wfft_slot(kb, jj, sw(kb))];
+          L[j].v, [&](int kb) { return twiddle(kb, j); },
+          [&](int kb, float2 y) { xbuf[atm::wfft_slot_l<NL>(kb, j, sw(kb))] = y; });
+    for (int j = 0; j < NL; ++j)
+      atm::wfft_stage2<R, D, NL>(L[j].v, [&](int h, int jj) {
+        const int kb = j + NL * h;
+        return xbuf[atm::wfft_slot_l<NL>(kb, jj, sw(kb))];
       });
   };
   if (dir < 0)
     run(std::integral_constant<int, -1>{});
   else
     run(std::integral_constant<int, 1>{});
-  for (int j = 0; j < 32; ++j)
+  for (int j = 0; j < NL; ++j)
     for (int q = 0; q < R; ++q) {
-      out[2 * (j + 32 * q)] = L[j].v[q].x;
-      out[2 * (j + 32 * q) + 1] = L[j].v[q].y;
+      out[2 * (j + NL * q)] = L[j].v[q].x;
+      out[2 * (j + NL * q) + 1] = L[j].v[q].y;
     }
   return 0;
 }
@@ -120,13 +130,15 @@ int host_wfft(int dir, int mode, const float* in, float* out) {
 
 extern "C" {
 
-// length-N warp FFT (N = 1024 or 2048; dir = -1 forward, +1 unnormalised
-// inverse) of interleaved complex data, exchange swizzle `mode` (see host_wfft)
+// length-N warp FFT (N = 1024 or 2048: 32 lanes; 4096: 64 lanes, modes 1 and
+// 2 only; dir = -1 forward, +1 unnormalised inverse) of interleaved complex
+// data, exchange swizzle `mode` (see host_wfft)
 int atm_selftest_wfft(int N, int dir, int mode, const float* in, float* out) {
   if (mode < 0 || mode > 4) return -1;
   switch (N) {
     case 1024: return host_wfft<32>(dir, mode, in, out);
     case 2048: return host_wfft<64>(dir, mode, in, out);
+    case 4096: return (mode == 1 || mode == 2) ? host_wfft<64, 64>(dir, mode, in, out) : -1;
   }
   return -1;
 }

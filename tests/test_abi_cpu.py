@@ -72,11 +72,11 @@ def test_kernel_fft_arithmetic_on_host(built, N):
         np.testing.assert_array_equal(out3, out2)
 
 
-@pytest.mark.parametrize("N", [1024, 2048])
+@pytest.mark.parametrize("N", [1024, 2048, 4096])
 def test_warp_fft_arithmetic_on_host(built, N):
     """The warp FFT of the row / column pass forms 11 / 10 (one exchange per
-    transform, lanes emulated on the host) against numpy in FP64; every
-    exchange swizzle gives the same bits."""
+    transform, lanes emulated on the host; 64 lanes at 4096) against numpy in
+    FP64; every exchange swizzle gives the same bits."""
     from pyatmosphere_gb300.engine._lib import load_selftest
     lib = load_selftest(built["selftest"])
     rng = np.random.default_rng(N + 1)
@@ -84,7 +84,7 @@ def test_warp_fft_arithmetic_on_host(built, N):
     for d in (-1, 1):
         ref = np.fft.fft(x.astype(np.complex128)) if d < 0 else np.fft.ifft(x.astype(np.complex128)) * N
         outs = []
-        for mode in range(5):
+        for mode in ((1, 2) if N == 4096 else range(5)):
             out = np.zeros(N, np.complex64)
             assert lib.atm_selftest_wfft(N, d, mode, x.ctypes.data, out.ctypes.data) == 0
             outs.append(out)
@@ -138,6 +138,31 @@ def test_warp_fft_exchange_is_bank_conflict_free(R):
         for m in range(R):
             slots = [(32 * m + 8 * w + lane // 4) * 4 + lane % 4 for lane in range(32)]
             assert slots == list(range(slots[0], slots[0] + 32))
+
+
+def test_warp_fft_4096_exchange_is_bank_conflict_free():
+    """N = 4096 (64-lane transforms, R = 64): lane (a = lane // 2, c = lane % 2)
+    of warp w is lane j = 16 w + a of column c of a two-column tile; its
+    exchange (swizzle (kb & 7) | (c << 3)) and the tile read are free of bank
+    conflicts per half warp, and the slots of a column are a permutation."""
+    L, R, N = 64, 64, 4096
+    half_warps = [range(0, 16), range(16, 32)]
+
+    def slot(kb, jj, c):
+        return c * N + kb * L + (jj ^ ((kb & 7) | (c << 3)))
+
+    for w in range(4):
+        for kb in range(R):
+            for hw in half_warps:
+                assert len({slot(kb, 16 * w + lane // 2, lane % 2) % 16 for lane in hw}) == 16
+        for jj in range(L):
+            for hw in half_warps:
+                assert len({slot(16 * w + lane // 2, jj, lane % 2) % 16 for lane in hw}) == 16
+        for m in range(R):
+            slots = [(L * m + 16 * w + lane // 2) * 2 + lane % 2 for lane in range(32)]
+            assert slots == list(range(slots[0], slots[0] + 32))
+    for c in range(2):
+        assert sorted(slot(kb, jj, c) - c * N for kb in range(R) for jj in range(L)) == list(range(N))
 
 
 def test_bessel_coefficients_on_host(built):

@@ -358,17 +358,16 @@ def test_product_twiddle_column_pass_matches_oracle(torch_cuda):
     assert o.rel_l2(field.cpu().numpy()[0], u) < FIELD_TOL
 
 
-@pytest.mark.parametrize("N", [1024, 2048])
-def test_warp_fft_passes_match_oracle(torch_cuda, N):
-    """The warp-FFT forms (row variant 11, column variant 10) keep the FP64
-    parity bound on fields and measures, at both grid sizes they serve, for a
-    batch of 3 (the column pass's two groups on neighbouring tiles of several
-    realisations), and through atm_vacuum on the same plan."""
+@pytest.mark.parametrize("N,variants,R", [(1024, (11, 4, 10), 3), (2048, (11, 4, 10), 3), (4096, (4, 4, 10), 2)])
+def test_warp_fft_passes_match_oracle(torch_cuda, N, variants, R):
+    """The warp-FFT forms (row variant 11 at 1024 and 2048; column variant 10,
+    with 64-lane transforms at 4096) keep the FP64 parity bound on fields and
+    measures, for batches of several realisations (the column pass's two
+    groups on neighbouring tiles), and through atm_vacuum on the same plan."""
     torch = torch_cuda
     spec = o.ChannelSpec(N=N, delta=3.0 / N, w0=0.1, length=20e3, count=4, Cn2=1e-15, pupil_radius=0.15)
-    R = 3
     plan, base = make_plan(spec, batch=R)
-    plan.set_variants(11, 4, 10)
+    plan.set_variants(*variants)
     rho, theta, value = spectra(spec, base, seed=77, R=R)
     field = torch.empty((R, N, N), dtype=torch.complex64, device="cuda")
     got = plan.run(*to_dev(torch, rho, theta, value), field_out=field).cpu().numpy()
