@@ -942,13 +942,19 @@ static cudaError_t row_plain_launch(int B, const RowArgs& a, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------
 // row pass with warp FFTs (N = 1024, 2048; row-major field): one warp per
-// row, W warps per CTA, rows strided over a persistent grid.  Lane 0 moves
-// the warp's next row into the warp's staging buffer with one bulk copy as
-// soon as the current row has left it, so a row is always in flight; the
-// screen phases of the row are loaded into registers when the row starts and
-// arrive while the inverse transform runs.  Lane j holds elements j + 32 m
-// (the warp FFT's layout, atm_common.cuh); each transform exchanges once
-// through the warp's own exchange buffer, with no barrier beyond __syncwarp.
+// row, W warps per CTA, rows strided over a persistent grid; lane j holds
+// elements j + 32 m (the warp FFT's layout, atm_common.cuh) and each
+// transform exchanges once through shared memory with no barrier beyond
+// __syncwarp.  Rows arrive by one bulk copy each into the warp's slot:
+// - N = 1024 (two 8 KB buffers per warp): the next row is copied into the
+//   staging buffer as soon as the current one has left it, and the exchanges
+//   use the second buffer; the row's screen phases are loaded into registers
+//   when the row starts;
+// - N = 2048 (one 16 KB slot per warp, eight warps of 255 registers): the slot
+//   stages the row, then serves both exchanges, and takes the next row once
+//   the last exchange has been read, while the results are stored; the screen
+//   phases come in two halves, the even elements' before the inverse
+//   transform and the odd elements' after its first stage.
 // Passes with measures (ROW_MEAS, ROW_STEP) or the unfolded screen phasor go
 // to the one-row product-twiddle form instead (row_launch).  The staging
 // wait is bounded (error word, then a drain of the copy in flight).
@@ -956,10 +962,11 @@ static cudaError_t row_plain_launch(int B, const RowArgs& a, cudaStream_t st) {
 template <int N>
 struct RowWarp {
   static constexpr int R = N / 32;
-  static constexpr int W = N == 2048 ? 6 : 12;                   // warps per CTA, one CTA per SM
+  static constexpr int SLOTS = N == 2048 ? 1 : 2;                 // row buffers per warp
+  static constexpr int W = N == 2048 ? 8 : 12;                   // warps per CTA, one CTA per SM (255 registers at 8)
   static constexpr size_t ROW = (size_t)N * sizeof(float2);       // a staged row / an exchange buffer
   static constexpr size_t TWT = (size_t)R * 32 * sizeof(float2);  // W_N^(j kb) per lane j
-  static constexpr size_t SMEM = 128 + (size_t)W * 2 * ROW + TWT;
+  static constexpr size_t SMEM = 128 + (size_t)W * SLOTS * ROW + TWT;
 };
 
 template <int N>
@@ -970,9 +977,10 @@ __global__ void __launch_bounds__(RowWarp<N>::W * 32, 1) row_pass_wfft_kernel(Ro
   __shared__ __align__(8) uint64_t full_bar[Cfg::W];
   unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
   const int warp = threadIdx.x >> 5, j = threadIdx.x & 31;
-  float2* stage = reinterpret_cast<float2*>(sbase + (size_t)warp * 2 * Cfg::ROW);
-  float2* xw = stage + N;
-  float2* twt = reinterpret_cast<float2*>(sbase + (size_t)Cfg::W * 2 * Cfg::ROW);
+  constexpr bool SLOT1 = Cfg::SLOTS == 1;
+  float2* stage = reinterpret_cast<float2*>(sbase + (size_t)warp * Cfg::SLOTS * Cfg::ROW);
+  float2* xw = SLOT1 ? stage : stage + N;
+  float2* twt = reinterpret_cast<float2*>(sbase + (size_t)Cfg::W * Cfg::SLOTS * Cfg::ROW);
   // twt[kb][jj] = exp(-2 pi i jj kb / N) = tw[jj kb]  (jj kb < N)
   for (int i = threadIdx.x; i < R * 32; i += blockDim.x) twt[i] = a.tw[(i >> 5) * (i & 31)];
   const uint32_t fb = (uint32_t)__cvta_generic_to_shared(&full_bar[warp]);
@@ -1023,24 +1031,31 @@ __global__ void __launch_bounds__(RowWarp<N>::W * 32, 1) row_pass_wfft_kernel(Ro
       }
 #pragma unroll
       for (int m = 0; m < R; ++m) v[m] = stage[j + 32 * m];
-      // the next row's copy (the async proxy) may overwrite the stage once every lane has read it
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      __syncwarp();
-      if (j == 0 && row + stride < n_rows) {
-        fetch(row + stride);
-        pending = true;
+      if constexpr (!SLOT1) {
+        // the next row's copy (the async proxy) may overwrite the stage once every lane has read it
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncwarp();
+        if (j == 0 && row + stride < n_rows) {
+          fetch(row + stride);
+          pending = true;
+        }
+      } else {
+        __syncwarp();  // every lane has read the row before the exchange overwrites the slot
       }
     } else {
       const float2 gy = a.ay[y];
 #pragma unroll
       for (int m = 0; m < R; ++m) v[m] = cmul(gy, a.ax[j + 32 * m]);
     }
-    // the screen phases (folded: one phasor per pixel), in flight during the inverse transform
+    // the screen phases (folded: one phasor per pixel), in flight during the inverse transform;
+    // with one slot per warp the odd elements' phases are loaded after the inverse's first stage
     float ph[R];
+    const float* php = a.phi + rowoff;
+    const bool split_ph = SLOT1 && (flags & ROW_INV);
     if (flags & ROW_PHASOR) {
-      const float* p = a.phi + rowoff;
 #pragma unroll
-      for (int m = 0; m < R; ++m) ph[m] = p[j + 32 * m];
+      for (int m = 0; m < R; ++m)
+        if (!split_ph || (m & 1) == 0) ph[m] = php[j + 32 * m];
     }
     // the screen phasor and the step's loss (a lossless step multiplies by the bare phasor),
     // applied to each element as the inverse transform forms it (or, without an inverse, as
@@ -1056,6 +1071,10 @@ __global__ void __launch_bounds__(RowWarp<N>::W * 32, 1) row_pass_wfft_kernel(Ro
     if (flags & ROW_INV) {
       wfft_stage1<R, 1>(v, tw, put);
       __syncwarp();
+      if (split_ph && (flags & ROW_PHASOR)) {
+#pragma unroll
+        for (int m = 1; m < R; m += 2) ph[m] = php[j + 32 * m];
+      }
       wfft_stage2<R, 1>(v, get, screen);
       __syncwarp();  // every lane has read its rows before the next transform stores
     }
@@ -1070,6 +1089,17 @@ __global__ void __launch_bounds__(RowWarp<N>::W * 32, 1) row_pass_wfft_kernel(Ro
     } else if (!(flags & ROW_INV) && ((flags & ROW_PHASOR) || loss != 1.0f)) {
 #pragma unroll
       for (int m = 0; m < R; ++m) v[m] = screen(m, v[m]);
+    }
+    if constexpr (SLOT1) {
+      // the slot's exchanges have been read: the next row's copy may land while this one is stored
+      if (load_field) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncwarp();
+        if (j == 0 && row + stride < n_rows) {
+          fetch(row + stride);
+          pending = true;
+        }
+      }
     }
     if (flags & ROW_STORE) {
       float2* dst = ((a.store_out && a.out) ? a.out : a.field) + rowoff;
