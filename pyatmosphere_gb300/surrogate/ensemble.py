@@ -19,7 +19,8 @@ from typing import Dict, List, Optional
 import numpy as np
 import torch
 
-from .model import N_HIST, N_MOM, Box, PointSimulator, SimConfig, Surrogate, features, targets_from_measures
+from .model import (N_HIST, N_MOM, Box, SimConfig, Surrogate, fallback_simulator, features, release_fallback,
+                    targets_from_measures)
 
 
 def disagreement(member_probs: torch.Tensor) -> torch.Tensor:
@@ -85,13 +86,16 @@ class EnsembleSurrogate:
         probs = probs.cpu().numpy()
         todo = np.nonzero(~ans)[0]
         if len(todo):
-            sim = PointSimulator(fallback_cfg or SimConfig(N=1024, realisations=256), device=self.device)
+            sim = fallback_simulator(self, fallback_cfg or SimConfig(N=1024, realisations=256), self.device)
             for i in todo:
                 q = {k: v[i] for k, v in params.items()}
                 t, _ = targets_from_measures(sim.run(q, 10_000_000 + int(i)), q["aperture"])
                 probs[i] = t[:N_HIST]
-            sim.plan.close()
         return probs, ans
+
+    def close(self):
+        """Frees the fallback simulator's plan (kept across queries)."""
+        release_fallback(self)
 
     # ---------------------------------------------------------------- files
     def save(self, path: str, **extra):

@@ -161,6 +161,25 @@ class PointSimulator:
         return self.plan.run(self.rho, self.theta, self.value)
 
 
+def fallback_simulator(owner, cfg: SimConfig, device) -> PointSimulator:
+    """The point simulator of `owner` (a surrogate) for this configuration,
+    kept across queries: its plan, workspace and tuned launch forms are built
+    once, not per query batch.  release_fallback(owner) frees them."""
+    sims = owner.__dict__.setdefault("_fallback_sims", {})
+    key = (tuple(sorted(vars(cfg).items())), str(device))
+    if key not in sims:
+        sims[key] = PointSimulator(cfg, device=device)
+    return sims[key]
+
+
+def release_fallback(owner):
+    """Frees the point simulators `owner` keeps (their plans' device memory)."""
+    for sim in owner.__dict__.pop("_fallback_sims", {}).values():
+        if sim.plan is not None:
+            sim.plan.close()
+            sim.plan = None
+
+
 def targets_from_measures(m: torch.Tensor, aperture: float) -> np.ndarray:
     """(64 histogram probabilities, mean eta, log10 beam-wandering variance,
     log10 long-term width) of one point's realisations."""
@@ -278,10 +297,9 @@ class Surrogate:
         oor = oor.cpu().numpy().astype(bool)
         n_fb = int(oor.sum())
         if n_fb:
-            sim = PointSimulator(fallback_cfg or SimConfig(N=1024, realisations=256), device=self.device)
+            sim = fallback_simulator(self, fallback_cfg or SimConfig(N=1024, realisations=256), self.device)
             for i in np.nonzero(oor)[0]:
                 q = {k: v[i] for k, v in params.items()}
                 t, _ = targets_from_measures(sim.run(q, 10_000_000 + int(i)), q["aperture"])
                 probs[i] = t[:N_HIST]
-            sim.plan.close()
         return probs, oor
