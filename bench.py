@@ -159,7 +159,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32 (numpy, reference precision)",
         "data": "synthetic (seeded spectra, reference's own formulas)",
-        "config": {"workload": WORKLOAD_NAME, "realisations_per_step": 1},
+        "config": {"workload": WORKLOAD_NAME, "batch": 1, "realisations_per_step": 1},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores(), "kind": "port",
                          "sample": f"{args.steps} single-realisation steps of the 2048^2 channel, numpy/OpenBLAS "
                                    "restatement of the reference path in its own precision"},
@@ -620,7 +620,7 @@ def run_gb300(args, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 (c64 field; fp64 phase args, accumulators)",
             "data": "synthetic (seeded spectra, reference formulas)",
-            "config": {"workload": "2048^2 advanced channel, 50 km, 5 SS screens x 1024", "batch": B,
+            "config": {"workload": WORKLOAD_NAME, "batch": B,
                        "realisations_per_step": B, "timed_as": "cuda graph replay" if graphs else "direct launches",
                        "direct_ms_per_step": round(direct_ms, 3), "kernels_timed": kernels_timed,
                        "l2": "inputs > L2 (8.6 GB field batch)", "gemm_k": K,
