@@ -137,6 +137,72 @@ def cpu_realisations(n_real: int, seed: int = 4242):
     return n_real / (time.perf_counter() - t)
 
 
+REF_INSTALL = os.path.join(ROOT, "baseline", "_ref")
+
+
+def import_stock_reference():
+    """The unmodified reference package as installed under baseline/_ref (pip
+    --target), or None.  Its plotting and pandas imports are served by empty
+    stand-in modules for the import only; the reference keeps its own
+    bindings.  Its numpy path is selected (gpu.py:4-20)."""
+    import importlib
+    import types
+    if not os.path.isdir(os.path.join(REF_INSTALL, "pyatmosphere")):
+        return None
+    added = []
+    for name in ("matplotlib", "matplotlib.pyplot", "pandas"):
+        if name not in sys.modules:
+            sys.modules[name] = types.ModuleType(name)
+            added.append(name)
+    if "matplotlib.pyplot" in added:
+        sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+    if REF_INSTALL not in sys.path:
+        sys.path.append(REF_INSTALL)
+    try:
+        ref = importlib.import_module("pyatmosphere")
+        for sub in ("channels", "grids", "sources", "pathes", "phase_screens", "pupils", "measures",
+                    "theory.models", "simulations", "simulations.simulation", "simulations.pdt",
+                    "simulations.beam", "utils"):
+            importlib.import_module("pyatmosphere." + sub)
+    finally:
+        for name in added:
+            sys.modules.pop(name, None)
+    ref.gpu.config["use_gpu"] = False
+    return ref
+
+
+class StockRealisation:
+    """One realisation of the workload through the unmodified reference:
+    Channel.run (channels.py:31-35; its SSPhaseScreen draws the spectra from
+    numpy's global generator, phase_screens.py:93-136) and the measures the
+    engine fuses (measures.py:7-38): total and pupil eta, centroid and second
+    moments."""
+
+    def __init__(self, ref):
+        import importlib
+        mod = {n: importlib.import_module("pyatmosphere." + n)
+               for n in ("channels", "grids", "pathes", "phase_screens", "pupils", "sources", "theory.models",
+                         "measures")}
+        w = WORKLOAD
+        self.m = mod["measures"]
+        self.channel = mod["channels"].Channel(
+            grid=mod["grids"].RectGrid(resolution=w["N"], delta=w["delta"]),
+            source=mod["sources"].GaussianSource(wvl=w["wvl"], w0=w["w0"], F0=w["F0"]),
+            path=mod["pathes"].IdenticalPhaseScreensPath(
+                phase_screen=mod["phase_screens"].SSPhaseScreen(
+                    model=mod["theory.models"].MVKModel(Cn2=w["Cn2"], l0=w["l0"], L0=w["L0"]),
+                    f_grid=mod["grids"].RandLogPolarGrid(points=w["points"], f_min=w["f_min"], f_max=w["f_max"])),
+                length=w["length"], count=w["count"]),
+            pupil=mod["pupils"].CirclePupil(radius=w["pupil_radius"]))
+
+    def __call__(self, seed: int):
+        np.random.seed(seed)
+        ch, m = self.channel, self.m
+        u = ch.run(pupil=False)
+        return [m.eta(ch, output=u), m.eta(ch, output=ch.pupil.output(u))] + \
+            [f(ch, output=u) for f in (m.mean_x, m.mean_y, m.mean_x2, m.mean_xy, m.mean_y2)]
+
+
 def cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -145,13 +211,28 @@ def cores():
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the unmodified reference package (baseline/_ref) on
+    its numpy path when it is installed, else the oracle's restatement of it
+    in the reference's precision; one realisation per step."""
     if rank != 0:
         return 0
-    for _ in range(args.warmup):
-        cpu_realisations(1, seed=1)
+    ref = None if args.ref_port else import_stock_reference()
+    if ref is not None:
+        step = StockRealisation(ref)
+        kind = "reference"
+        sample = (f"{args.steps} single-realisation steps of the 2048^2 channel through the unmodified reference "
+                  "(Channel.run and measures on its numpy path, spectra drawn inside the step)")
+    else:
+        def step(seed):
+            return cpu_realisations(1, seed=seed)
+        kind = "port"
+        sample = (f"{args.steps} single-realisation steps of the 2048^2 channel, numpy/OpenBLAS restatement of "
+                  "the reference path in its own precision")
+    for w in range(args.warmup):
+        step(1 + w)
     t = time.perf_counter()
     for k in range(args.steps):
-        cpu_realisations(1, seed=100 + k)
+        step(100 + k)
     el = time.perf_counter() - t
     val = args.steps / el
     line = {
@@ -160,9 +241,7 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32 (numpy, reference precision)",
         "data": "synthetic (seeded spectra, reference's own formulas)",
         "config": {"workload": WORKLOAD_NAME, "batch": 1, "realisations_per_step": 1},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores(), "kind": "port",
-                         "sample": f"{args.steps} single-realisation steps of the 2048^2 channel, numpy/OpenBLAS "
-                                   "restatement of the reference path in its own precision"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores(), "kind": kind, "sample": sample},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -604,10 +683,22 @@ def run_gb300(args, rank, world, local_rank):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         n_cpu = args.cpu_realisations
-        v = cpu_realisations(n_cpu)
-        cpu = {"value": v, "unit": UNIT, "cores": cores(), "kind": "port",
-               "sample": f"{n_cpu} realisations of the same 2048^2 channel through the numpy restatement of "
-                         "the reference path in its own precision (OpenBLAS threads = cores; numpy FFT single-threaded)"}
+        ref = None if args.ref_port else import_stock_reference()
+        if ref is not None:
+            stock = StockRealisation(ref)
+            t0 = time.perf_counter()
+            for k in range(n_cpu):
+                stock(4242 + k)
+            v = n_cpu / (time.perf_counter() - t0)
+            cpu = {"value": v, "unit": UNIT, "cores": cores(), "kind": "reference",
+                   "sample": f"{n_cpu} realisations of the same 2048^2 channel through the unmodified reference on "
+                             "its numpy path (OpenBLAS threads = cores; numpy FFT single-threaded)"}
+        else:
+            v = cpu_realisations(n_cpu)
+            cpu = {"value": v, "unit": UNIT, "cores": cores(), "kind": "port",
+                   "sample": f"{n_cpu} realisations of the same 2048^2 channel through the numpy restatement of "
+                             "the reference path in its own precision (OpenBLAS threads = cores; numpy FFT "
+                             "single-threaded)"}
 
     if rank == 0:
         def r3(v):
@@ -663,6 +754,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--ref-port", action="store_true",
+                    help="reference arm: time the oracle's restatement even where the stock reference is installed")
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--plain", type=int, default=16, help="realisations timed in the plain form (0: skip)")
     ap.add_argument("--seed", type=int, default=2024)
