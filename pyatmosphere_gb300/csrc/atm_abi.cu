@@ -1150,14 +1150,18 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
       }
     }
   }
-  if (!pl->tiled && col_warp) {
-    // the warp-FFT column groups choose their own tile (4 columns, 2 at 4096); recorded as column tile 4
-    ca.variant = 10;
+  // the warp-FFT column groups choose their own tile (4 columns, 2 at 4096; 14: 4096-row tiles of 4
+  // columns as two 2048-point halves); recorded as column tile 4
+  std::vector<int> warp_cols;
+  if (!pl->tiled && col_warp) warp_cols.push_back(10);
+  if (!pl->tiled && N == 4096) warp_cols.push_back(14);
+  for (int v : warp_cols) {
+    ca.variant = v;
     const double ms = time_it([&] { return atm::launch_col_pass(N, batch, 4, ca, st); });
     if (ms >= 0 && (best_col < 0 || ms < best_col)) {
       best_col = ms;
       col_tile = 4;
-      col_variant = 10;
+      col_variant = v;
     }
   }
   cudaEventDestroy(e0);
@@ -1195,14 +1199,17 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
   const bool col_warp = warp_fft || pl->N == 4096;         // column 10: warp FFTs
   if (row_variant < 0 || (row_variant > 4 && row_variant != 7 && !(row_variant == 11 && warp_fft)))
     return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4, 7%s", row_variant, warp_fft ? " or 11" : "");
-  if (col_variant < 0 || (col_variant > 4 && col_variant != 7 && !(col_variant == 10 && col_warp)))
-    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4, 7%s", col_variant, col_warp ? " or 10" : "");
-  if (col_variant == 10 && col_tile != 4)
-    return fail(ATM_ERR_INVALID, "col_variant 10 takes col_tile 4");
+  const bool split = pl->N == 4096;                        // column 14: two 2048-point halves per column
+  if (col_variant < 0 ||
+      (col_variant > 4 && col_variant != 7 && !(col_variant == 10 && col_warp) && !(col_variant == 14 && split)))
+    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4, 7%s", col_variant,
+                split ? ", 10 or 14" : (col_warp ? " or 10" : ""));
+  if ((col_variant == 10 || col_variant == 14) && col_tile != 4)
+    return fail(ATM_ERR_INVALID, "col_variant %d takes col_tile 4", col_variant);
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
     return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);
   // (the warp-FFT column groups are 256 threads whatever the recorded tile)
-  if (col_variant != 10 && (col_tile * (pl->N / 16) > 512 || col_tile > pl->N))
+  if (col_variant != 10 && col_variant != 14 && (col_tile * (pl->N / 16) > 512 || col_tile > pl->N))
     return fail(ATM_ERR_UNSUPPORTED, "col_tile %d exceeds 512 threads per CTA at N = %d", col_tile, pl->N);
   pl->row_variant = row_variant;
   pl->col_tile = col_tile;

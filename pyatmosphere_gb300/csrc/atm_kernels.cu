@@ -1985,6 +1985,198 @@ static cudaError_t col_wfft_launch(int B, const ColArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// column pass at N = 4096 from two 2048-point warp FFTs per column (a radix-2
+// split in y), so that the tiles keep 4 columns (32-byte rows) and the
+// transforms keep the 2048-point groups' 64 elements per lane.  A tile of 4
+// columns x 4096 rows arrives as two 64 KB units, its top and bottom 2048
+// rows, in a ring of three unit stages, and both groups of four warps work on
+// the same tile:
+//   in:  group 0 forms a[n] + b[n], group 1 (a[n] - b[n]) W_N^n (n < 2048; a
+//        the top rows, b the bottom rows); the 2048-point transforms of these
+//        are the even and the odd frequencies of the 4096-point transform;
+//   each group transforms its half (forward; H = hy[K] hx applied as the
+//        inverse gathers its inputs, K = 2 k + g; inverse), exchanging
+//        through its own unit (group 0 the top one, group 1 the bottom one);
+//   out: group 1 scales its inverse by W_N^-n, both write their halves back
+//        into their units, and the top rows are E[n] + O[n], the bottom rows
+//        E[n] - O[n]; they are stored from registers (8 rows x 4 columns per
+//        store instruction) once both units have been read, while the CTA's
+//        next units load into them.
+// hy is symmetric in the unshifted order (hy[K] = hy[N - K], the frequencies
+// of K and N - K have the same square): the CTA stages hy[0..N/2] (16 KB), so
+// that three units, the W_2048 table and hy fit in one CTA's shared memory.
+// Tile t takes units 2t and 2t + 1 (stages (2t) % 3 and (2t + 1) % 3); once
+// tile t has been read the CTA loads units 2t + 3 and 2t + 4 into the same
+// stages, so the next tile's first unit is in flight during a tile's
+// transforms.  Every wait is bounded (error word, then a drain of the copies
+// in flight).
+// ---------------------------------------------------------------------------
+struct ColSplit {
+  static constexpr int N = 4096;
+  static constexpr int H = N / 2;                                 // rows of a unit, length of the halves' FFTs
+  static constexpr int L = 32, C = 4, RW = 8, R = H / L;          // the 2048-point column groups' lanes
+  static constexpr int S = 3;                                     // unit stages
+  static constexpr size_t UNIT = (size_t)H * C * sizeof(float2);  // 64 KB
+  static constexpr size_t TWT = (size_t)R * L * sizeof(float2);   // W_H^(j kb) per lane j
+  static constexpr size_t HY = (((size_t)H + 1) * sizeof(float2) + 127) / 128 * 128;  // hy[0..H]
+  static constexpr size_t SMEM = 128 + S * UNIT + TWT + HY;
+  static constexpr int BOX_ROWS = 256, BOXES = H / BOX_ROWS;
+  static_assert(SMEM <= 227 * 1024, "stages exceed shared memory");
+};
+
+__global__ void __launch_bounds__(256, 1)
+col_pass_wsplit_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_tiles) {
+  using Cfg = ColSplit;
+  constexpr int N = Cfg::N, H = Cfg::H, R = Cfg::R, L = Cfg::L, C = Cfg::C, S = Cfg::S;
+  constexpr int NCT = N / C;  // tiles per realisation
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[S];
+  __shared__ int n_issued[S], n_consumed[S];  // loads issued / waited for, per stage
+  const int tid = threadIdx.x;
+  const int g = tid >> 7, gt = tid & 127;
+  const int w = gt >> 5, lane = tid & 31;
+  const int a4 = lane / C, c = lane % C;
+  const int j = Cfg::RW * w + a4;  // lane of column c's transforms
+  const int bar = 1 + g;
+  unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
+  float2* twt = reinterpret_cast<float2*>(sbase + (size_t)S * Cfg::UNIT);
+  float2* hys = twt + Cfg::TWT / sizeof(float2);
+  for (int i = tid; i < R * L; i += blockDim.x) twt[i] = a.tw[2 * (i / L) * (i % L)];  // W_H^k = W_N^2k; < N
+  for (int i = tid; i <= H; i += blockDim.x) hys[i] = a.hy[i];
+  const int n_t = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int n_units = 2 * n_t;
+  auto item_of = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
+  auto unit_ptr = [&](int st) { return reinterpret_cast<float2*>(sbase + (size_t)st * Cfg::UNIT); };
+  auto fbar = [&](int st) { return (uint32_t)__cvta_generic_to_shared(&full_bar[st]); };
+  auto load = [&](int u) {  // unit u (tile u / 2, half u % 2) into stage u % 3, by one thread
+    const int st = u % S;
+    const int item = item_of(u >> 1);
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
+    const uint32_t fb = fbar(st);
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(unit_ptr(st));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::UNIT)
+                 : "memory");
+#pragma unroll 1
+    for (int b = 0; b < Cfg::BOXES; ++b)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+          "[%5];\n" ::"r"(dst + (uint32_t)(b * Cfg::BOX_ROWS * C * sizeof(float2))),
+          "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(2 * x0), "r"((u & 1) * H + b * Cfg::BOX_ROWS), "r"(r),
+          "r"(fb)
+          : "memory");
+    n_issued[st] += 1;
+  };
+  if (tid == 0) {
+    for (int st = 0; st < S; ++st) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fbar(st)) : "memory");
+      n_issued[st] = 0;
+      n_consumed[st] = 0;
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    for (int u = 0; u < S && u < n_units; ++u) load(u);
+  }
+  __syncthreads();
+  const unsigned long long wait_ns = g_pass_wait_ns;
+  auto tw = [&](int kb) { return twt[kb * L + j]; };
+  for (int t = 0; t < n_t; ++t) {
+    const int u0 = 2 * t, u1 = u0 + 1;
+    const int s0 = u0 % S, s1 = u1 % S;
+    // a unit's load is issued (after the previous use of its stage was read) before the CTA barrier
+    // that ends the previous tile, so each wait is on the phase of the stage's current use
+    const bool ok = pass_mbar_wait(fbar(s0), (uint32_t)((u0 / S) & 1), wait_ns) &&
+                    pass_mbar_wait(fbar(s1), (uint32_t)((u1 / S) & 1), wait_ns);
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) {
+        atomicExch(&g_pass_error, 1);
+        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      }
+      break;
+    }
+    if (tid == 0) {
+      n_consumed[s0] = u0 / S + 1;
+      n_consumed[s1] = u1 / S + 1;
+    }
+    const int item = item_of(t);
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
+    float2* top = unit_ptr(s0);
+    float2* bot = unit_ptr(s1);
+    float2 v[R];
+    if (g == 0) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) v[m] = cadd(top[(L * m + j) * C + c], bot[(L * m + j) * C + c]);
+    } else {
+#pragma unroll
+      for (int m = 0; m < R; ++m)
+        v[m] = cmul(csub(top[(L * m + j) * C + c], bot[(L * m + j) * C + c]), __ldg(a.tw + L * m + j));
+    }
+    __syncthreads();  // both units read: the groups' exchanges overwrite them
+    float2* own = g == 0 ? top : bot;
+    float2* xc = own + c * H;  // column c's exchange rows in the group's unit
+    auto put = [&](int kb, float2 y) { xc[wfft_slot_l<L>(kb, j, wfft_col_swizzle<C>(kb, c))] = y; };
+    auto get = [&](int h, int jj) {
+      const int kb = j + L * h;
+      return xc[wfft_slot_l<L>(kb, jj, wfft_col_swizzle<C>(kb, c))];
+    };
+    wfft_stage1<R, -1>(v, tw, put);
+    group_sync(bar, 128);
+    wfft_stage2<R, -1, L>(v, get);
+    group_sync(bar, 128);  // every lane has read its rows before the inverse stores
+    const float2 hx = a.hx[x0 + c];
+    wfft_stage1<R, 1>(v, tw, put, [&](int q, float2 y) {
+      const int K = 2 * (j + L * q) + g;  // frequency of element j + L q of this half
+      return cmul(y, cmul(hys[K <= H ? K : N - K], hx));
+    });
+    group_sync(bar, 128);
+    wfft_stage2<R, 1, L>(v, get);
+    if (g == 1) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q] = cmul(v[q], cconj(__ldg(a.tw + L * q + j)));
+    }
+    group_sync(bar, 128);  // the group's exchange has been read: its unit takes the half's result
+#pragma unroll
+    for (int q = 0; q < R; ++q) own[(L * q + j) * C + c] = v[q];
+    __syncthreads();
+    const float2* other = g == 0 ? bot : top;
+    if (g == 0) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q] = cadd(v[q], other[(L * q + j) * C + c]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q] = csub(other[(L * q + j) * C + c], v[q]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();  // both units read: the next units may land in them
+    if (tid == 0) {
+      if (u0 + S < n_units) load(u0 + S);
+      if (u1 + S < n_units) load(u1 + S);
+    }
+    float2* f = a.field + (size_t)r * N * N + (size_t)g * H * N + x0 + c;
+#pragma unroll
+    for (int q = 0; q < R; ++q) f[(size_t)(L * q + j) * N] = v[q];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // no copy may land after the CTA leaves: a load issued and never waited for (the loop left early)
+    for (int st = 0; st < S; ++st)
+      if (n_issued[st] > n_consumed[st]) pass_mbar_wait(fbar(st), (uint32_t)(n_consumed[st] & 1));
+  }
+}
+
+static cudaError_t col_wsplit_launch(int B, const ColArgs& a, cudaStream_t st) {
+  using Cfg = ColSplit;
+  alignas(128) CUtensorMap map;
+  if (!encode_field_tiles(&map, a.field, Cfg::N, B, Cfg::C, Cfg::BOX_ROWS)) return cudaErrorNotSupported;
+  static LaunchCache cache;
+  int grid_max = 0;
+  cudaError_t e = cache.get(col_pass_wsplit_kernel, 256, Cfg::SMEM, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_tiles = B * (Cfg::N / Cfg::C);
+  const int grid = std::max(1, std::min(n_tiles, grid_max));
+  col_pass_wsplit_kernel<<<grid, 256, Cfg::SMEM, st>>>(map, a, n_tiles);
+  return cudaGetLastError();
+}
+
 template <int N, int C, int TWREC>
 static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
   static LaunchCache cache;
@@ -2097,6 +2289,15 @@ cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t 
     if (N == 2048) return col_wfft_launch<2048, 1>(B, a, st);
     if (N == 4096) return col_wfft_launch<4096, 1>(B, a, st);  // 64-lane transforms, tiles of 2 columns
     return cudaErrorInvalidValue;
+  }
+  if (a.variant == 14) {
+    // N = 4096: two 2048-point warp FFTs per column (radix-2 split), tiles of 4 columns; an inverse-only
+    // pass (FFT screens) takes the radix-16 TMA form
+    if (N != 4096 || !aligned16(a.field)) return cudaErrorInvalidValue;
+    if (!a.inv_only) return col_wsplit_launch(B, a, st);
+    ColArgs b = a;
+    b.variant = 3;
+    return col_dispatch<4096>(col_tile_default(N), B, b, st);
   }
   if (C <= 0) C = col_tile_default(N);
   switch (N) {

@@ -358,12 +358,14 @@ def test_product_twiddle_column_pass_matches_oracle(torch_cuda):
     assert o.rel_l2(field.cpu().numpy()[0], u) < FIELD_TOL
 
 
-@pytest.mark.parametrize("N,variants,R", [(1024, (11, 4, 10), 3), (2048, (11, 4, 10), 3), (4096, (4, 4, 10), 2)])
+@pytest.mark.parametrize("N,variants,R", [(1024, (11, 4, 10), 3), (2048, (11, 4, 10), 3), (4096, (4, 4, 10), 2),
+                                         (4096, (4, 4, 14), 2)])
 def test_warp_fft_passes_match_oracle(torch_cuda, N, variants, R):
     """The warp-FFT forms (row variant 11 at 1024 and 2048; column variant 10,
-    with 64-lane transforms at 4096) keep the FP64 parity bound on fields and
-    measures, for batches of several realisations (the column pass's two
-    groups on neighbouring tiles), and through atm_vacuum on the same plan."""
+    with 64-lane transforms at 4096; column variant 14 at 4096, two 2048-point
+    halves per column) keep the FP64 parity bound on fields and measures, for
+    batches of several realisations (the column pass's two groups on
+    neighbouring tiles), and through atm_vacuum on the same plan."""
     torch = torch_cuda
     spec = o.ChannelSpec(N=N, delta=3.0 / N, w0=0.1, length=20e3, count=4, Cn2=1e-15, pupil_radius=0.15)
     plan, base = make_plan(spec, batch=R)
