@@ -1998,19 +1998,20 @@ static cudaError_t col_wfft_launch(int B, const ColArgs& a, cudaStream_t st) {
 //   each group transforms its half (forward; H = hy[K] hx applied as the
 //        inverse gathers its inputs, K = 2 k + g; inverse), exchanging
 //        through its own unit (group 0 the top one, group 1 the bottom one);
-//   out: group 1 scales its inverse by W_N^-n, both write their halves back
-//        into their units, and the top rows are E[n] + O[n], the bottom rows
-//        E[n] - O[n]; they are stored from registers (8 rows x 4 columns per
-//        store instruction) once both units have been read, while the CTA's
-//        next units load into them.
+//   out: once group 0's inverse has read its exchange, the top unit takes
+//        the next tile's second unit; group 1 writes its inverse, scaled by
+//        W_N^-n, into the bottom unit; group 0 keeps the top rows E[n] + O[n]
+//        and writes the bottom rows E[n] - O[n] over O[n], which group 1 then
+//        reads (and the bottom unit takes the unit after next); both store
+//        from registers (8 rows x 4 columns per store instruction).
 // hy is symmetric in the unshifted order (hy[K] = hy[N - K], the frequencies
 // of K and N - K have the same square): the CTA stages hy[0..N/2] (16 KB), so
 // that three units, the W_2048 table and hy fit in one CTA's shared memory.
-// Tile t takes units 2t and 2t + 1 (stages (2t) % 3 and (2t + 1) % 3); once
-// tile t has been read the CTA loads units 2t + 3 and 2t + 4 into the same
-// stages, so the next tile's first unit is in flight during a tile's
-// transforms.  Every wait is bounded (error word, then a drain of the copies
-// in flight).
+// Tile t takes units 2t and 2t + 1 (stages (2t) % 3 and (2t + 1) % 3) and
+// loads units 2t + 3 and 2t + 4 into the same stages as they are freed, so
+// the next tile's first unit is in flight during a tile's transforms and its
+// second during the combine and the stores.  Every wait is bounded (error
+// word, then a drain of the copies in flight).
 // ---------------------------------------------------------------------------
 struct ColSplit {
   static constexpr int N = 4096;
@@ -2129,27 +2130,32 @@ col_pass_wsplit_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
     });
     group_sync(bar, 128);
     wfft_stage2<R, 1, L>(v, get);
-    if (g == 1) {
-#pragma unroll
-      for (int q = 0; q < R; ++q) v[q] = cmul(v[q], cconj(__ldg(a.tw + L * q + j)));
-    }
-    group_sync(bar, 128);  // the group's exchange has been read: its unit takes the half's result
-#pragma unroll
-    for (int q = 0; q < R; ++q) own[(L * q + j) * C + c] = v[q];
-    __syncthreads();
-    const float2* other = g == 0 ? bot : top;
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    group_sync(bar, 128);  // the group's exchange has been read
     if (g == 0) {
-#pragma unroll
-      for (int q = 0; q < R; ++q) v[q] = cadd(v[q], other[(L * q + j) * C + c]);
+      // the top unit is free: the next tile's second unit loads into it during the combine
+      if (gt == 0 && u0 + S < n_units) load(u0 + S);
     } else {
 #pragma unroll
-      for (int q = 0; q < R; ++q) v[q] = csub(other[(L * q + j) * C + c], v[q]);
+      for (int q = 0; q < R; ++q) bot[(L * q + j) * C + c] = cmul(v[q], cconj(__ldg(a.tw + L * q + j)));
     }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();  // both units read: the next units may land in them
-    if (tid == 0) {
-      if (u0 + S < n_units) load(u0 + S);
-      if (u1 + S < n_units) load(u1 + S);
+    __syncthreads();  // O[n] = W_N^-n (odd half's inverse) in the bottom unit
+    if (g == 0) {
+      // E[n] + O[n] stays in registers (top rows), E[n] - O[n] replaces O[n] (bottom rows)
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const float2 o = bot[(L * q + j) * C + c];
+        bot[(L * q + j) * C + c] = csub(v[q], o);
+        v[q] = cadd(v[q], o);
+      }
+    }
+    __syncthreads();  // the bottom rows in the bottom unit
+    if (g == 1) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q] = bot[(L * q + j) * C + c];
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      group_sync(bar, 128);  // the bottom unit has been read: the unit after next loads into it
+      if (gt == 0 && u1 + S < n_units) load(u1 + S);
     }
     float2* f = a.field + (size_t)r * N * N + (size_t)g * H * N + x0 + c;
 #pragma unroll
