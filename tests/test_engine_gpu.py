@@ -390,3 +390,11 @@ def test_warp_fft_passes_match_oracle(torch_cuda, N, variants, R):
     for r in range(2):
         assert o.rel_l2(dev[r].cpu().numpy(), ref) < FIELD_TOL
     plan.close()
+
+
+def test_sizes_tool_runs(torch_cuda, capsys):
+    """python -m pyatmosphere_gb300.engine.sizes: per-kernel times at one grid size."""
+    from pyatmosphere_gb300.engine import sizes
+    assert sizes.main(["--N", "256", "--batch", "2", "--warmup", "1", "--runs", "1", "--variants", "3,4,3"]) == 0
+    out = capsys.readouterr().out
+    assert "row_pass" in out and "col_pass" in out and "GB/s" in out
