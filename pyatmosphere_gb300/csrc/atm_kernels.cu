@@ -2001,9 +2001,10 @@ static cudaError_t col_wfft_launch(int B, const ColArgs& a, cudaStream_t st) {
 //   out: once group 0's inverse has read its exchange, the top unit takes
 //        the next tile's second unit; group 1 writes its inverse, scaled by
 //        W_N^-n, into the bottom unit; group 0 keeps the top rows E[n] + O[n]
-//        and writes the bottom rows E[n] - O[n] over O[n], which group 1 then
-//        reads (and the bottom unit takes the unit after next); both store
-//        from registers (8 rows x 4 columns per store instruction).
+//        and writes the bottom rows E[n] - O[n] over O[n]; it stores the top
+//        rows from registers (8 rows x 4 columns per store instruction), while
+//        the bottom rows leave the bottom unit by tensor stores, after which
+//        the unit takes the unit after next.
 // hy is symmetric in the unshifted order (hy[K] = hy[N - K], the frequencies
 // of K and N - K have the same square): the CTA stages hy[0..N/2] (16 KB), so
 // that three units, the W_2048 table and hy fit in one CTA's shared memory.
@@ -2148,19 +2149,29 @@ col_pass_wsplit_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
         bot[(L * q + j) * C + c] = csub(v[q], o);
         v[q] = cadd(v[q], o);
       }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the bottom rows, for the tensor stores
     }
     __syncthreads();  // the bottom rows in the bottom unit
-    if (g == 1) {
+    if (g == 0) {
+      float2* f = a.field + (size_t)r * N * N + x0 + c;
 #pragma unroll
-      for (int q = 0; q < R; ++q) v[q] = bot[(L * q + j) * C + c];
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      group_sync(bar, 128);  // the bottom unit has been read: the unit after next loads into it
-      if (gt == 0 && u1 + S < n_units) load(u1 + S);
+      for (int q = 0; q < R; ++q) f[(size_t)(L * q + j) * N] = v[q];
+    } else if (gt == 0) {
+      // the bottom rows leave by tensor stores; once they have read the unit, the unit after next
+      // loads into it
+      const uint32_t src = (uint32_t)__cvta_generic_to_shared(bot);
+#pragma unroll 1
+      for (int b = 0; b < Cfg::BOXES; ++b)
+        tma_store_col(&tiles, src + (uint32_t)(b * Cfg::BOX_ROWS * C * sizeof(float2)), 2 * x0,
+                      H + b * Cfg::BOX_ROWS, r);
+      asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+      if (u1 + S < n_units) {
+        asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+        load(u1 + S);
+      }
     }
-    float2* f = a.field + (size_t)r * N * N + (size_t)g * H * N + x0 + c;
-#pragma unroll
-    for (int q = 0; q < R; ++q) f[(size_t)(L * q + j) * N] = v[q];
   }
+  if (tid == 128) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");  // its tensor stores are done
   __syncthreads();
   if (tid == 0) {
     // no copy may land after the CTA leaves: a load issued and never waited for (the loop left early)
