@@ -1994,7 +1994,10 @@ static cudaError_t col_wfft_launch(int B, const ColArgs& a, cudaStream_t st) {
 // the same tile:
 //   in:  group 0 forms a[n] + b[n], group 1 (a[n] - b[n]) W_N^n (n < 2048; a
 //        the top rows, b the bottom rows); the 2048-point transforms of these
-//        are the even and the odd frequencies of the 4096-point transform;
+//        are the even and the odd frequencies of the 4096-point transform.
+//        Group 0 also forms the first MT of group 1's inputs (into the bottom
+//        unit), so that the two groups reach the barrier after the split
+//        together;
 //   each group transforms its half (forward; H = hy[K] hx applied as the
 //        inverse gathers its inputs, K = 2 k + g; inverse), exchanging
 //        through its own unit (group 0 the top one, group 1 the bottom one);
@@ -2024,7 +2027,9 @@ struct ColSplit {
   static constexpr size_t HY = (((size_t)H + 1) * sizeof(float2) + 127) / 128 * 128;  // hy[0..H]
   static constexpr size_t SMEM = 128 + S * UNIT + TWT + HY;
   static constexpr int BOX_ROWS = 256, BOXES = H / BOX_ROWS;
+  static constexpr int MT = 20;  // odd-half inputs group 0 forms at the split (balances the groups' work)
   static_assert(SMEM <= 227 * 1024, "stages exceed shared memory");
+  static_assert(MT < R, "group 1 forms at least one of its inputs");
 };
 
 __global__ void __launch_bounds__(256, 1)
@@ -2103,16 +2108,27 @@ col_pass_wsplit_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
     const int r = item / NCT, x0 = (item - r * NCT) * C;
     float2* top = unit_ptr(s0);
     float2* bot = unit_ptr(s1);
+    auto row = [&](int m) { return (L * m + j) * C + c; };  // row j + L m of column c in a unit
     float2 v[R];
     if (g == 0) {
+      // the even half's inputs, and the first MT of the odd half's (twiddled) into the bottom unit, so
+      // that the two groups' split takes about the same time
 #pragma unroll
-      for (int m = 0; m < R; ++m) v[m] = cadd(top[(L * m + j) * C + c], bot[(L * m + j) * C + c]);
+      for (int m = 0; m < R; ++m) {
+        const float2 x = top[row(m)], y = bot[row(m)];
+        v[m] = cadd(x, y);
+        if (m < Cfg::MT) bot[row(m)] = cmul(csub(x, y), __ldg(a.tw + L * m + j));
+      }
     } else {
 #pragma unroll
-      for (int m = 0; m < R; ++m)
-        v[m] = cmul(csub(top[(L * m + j) * C + c], bot[(L * m + j) * C + c]), __ldg(a.tw + L * m + j));
+      for (int m = Cfg::MT; m < R; ++m) v[m] = cmul(csub(top[row(m)], bot[row(m)]), __ldg(a.tw + L * m + j));
     }
     __syncthreads();  // both units read: the groups' exchanges overwrite them
+    if (g == 1) {
+#pragma unroll
+      for (int m = 0; m < Cfg::MT; ++m) v[m] = bot[row(m)];
+      group_sync(bar, 128);  // before the exchange overwrites them
+    }
     float2* own = g == 0 ? top : bot;
     float2* xc = own + c * H;  // column c's exchange rows in the group's unit
     auto put = [&](int kb, float2 y) { xc[wfft_slot_l<L>(kb, j, wfft_col_swizzle<C>(kb, c))] = y; };
@@ -2137,16 +2153,17 @@ col_pass_wsplit_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
       // the top unit is free: the next tile's second unit loads into it during the combine
       if (gt == 0 && u0 + S < n_units) load(u0 + S);
     } else {
+      // (group 1's exchange lives in the bottom unit: only group 1 writes it before the barrier)
 #pragma unroll
-      for (int q = 0; q < R; ++q) bot[(L * q + j) * C + c] = cmul(v[q], cconj(__ldg(a.tw + L * q + j)));
+      for (int q = 0; q < R; ++q) bot[row(q)] = cmul(v[q], cconj(__ldg(a.tw + L * q + j)));
     }
     __syncthreads();  // O[n] = W_N^-n (odd half's inverse) in the bottom unit
     if (g == 0) {
       // E[n] + O[n] stays in registers (top rows), E[n] - O[n] replaces O[n] (bottom rows)
 #pragma unroll
       for (int q = 0; q < R; ++q) {
-        const float2 o = bot[(L * q + j) * C + c];
-        bot[(L * q + j) * C + c] = csub(v[q], o);
+        const float2 o = bot[row(q)];
+        bot[row(q)] = csub(v[q], o);
         v[q] = cadd(v[q], o);
       }
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the bottom rows, for the tensor stores
