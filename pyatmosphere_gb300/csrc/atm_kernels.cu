@@ -2089,8 +2089,9 @@ col_pass_wsplit_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int
   for (int t = 0; t < n_t; ++t) {
     const int u0 = 2 * t, u1 = u0 + 1;
     const int s0 = u0 % S, s1 = u1 % S;
-    // a unit's load is issued (after the previous use of its stage was read) before the CTA barrier
-    // that ends the previous tile, so each wait is on the phase of the stage's current use
+    // unit u's load is issued during an earlier tile (units 2t + 3 and 2t + 4 during tile t, once the
+    // previous use of their stage has been read), before the barrier that starts tile t + 1, so
+    // each wait is on the phase of the stage's current use
     const bool ok = pass_mbar_wait(fbar(s0), (uint32_t)((u0 / S) & 1), wait_ns) &&
                     pass_mbar_wait(fbar(s1), (uint32_t)((u1 / S) & 1), wait_ns);
     if (!__syncthreads_and(ok)) {
