@@ -40,10 +40,11 @@ WORKLOAD_NAME = ("advanced channel: 2048^2 grid, delta 1.5 mm, 808 nm, w0 0.12 m
                  "5 SS screens x 1024 annuli, MVK Cn2 5e-16, pupil 0.2 m")
 
 
-# DRAM bytes (read + write) per launch and realisation of the default forms
-# (row pass 4, column pass 10), from ncu captures of 16-realisation runs of
-# this workload, averaged over the launches of a run (traffic grows with the
-# realisations); a fixed figure, not measured by this script.
+# DRAM bytes (read + write) per launch and realisation of the forms row pass 4
+# and column pass 10, from ncu captures of 16-realisation runs of this
+# workload, averaged over the launches of a run (traffic grows with the
+# realisations); a fixed figure, not measured by this script.  Column pass 15
+# (the split form) loads and stores the same 32-byte tile rows once.
 TRAFFIC_PER_REALISATION = {"row_pass": 66.98e6, "col_pass": 63.78e6, "screen_gemm": 25.98e6,
                            "screen_table": 8.24e6}
 

@@ -159,7 +159,11 @@ typedef struct AtmPlanInfo {
                                  14: N = 4096, column tile 4: each 4096-point column transform as two
                                      2048-point warp FFTs (a radix-2 split in y), one per group of
                                      four warps, on tiles of 4 columns held as two 2048-row units in
-                                     a ring of three; an inverse-only pass runs the form of 3 */
+                                     a ring of three; an inverse-only pass runs the form of 3,
+                                 15: N = 2048, column tile 4: the split of 14 with 1024-point halves
+                                     (32 elements per lane, 16 warps per SM), two pairs of groups
+                                     per CTA sharing a ring of six 1024-row units; an inverse-only
+                                     pass runs the form of 10 */
   int32_t tuned;              /* 1 after a successful atm_autotune */
   int32_t gemm_form;          /* screen GEMM: 0 FP32 SIMT, 1 tcgen05 cp.async form, 2 tcgen05 persistent TMA
                                  form with 128 x 128 tiles (ATM_FLAG_TC_N128), 3 the same with 128 x 256
@@ -369,7 +373,7 @@ int atm_structure_function(const float* phi, int32_t batch, int32_t N, double* s
 /* Sets the launch choices atm_autotune makes by hand: row-pass variant 0..4
  * or 7, column tile 2/4/8/16 with at most 512 threads per CTA, column-pass
  * variant 0..4 or 7; at N = 1024 and 2048 also row 11, and at N = 1024, 2048
- * and 4096 column 10 and at N = 4096 column 14 (recorded with column tile 4),
+ * and 4096 column 10, at N = 4096 column 14 and at N = 2048 column 15 (recorded with column tile 4),
  * the warp-FFT forms; a tiled plan (ATM_FLAG_TILED) takes row
  * 5, 6, 8, 9 or 10, column tile 4 and column 5, 6, 8 or 9 (and 13 at N = 1024
  * and 2048).  Results do not

@@ -1155,6 +1155,7 @@ int atm_autotune(AtmPlan* pl, int32_t batch, int32_t repeats, void* stream) {
   std::vector<int> warp_cols;
   if (!pl->tiled && col_warp) warp_cols.push_back(10);
   if (!pl->tiled && N == 4096) warp_cols.push_back(14);
+  if (!pl->tiled && N == 2048) warp_cols.push_back(15);
   for (int v : warp_cols) {
     ca.variant = v;
     const double ms = time_it([&] { return atm::launch_col_pass(N, batch, 4, ca, st); });
@@ -1199,17 +1200,17 @@ int atm_plan_set_variants(AtmPlan* pl, int32_t row_variant, int32_t col_tile, in
   const bool col_warp = warp_fft || pl->N == 4096;         // column 10: warp FFTs
   if (row_variant < 0 || (row_variant > 4 && row_variant != 7 && !(row_variant == 11 && warp_fft)))
     return fail(ATM_ERR_INVALID, "row_variant %d not in 0..4, 7%s", row_variant, warp_fft ? " or 11" : "");
-  const bool split = pl->N == 4096;                        // column 14: two 2048-point halves per column
+  const int split = pl->N == 4096 ? 14 : (pl->N == 2048 ? 15 : -1);  // two half-length warp FFTs per column
   if (col_variant < 0 ||
-      (col_variant > 4 && col_variant != 7 && !(col_variant == 10 && col_warp) && !(col_variant == 14 && split)))
-    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4, 7%s", col_variant,
-                split ? ", 10 or 14" : (col_warp ? " or 10" : ""));
-  if ((col_variant == 10 || col_variant == 14) && col_tile != 4)
+      (col_variant > 4 && col_variant != 7 && !(col_variant == 10 && col_warp) && col_variant != split))
+    return fail(ATM_ERR_INVALID, "col_variant %d not in 0..4, 7%s%s", col_variant, col_warp ? ", 10" : "",
+                split == 14 ? " or 14" : (split == 15 ? " or 15" : ""));
+  if ((col_variant == 10 || col_variant == 14 || col_variant == 15) && col_tile != 4)
     return fail(ATM_ERR_INVALID, "col_variant %d takes col_tile 4", col_variant);
   if (col_tile != 2 && col_tile != 4 && col_tile != 8 && col_tile != 16)
     return fail(ATM_ERR_INVALID, "col_tile %d not in {2, 4, 8, 16}", col_tile);
   // (the warp-FFT column groups are 256 threads whatever the recorded tile)
-  if (col_variant != 10 && col_variant != 14 && (col_tile * (pl->N / 16) > 512 || col_tile > pl->N))
+  if (col_variant != 10 && col_variant != 14 && col_variant != 15 && (col_tile * (pl->N / 16) > 512 || col_tile > pl->N))
     return fail(ATM_ERR_UNSUPPORTED, "col_tile %d exceeds 512 threads per CTA at N = %d", col_tile, pl->N);
   pl->row_variant = row_variant;
   pl->col_tile = col_tile;

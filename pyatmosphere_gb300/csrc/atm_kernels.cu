@@ -2212,6 +2212,218 @@ static cudaError_t col_wsplit_launch(int B, const ColArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// column pass at N = 2048 with the radix-2 split of the 4096 form above:
+// each 2048-point column transform as two 1024-point warp FFTs (32 elements
+// per lane), which leaves a lane 128 registers, so that 16 warps fit on an
+// SM instead of 8.  Four groups of four warps form two pairs; pair p works on
+// the CTA's tiles t = p, p + 2, ... (neighbouring tiles, as in the 2048-point
+// groups), each tile of 4 columns x 2048 rows held as two 32 KB units (its
+// top and bottom 1024 rows) in a ring of six unit stages that the pairs share:
+// unit u = 2t + h goes to stage u % 6, and once it has been read its stage
+// takes unit u + 6 (the other pair's tile t + 3).  Within a pair the steps
+// are those of the 4096 form, on the pair's named barrier instead of the
+// CTA's.  A consumer waits first on its stage's `issued` mbarrier, then on
+// its `full` one (the load of unit u - 6 was issued by its own pair, so the
+// parity it waits on is never two phases old).  Every wait is bounded.
+// ---------------------------------------------------------------------------
+struct ColSplit2 {
+  static constexpr int N = 2048;
+  static constexpr int H = N / 2;                                 // rows of a unit, length of the halves' FFTs
+  static constexpr int L = 32, C = 4, RW = 8, R = H / L;          // 32 elements per lane
+  static constexpr int S = 6;                                     // unit stages shared by the two pairs
+  static constexpr int MT = 10;                                   // odd-half inputs group h = 0 forms at the split
+  static constexpr size_t UNIT = (size_t)H * C * sizeof(float2);  // 32 KB
+  static constexpr size_t TWT = (size_t)R * L * sizeof(float2);   // W_H^(j kb) per lane j
+  static constexpr size_t HY = (((size_t)H + 1) * sizeof(float2) + 127) / 128 * 128;  // hy[0..H]
+  static constexpr size_t SMEM = 128 + S * UNIT + TWT + HY;
+  static constexpr int BOX_ROWS = 256, BOXES = H / BOX_ROWS;
+  static_assert(SMEM <= 227 * 1024, "stages exceed shared memory");
+  static_assert(MT < R, "group h = 1 forms at least one of its inputs");
+};
+
+__global__ void __launch_bounds__(512, 1)
+col_pass_wsplit2_kernel(const __grid_constant__ CUtensorMap tiles, ColArgs a, int n_tiles) {
+  using Cfg = ColSplit2;
+  constexpr int N = Cfg::N, H = Cfg::H, R = Cfg::R, L = Cfg::L, C = Cfg::C, S = Cfg::S;
+  constexpr int NCT = N / C;  // tiles per realisation
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[S], issued_bar[S];
+  __shared__ int n_issued[S], n_consumed[S];  // loads issued / waited for, per stage
+  const int tid = threadIdx.x;
+  const int g = tid >> 7, gt = tid & 127;    // group of four warps
+  const int p = g >> 1, h = g & 1, pt = tid & 255;  // pair, half (0: even frequencies, top rows), thread in pair
+  const int w = gt >> 5, lane = tid & 31;
+  const int a4 = lane / C, c = lane % C;
+  const int j = Cfg::RW * w + a4;  // lane of column c's transforms
+  const int gbar = 1 + g, pbar = 5 + p;
+  unsigned char* sbase = smem_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
+  float2* twt = reinterpret_cast<float2*>(sbase + (size_t)S * Cfg::UNIT);
+  float2* hys = twt + Cfg::TWT / sizeof(float2);
+  for (int i = tid; i < R * L; i += blockDim.x) twt[i] = a.tw[2 * (i / L) * (i % L)];  // W_H^k = W_N^2k; < N
+  for (int i = tid; i <= H; i += blockDim.x) hys[i] = a.hy[i];
+  // the CTA's tiles: pairs of neighbouring tiles, item(t) = 2 (blockIdx.x + (t / 2) gridDim.x) + t % 2
+  const int n_pairs = n_tiles / 2;
+  const int n_t = (int)blockIdx.x < n_pairs ? 2 * ((n_pairs - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) : 0;
+  const int n_units = 2 * n_t;
+  auto item_of = [&](int t) { return 2 * ((int)blockIdx.x + (t >> 1) * (int)gridDim.x) + (t & 1); };
+  auto unit_ptr = [&](int st) { return reinterpret_cast<float2*>(sbase + (size_t)st * Cfg::UNIT); };
+  auto bar_addr = [&](uint64_t* b, int st) { return (uint32_t)__cvta_generic_to_shared(&b[st]); };
+  auto load = [&](int u) {  // unit u (tile u / 2, half u % 2) into stage u % 6, by one thread
+    const int st = u % S;
+    const int item = item_of(u >> 1);
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
+    const uint32_t fb = bar_addr(full_bar, st);
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(unit_ptr(st));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"((uint32_t)Cfg::UNIT)
+                 : "memory");
+#pragma unroll 1
+    for (int b = 0; b < Cfg::BOXES; ++b)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+          "[%5];\n" ::"r"(dst + (uint32_t)(b * Cfg::BOX_ROWS * C * sizeof(float2))),
+          "l"(reinterpret_cast<uint64_t>(&tiles)), "r"(2 * x0), "r"((u & 1) * H + b * Cfg::BOX_ROWS), "r"(r),
+          "r"(fb)
+          : "memory");
+    n_issued[st] += 1;
+    mbar_arrive_cta(bar_addr(issued_bar, st));
+  };
+  if (tid == 0) {
+    for (int st = 0; st < S; ++st) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_addr(full_bar, st)) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_addr(issued_bar, st)) : "memory");
+      n_issued[st] = 0;
+      n_consumed[st] = 0;
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    for (int u = 0; u < S && u < n_units; ++u) load(u);
+  }
+  __syncthreads();
+  const unsigned long long wait_ns = g_pass_wait_ns;
+  auto tw = [&](int kb) { return twt[kb * L + j]; };
+  for (int t = p; t < n_t; t += 2) {
+    const int u0 = 2 * t, u1 = u0 + 1;
+    const int s0 = u0 % S, s1 = u1 % S;
+    const uint32_t ph0 = (uint32_t)((u0 / S) & 1), ph1 = (uint32_t)((u1 / S) & 1);
+    const bool ok = pass_mbar_wait(bar_addr(issued_bar, s0), ph0, wait_ns) &&
+                    pass_mbar_wait(bar_addr(full_bar, s0), ph0, wait_ns) &&
+                    pass_mbar_wait(bar_addr(issued_bar, s1), ph1, wait_ns) &&
+                    pass_mbar_wait(bar_addr(full_bar, s1), ph1, wait_ns);
+    if (!group_all(pbar, 256, ok)) {
+      if (pt == 0) {
+        atomicExch(&g_pass_error, 1);
+        if (a.status) atomicOr(a.status, STATUS_PASS_WAIT);
+      }
+      break;
+    }
+    if (pt == 0) {
+      n_consumed[s0] = u0 / S + 1;
+      n_consumed[s1] = u1 / S + 1;
+    }
+    const int item = item_of(t);
+    const int r = item / NCT, x0 = (item - r * NCT) * C;
+    float2* top = unit_ptr(s0);
+    float2* bot = unit_ptr(s1);
+    auto row = [&](int m) { return (L * m + j) * C + c; };  // row j + L m of column c in a unit
+    float2 v[R];
+    if (h == 0) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) {
+        const float2 x = top[row(m)], y = bot[row(m)];
+        v[m] = cadd(x, y);
+        if (m < Cfg::MT) bot[row(m)] = cmul(csub(x, y), __ldg(a.tw + L * m + j));
+      }
+    } else {
+#pragma unroll
+      for (int m = Cfg::MT; m < R; ++m) v[m] = cmul(csub(top[row(m)], bot[row(m)]), __ldg(a.tw + L * m + j));
+    }
+    group_sync(pbar, 256);  // both units read: the pair's exchanges overwrite them
+    if (h == 1) {
+#pragma unroll
+      for (int m = 0; m < Cfg::MT; ++m) v[m] = bot[row(m)];
+      group_sync(gbar, 128);  // before the exchange overwrites them
+    }
+    float2* own = h == 0 ? top : bot;
+    float2* xc = own + c * H;  // column c's exchange rows in the group's unit
+    auto put = [&](int kb, float2 y) { xc[wfft_slot_l<L>(kb, j, wfft_col_swizzle<C>(kb, c))] = y; };
+    auto get = [&](int hh, int jj) {
+      const int kb = j + L * hh;
+      return xc[wfft_slot_l<L>(kb, jj, wfft_col_swizzle<C>(kb, c))];
+    };
+    wfft_stage1<R, -1>(v, tw, put);
+    group_sync(gbar, 128);
+    wfft_stage2<R, -1, L>(v, get);
+    group_sync(gbar, 128);  // every lane has read its rows before the inverse stores
+    const float2 hx = a.hx[x0 + c];
+    wfft_stage1<R, 1>(v, tw, put, [&](int q, float2 y) {
+      const int K = 2 * (j + L * q) + h;  // frequency of element j + L q of this half
+      return cmul(y, cmul(hys[K <= H ? K : N - K], hx));
+    });
+    group_sync(gbar, 128);
+    wfft_stage2<R, 1, L>(v, get);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    group_sync(gbar, 128);  // the group's exchange has been read
+    if (h == 0) {
+      // the top unit is free: unit u0 + 6 (the other pair's tile t + 3) loads into it
+      if (gt == 0 && u0 + S < n_units) load(u0 + S);
+    } else {
+#pragma unroll
+      for (int q = 0; q < R; ++q) bot[row(q)] = cmul(v[q], cconj(__ldg(a.tw + L * q + j)));
+    }
+    group_sync(pbar, 256);  // O[n] = W_N^-n (odd half's inverse) in the bottom unit
+    if (h == 0) {
+      // E[n] + O[n] stays in registers (top rows), E[n] - O[n] replaces O[n] (bottom rows)
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const float2 o = bot[row(q)];
+        bot[row(q)] = csub(v[q], o);
+        v[q] = cadd(v[q], o);
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the bottom rows, for the tensor stores
+    }
+    group_sync(pbar, 256);  // the bottom rows in the bottom unit
+    if (h == 0) {
+      float2* f = a.field + (size_t)r * N * N + x0 + c;
+#pragma unroll
+      for (int q = 0; q < R; ++q) f[(size_t)(L * q + j) * N] = v[q];
+    } else if (gt == 0) {
+      // the bottom rows leave by tensor stores; once they have read the unit, unit u1 + 6 loads into it
+      const uint32_t src = (uint32_t)__cvta_generic_to_shared(bot);
+#pragma unroll 1
+      for (int b = 0; b < Cfg::BOXES; ++b)
+        tma_store_col(&tiles, src + (uint32_t)(b * Cfg::BOX_ROWS * C * sizeof(float2)), 2 * x0,
+                      H + b * Cfg::BOX_ROWS, r);
+      asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+      if (u1 + S < n_units) {
+        asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+        load(u1 + S);
+      }
+    }
+  }
+  if (h == 1 && gt == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");  // its tensor stores are done
+  __syncthreads();
+  if (tid == 0) {
+    // no copy may land after the CTA leaves: a load issued and never waited for (a pair left early)
+    for (int st = 0; st < S; ++st)
+      if (n_issued[st] > n_consumed[st])
+        pass_mbar_wait(bar_addr(full_bar, st), (uint32_t)(n_consumed[st] & 1));
+  }
+}
+
+static cudaError_t col_wsplit2_launch(int B, const ColArgs& a, cudaStream_t st) {
+  using Cfg = ColSplit2;
+  alignas(128) CUtensorMap map;
+  if (!encode_field_tiles(&map, a.field, Cfg::N, B, Cfg::C, Cfg::BOX_ROWS)) return cudaErrorNotSupported;
+  static LaunchCache cache;
+  int grid_max = 0;
+  cudaError_t e = cache.get(col_pass_wsplit2_kernel, 512, Cfg::SMEM, &grid_max);
+  if (e != cudaSuccess) return e;
+  const int n_tiles = B * (Cfg::N / Cfg::C);
+  const int grid = std::max(1, std::min(n_tiles / 2, grid_max));
+  col_pass_wsplit2_kernel<<<grid, 512, Cfg::SMEM, st>>>(map, a, n_tiles);
+  return cudaGetLastError();
+}
+
 template <int N, int C, int TWREC>
 static cudaError_t col_pipe_launch(int B, const ColArgs& a, cudaStream_t st) {
   static LaunchCache cache;
@@ -2324,6 +2536,13 @@ cudaError_t launch_col_pass(int N, int B, int C, const ColArgs& a, cudaStream_t 
     if (N == 2048) return col_wfft_launch<2048, 1>(B, a, st);
     if (N == 4096) return col_wfft_launch<4096, 1>(B, a, st);  // 64-lane transforms, tiles of 2 columns
     return cudaErrorInvalidValue;
+  }
+  if (a.variant == 15) {
+    // N = 2048: two 1024-point warp FFTs per column, two pairs of groups per CTA; an inverse-only pass
+    // (FFT screens) takes the warp-FFT column groups
+    if (N != 2048 || !aligned16(a.field)) return cudaErrorInvalidValue;
+    if (!a.inv_only) return col_wsplit2_launch(B, a, st);
+    return col_wfft_launch<2048, 1>(B, a, st);
   }
   if (a.variant == 14) {
     // N = 4096: two 2048-point warp FFTs per column (radix-2 split), tiles of 4 columns; an inverse-only

@@ -37,6 +37,7 @@ pytestmark = pytest.mark.gpu
 BENCH_SEED = 2024
 FORMS = [("row-major", 0, (4, 4, 4)), ("row-major", 0, (4, 4, 3)), ("row-major", 0, (7, 4, 7)),
          ("row-major", 0, (11, 4, 10)), ("row-major", 0, (11, 4, 7)), ("row-major", 0, (7, 4, 10)),
+         ("row-major", 0, (4, 4, 15)),
          ("tiled", 64, (6, 4, 6)), ("tiled", 64, (8, 4, 8)), ("tiled", 64, (6, 4, 9)), ("tiled", 64, (9, 4, 9)),
          ("tiled", 64, (9, 4, 13)), ("tiled", 64, (10, 4, 13))]
 

@@ -217,11 +217,13 @@ PRODUCT_COL = (2, 7)
 # the warp-FFT forms (N = 1024 and 2048; column tile 4): their own FP32 round-off
 WARP_ROW = (11,)
 WARP_COL = (10,)
+# the split column forms (two half-length warp FFTs per column; column tile 4): 15 at 2048, 14 at 4096
+SPLIT_COL = {2048: (15,), 4096: (14,)}
 
 
 def _forms(N):
     warp = N in (1024, 2048)
-    return ROW_FORMS + (WARP_ROW if warp else ()), COL_FORMS + (WARP_COL if warp else ())
+    return ROW_FORMS + (WARP_ROW if warp else ()), COL_FORMS + (WARP_COL if warp else ()) + SPLIT_COL.get(N, ())
 
 
 @pytest.mark.parametrize("N", [512, 2048])
@@ -241,21 +243,21 @@ def test_autotune_keeps_results(torch_cuda, N):
     row_forms, col_forms = _forms(N)
     assert choice["row_variant"] in row_forms and choice["col_variant"] in col_forms
     after = plan.run(*sp).cpu().numpy()
-    rounding = PRODUCT_COL + WARP_COL, PRODUCT_ROW + WARP_ROW
+    rounding = PRODUCT_COL + WARP_COL + (14, 15), PRODUCT_ROW + WARP_ROW
     if choice["col_variant"] in rounding[0] or choice["row_variant"] in rounding[1]:
         np.testing.assert_allclose(after, before, rtol=2e-5, atol=1e-9)
     else:
         np.testing.assert_array_equal(after, before)
     # every launch form computes the same arithmetic, except the product
     # twiddles (row variants 4 and 7, column variants 2 and 7) and the warp
-    # FFTs (row 11, column 10): FP32 round-off
+    # FFTs (row 11, columns 10 and 15): FP32 round-off
     product = {}
     for rv in row_forms:
         for ct in (2, 4, 8, 16):
             if ct * N // 16 > 512:
                 continue
             for cv in col_forms:
-                if cv in WARP_COL and ct != 4:
+                if cv in WARP_COL + (14, 15) and ct != 4:
                     continue
                 plan.set_variants(rv, ct, cv)
                 got = plan.run(*sp).cpu().numpy()
@@ -359,11 +361,11 @@ def test_product_twiddle_column_pass_matches_oracle(torch_cuda):
 
 
 @pytest.mark.parametrize("N,variants,R", [(1024, (11, 4, 10), 3), (2048, (11, 4, 10), 3), (4096, (4, 4, 10), 2),
-                                         (4096, (4, 4, 14), 2)])
+                                         (4096, (4, 4, 14), 2), (2048, (4, 4, 15), 3)])
 def test_warp_fft_passes_match_oracle(torch_cuda, N, variants, R):
     """The warp-FFT forms (row variant 11 at 1024 and 2048; column variant 10,
-    with 64-lane transforms at 4096; column variant 14 at 4096, two 2048-point
-    halves per column) keep the FP64 parity bound on fields and measures, for
+    with 64-lane transforms at 4096; column variants 14 at 4096 and 15 at 2048,
+    two half-length warp FFTs per column) keep the FP64 parity bound on fields and measures, for
     batches of several realisations (the column pass's two groups on
     neighbouring tiles), and through atm_vacuum on the same plan."""
     torch = torch_cuda

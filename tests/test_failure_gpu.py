@@ -41,7 +41,8 @@ def _setup(torch, N, flags=0, variants=None, R=2):
     return plan, [torch.from_numpy(a).cuda() for a in arrs]
 
 
-@pytest.mark.parametrize("form", ["row-major TMA forms", "tiled", "warp-FFT column groups", "4096 split columns"])
+@pytest.mark.parametrize("form", ["row-major TMA forms", "tiled", "warp-FFT column groups", "4096 split columns",
+                                  "2048 split columns"])
 def test_wait_budget_runs_out_then_recovers(torch_cuda, form):
     from pyatmosphere_gb300.engine import _lib
     from pyatmosphere_gb300.engine.plan import set_wait_budget
@@ -51,6 +52,9 @@ def test_wait_budget_runs_out_then_recovers(torch_cuda, form):
     elif form == "warp-FFT column groups":
         # column variant 10: two groups handing stages to each other through mbarriers
         plan, dev = _setup(torch, 1024, variants=(3, 4, 10))
+    elif form == "2048 split columns":
+        # column variant 15: two pairs of groups handing unit stages to each other through mbarriers
+        plan, dev = _setup(torch, 2048, variants=(3, 4, 15))
     elif form == "4096 split columns":
         # column variant 14: both groups on one tile of two units, CTA-wide handoffs
         plan, dev = _setup(torch, 4096, variants=(3, 4, 14))
