@@ -10,6 +10,9 @@
 //   row_pass      (inverse row FFT, exp(-i phi) multiply, forward row FFT)
 //   col_pass      (forward column FFT, H(fy,fx,dz), inverse column FFT)
 // and one last row_pass with the pupil / moment reductions, then finalize.
+// The FFT passes come in three families: radix-16 Stockham transforms over
+// thread groups, warp FFTs (one exchange per transform), and at 2048^2 and
+// 4096^2 column transforms split in y into two half-length warp FFTs.
 #include <cuda.h>  // CUtensorMap (the column pass's TMA form)
 
 #include <algorithm>
